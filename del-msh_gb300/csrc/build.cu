@@ -1,0 +1,463 @@
+// build.cu — LBVH build kernels: centroid AABB + fit transform, Morton codes
+// (with the radix sort's digit histogram fused in), Karras topology and the
+// bottom-up AABB refit.  All of them are HBM-bound integer / min-max work.
+#include <cfloat>
+
+#include "dm_device.cuh"
+#include "dm_internal.h"
+
+namespace dm {
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int grid_for(uint32_t n, int per_block, int max_blocks) {
+  const uint32_t b = (n + per_block - 1) / per_block;
+  return static_cast<int>(b < 1 ? 1 : (b > static_cast<uint32_t>(max_blocks) ? max_blocks : b));
+}
+
+// Vertex index checked against num_vtx (out of range -> vertex 0 + status).
+__device__ __forceinline__ uint32_t vtx_index(const uint32_t* __restrict__ p, uint32_t num_vtx, uint32_t* status) {
+  const uint32_t v = __ldg(p);
+  if (v < num_vtx) return v;
+  raise_status(status, kStatusBadIndex);
+  return 0u;
+}
+
+__device__ __forceinline__ float3 tri_centroid(const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
+                                               const float* __restrict__ vtx2xyz, uint32_t it, uint32_t* status) {
+  const uint32_t* t = tri2vtx + static_cast<size_t>(it) * 3;
+  const float3 p0 = load_vtx(vtx2xyz, vtx_index(t, num_vtx, status));
+  const float3 p1 = load_vtx(vtx2xyz, vtx_index(t + 1, num_vtx, status));
+  const float3 p2 = load_vtx(vtx2xyz, vtx_index(t + 2, num_vtx, status));
+  return make_float3(centroid1(p0.x, p1.x, p2.x), centroid1(p0.y, p1.y, p2.y), centroid1(p0.z, p1.z, p2.z));
+}
+
+// Reduction of (min, max) over 6 lanes-of-values held by each thread; NaN is
+// ignored because every comparison with NaN is false.
+struct MinMax {
+  float lo[3], hi[3];
+};
+
+__device__ __forceinline__ void mm_merge(MinMax& a, const MinMax& b) {
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    if (b.lo[d] < a.lo[d]) a.lo[d] = b.lo[d];
+    if (b.hi[d] > a.hi[d]) a.hi[d] = b.hi[d];
+  }
+}
+
+__device__ __forceinline__ MinMax block_reduce_mm(MinMax v, MinMax* sh /* [kThreads/32] */) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    MinMax o;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      o.lo[d] = __shfl_down_sync(0xffffffffu, v.lo[d], off);
+      o.hi[d] = __shfl_down_sync(0xffffffffu, v.hi[d], off);
+    }
+    mm_merge(v, o);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) sh[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    MinMax w;
+    if (lane < kThreads / 32) {
+      w = sh[lane];
+    } else {
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        w.lo[d] = INFINITY;
+        w.hi[d] = -INFINITY;
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      MinMax o;
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        o.lo[d] = __shfl_down_sync(0xffffffffu, w.lo[d], off);
+        o.hi[d] = __shfl_down_sync(0xffffffffu, w.hi[d], off);
+      }
+      mm_merge(w, o);
+    }
+    v = w;
+  }
+  return v;  // valid in thread 0
+}
+
+// vtx2xyz.rs:19-37 applied to the triangle centroids, then the fit transform
+// of Mat44/torch.py:120-140.  The sequential code seeds the box with the first
+// centroid and widens it with strict comparisons, so a component is NaN iff
+// the first centroid's is, and otherwise equals the min / max over the
+// non-NaN values (the max of c + 0).  A two-level reduction with a last-block
+// ticket computes exactly that.
+__global__ void __launch_bounds__(kThreads) k_centroid_aabb(uint32_t num_tri, const uint32_t* __restrict__ tri2vtx,
+                                                           uint32_t num_vtx, const float* __restrict__ vtx2xyz,
+                                                           float* partials, uint32_t* ticket, float* aabb_out,
+                                                           float* transform_out, uint32_t* status) {
+  __shared__ MinMax sh[kThreads / 32];
+  __shared__ bool s_last;
+  MinMax v;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    v.lo[d] = INFINITY;
+    v.hi[d] = -INFINITY;
+  }
+  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < num_tri; i += gridDim.x * kThreads) {
+    const float3 c = tri_centroid(tri2vtx, num_vtx, vtx2xyz, i, status);
+    const float cc[3] = {c.x, c.y, c.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      if (cc[d] < v.lo[d]) v.lo[d] = cc[d];
+      const float h = __fadd_rn(cc[d], 0.0f);
+      if (h > v.hi[d]) v.hi[d] = h;
+    }
+  }
+  v = block_reduce_mm(v, sh);
+  if (threadIdx.x == 0) {
+    float* p = partials + blockIdx.x * 6;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      p[d] = v.lo[d];
+      p[d + 3] = v.hi[d];
+    }
+    __threadfence();
+    s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    v.lo[d] = INFINITY;
+    v.hi[d] = -INFINITY;
+  }
+  for (uint32_t b = threadIdx.x; b < gridDim.x; b += kThreads) {
+    MinMax o;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      o.lo[d] = __ldcg(partials + b * 6 + d);
+      o.hi[d] = __ldcg(partials + b * 6 + 3 + d);
+    }
+    mm_merge(v, o);
+  }
+  __syncthreads();
+  v = block_reduce_mm(v, sh);
+  if (threadIdx.x == 0) {
+    const float3 c0 = tri_centroid(tri2vtx, num_vtx, vtx2xyz, 0, status);
+    const float c0a[3] = {c0.x, c0.y, c0.z};
+    float lo[3], hi[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const bool nan0 = c0a[d] != c0a[d];
+      lo[d] = nan0 ? c0a[d] : v.lo[d];
+      hi[d] = nan0 ? c0a[d] : v.hi[d];
+      if (aabb_out) {
+        aabb_out[d] = lo[d];
+        aabb_out[d + 3] = hi[d];
+      }
+    }
+    float ext = __fsub_rn(hi[0], lo[0]);
+    const float ey = __fsub_rn(hi[1], lo[1]), ez = __fsub_rn(hi[2], lo[2]);
+    if (ey > ext) ext = ey;
+    if (ez > ext) ext = ez;
+    const float s = __fdiv_rn(1.0f, ext);
+    float m[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) m[k] = 0.0f;
+    m[0] = s;
+    m[5] = s;
+    m[10] = s;
+    m[15] = 1.0f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float c = __fmul_rn(__fadd_rn(lo[d], hi[d]), 0.5f);
+      m[12 + d] = __fadd_rn(__fmul_rn(-c, s), 0.5f);
+    }
+#pragma unroll
+    for (int k = 0; k < 16; ++k) transform_out[k] = m[k];
+    *ticket = 0u;  // ready for the next launch
+  }
+}
+
+// Centroid -> transform_homogeneous -> morton_code3 per triangle
+// (bvhnodes_morton.rs:151-159 -> mortons.rs:115-138).  With kHist the four
+// 8-bit digit histograms of the codes are accumulated for the radix sort.
+template <bool kHist>
+__global__ void __launch_bounds__(kThreads) k_morton_tri(uint32_t num_tri, const uint32_t* __restrict__ tri2vtx,
+                                                        uint32_t num_vtx, const float* __restrict__ vtx2xyz,
+                                                        const float* __restrict__ transform,
+                                                        uint32_t* __restrict__ codes, uint32_t* __restrict__ hist,
+                                                        uint32_t* status) {
+  __shared__ float m[16];
+  __shared__ uint32_t sh[kHist ? 4 * kRadix : 1];
+  if (threadIdx.x < 16) m[threadIdx.x] = transform[threadIdx.x];
+  if (kHist)
+    for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads) sh[i] = 0;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < num_tri; i += gridDim.x * kThreads) {
+    const float3 c = tri_centroid(tri2vtx, num_vtx, vtx2xyz, i, status);
+    const float3 q = transform_homogeneous(m, c.x, c.y, c.z);
+    const uint32_t code = morton_code3(q.x, q.y, q.z);
+    codes[i] = code;
+    if (kHist) {
+#pragma unroll
+      for (int p = 0; p < 4; ++p) atomicAdd(&sh[p * kRadix + ((code >> (8 * p)) & 0xFFu)], 1u);
+    }
+  }
+  if (kHist) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads)
+      if (sh[i]) atomicAdd(hist + i, sh[i]);
+  }
+}
+
+// mortons.cu:8-37 (one code per point) with del-msh-cpu's clamping instead of
+// the device asserts (mortons.rs:171-212).
+__global__ void __launch_bounds__(kThreads) k_vtx2morton(uint32_t n, uint32_t num_dim, const float* __restrict__ vtx2co,
+                                                        const float* __restrict__ transform, uint32_t* __restrict__ out) {
+  __shared__ float m[16];
+  if (threadIdx.x < 16) m[threadIdx.x] = (threadIdx.x < num_dim * num_dim + 2 * num_dim + 1) ? transform[threadIdx.x] : 0.f;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    if (num_dim == 3) {
+      const float* p = vtx2co + static_cast<size_t>(i) * 3;
+      const float3 q = transform_homogeneous(m, __ldg(p), __ldg(p + 1), __ldg(p + 2));
+      out[i] = morton_code3(q.x, q.y, q.z);
+    } else {
+      const float* p = vtx2co + static_cast<size_t>(i) * 2;
+      const float2 q = transform_homogeneous2(m, __ldg(p), __ldg(p + 1));
+      out[i] = morton_code2(q.x, q.y);
+    }
+  }
+}
+
+// ----------------------------------------------------------------- topology
+
+__device__ __forceinline__ int delta_of(const uint32_t* __restrict__ c, uint32_t i, uint32_t j) {
+  return __clz(__ldg(c + i) ^ __ldg(c + j));
+}
+
+// Last index of the run of value v that contains position `from` (sorted c).
+// Equal to the linear scan of mortons.rs:235-245, found by galloping search.
+__device__ __forceinline__ uint32_t run_end(const uint32_t* __restrict__ c, uint32_t n, uint32_t from, uint32_t v) {
+  uint32_t lo = from;  // c[lo] == v
+  uint32_t step = 1;
+  uint32_t hi = n;     // first index known to differ (or n)
+  for (;;) {
+    const uint64_t probe = static_cast<uint64_t>(lo) + step;
+    if (probe >= n) break;
+    if (__ldg(c + probe) != v) {
+      hi = static_cast<uint32_t>(probe);
+      break;
+    }
+    lo = static_cast<uint32_t>(probe);
+    step <<= 1;
+  }
+  while (hi - lo > 1) {  // invariant: c[lo] == v, hi == n or c[hi] != v
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (__ldg(c + mid) == v) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// mortons.rs:221-288 (range) and 290-325 (split), bvhnodes_morton.rs:24-47.
+__global__ void __launch_bounds__(kThreads) k_topology(uint32_t n, const uint32_t* __restrict__ c,
+                                                      const uint32_t* __restrict__ idx2obj, uint32_t* bvhnodes) {
+  const uint32_t ib = blockIdx.x * kThreads + threadIdx.x;
+  if (ib >= n - 1) return;
+  uint32_t r0, r1;
+  if (ib == 0) {
+    r0 = 0;
+    r1 = n - 1;
+  } else {
+    const uint32_t mc0 = __ldg(c + ib - 1), mc1 = __ldg(c + ib), mc2 = __ldg(c + ib + 1);
+    if (mc0 == mc1 && mc1 == mc2) {
+      r0 = ib;
+      r1 = run_end(c, n, ib + 1, mc1);
+    } else {
+      const int dd = __clz(mc1 ^ mc2) - __clz(mc1 ^ mc0);
+      const int d = dd > 0 ? 1 : -1;
+      const int delta_min = __clz(mc1 ^ (d > 0 ? mc0 : mc2));
+      int64_t lmax = 2;
+      for (;;) {
+        const int64_t j = static_cast<int64_t>(ib) + lmax * d;
+        if (j < 0 || j >= static_cast<int64_t>(n)) break;
+        if (delta_of(c, ib, static_cast<uint32_t>(j)) <= delta_min) break;
+        lmax *= 2;
+      }
+      int64_t l = 0;
+      for (int64_t t = lmax / 2; t >= 1; t /= 2) {
+        const int64_t j = static_cast<int64_t>(ib) + (l + t) * d;
+        if (j >= 0 && j < static_cast<int64_t>(n) && delta_of(c, ib, static_cast<uint32_t>(j)) > delta_min) l += t;
+      }
+      const uint32_t j = static_cast<uint32_t>(static_cast<int64_t>(ib) + l * d);
+      r0 = ib <= j ? ib : j;
+      r1 = ib <= j ? j : ib;
+    }
+  }
+  // split
+  uint32_t isplit;
+  {
+    const uint32_t mc_start = __ldg(c + r0);
+    const int common = __clz(mc_start ^ __ldg(c + r1));
+    if (common == 32) {
+      isplit = r0;
+    } else {
+      isplit = r0;
+      uint32_t step = r1 - r0;
+      while (step > 1) {
+        step = (step + 1) / 2;
+        const uint32_t cand = isplit + step;
+        if (cand >= r1) continue;
+        if (__clz(mc_start ^ __ldg(c + cand)) > common) isplit = cand;
+      }
+    }
+  }
+  const uint32_t nb = n - 1;
+  uint32_t* me = bvhnodes + static_cast<size_t>(ib) * 3;
+  if (r0 == isplit) {
+    const uint32_t a = nb + isplit;
+    me[1] = a;
+    uint32_t* la = bvhnodes + static_cast<size_t>(a) * 3;
+    la[0] = ib;
+    la[1] = __ldg(idx2obj + isplit);
+    la[2] = kUMax;
+  } else {
+    me[1] = isplit;
+    bvhnodes[static_cast<size_t>(isplit) * 3] = ib;
+  }
+  if (r1 == isplit + 1) {
+    const uint32_t b = nb + isplit + 1;
+    me[2] = b;
+    uint32_t* lb = bvhnodes + static_cast<size_t>(b) * 3;
+    lb[0] = ib;
+    lb[1] = __ldg(idx2obj + isplit + 1);
+    lb[2] = kUMax;
+  } else {
+    me[2] = isplit + 1;
+    bvhnodes[static_cast<size_t>(isplit + 1) * 3] = ib;
+  }
+  if (ib == 0) me[0] = kUMax;
+}
+
+// A single object: the one-leaf tree [MAX, obj, MAX] (the reference leaves
+// node 0 without children for n == 1).
+__global__ void k_topology_single(const uint32_t* __restrict__ idx2obj, uint32_t* bvhnodes) {
+  bvhnodes[0] = kUMax;
+  bvhnodes[1] = idx2obj[0];
+  bvhnodes[2] = kUMax;
+}
+
+// ------------------------------------------------------------------- refit
+
+__device__ __forceinline__ Box leaf_box(const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
+                                        const float* __restrict__ xyz, uint32_t it, uint32_t* status) {
+  const uint32_t* t = tri2vtx + static_cast<size_t>(it) * 3;
+  Box b;
+  box_set(b, load_vtx(xyz, vtx_index(t, num_vtx, status)), 0.0f);
+  box_add(b, load_vtx(xyz, vtx_index(t + 1, num_vtx, status)), 0.0f);
+  box_add(b, load_vtx(xyz, vtx_index(t + 2, num_vtx, status)), 0.0f);
+  return b;
+}
+
+// One thread per leaf; each branch is merged by the second child to arrive
+// (atomic arrival counter per branch, bvhnode2aabb.cu:7-65), always as
+// from_two_aabbs(child0, child1).  The arrival word also carries the height
+// of the first-arriving subtree, so the climb yields the tree height for free,
+// and the second arriver clears the word so the flags stay zero between calls.
+__global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint32_t* __restrict__ bvhnodes,
+                                                   const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
+                                                   const float* __restrict__ vtx2xyz0,
+                                                   const float* __restrict__ vtx2xyz1, float* aabb, uint32_t* flags,
+                                                   uint32_t* height_out, uint32_t* status) {
+  const uint32_t ii = blockIdx.x * kThreads + threadIdx.x;
+  if (ii >= num_tri) return;
+  const uint32_t num_node = 2 * num_tri - 1;
+  const uint32_t leaf = num_tri - 1 + ii;
+  const uint32_t it = __ldg(bvhnodes + static_cast<size_t>(leaf) * 3 + 1);
+  if (it >= num_tri) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  Box b = leaf_box(tri2vtx, num_vtx, vtx2xyz0, it, status);
+  if (vtx2xyz1) b = box_union(b, leaf_box(tri2vtx, num_vtx, vtx2xyz1, it, status));
+  box_store(aabb + static_cast<size_t>(leaf) * 6, b);
+  uint32_t h = 1;
+  uint32_t node = __ldg(bvhnodes + static_cast<size_t>(leaf) * 3);
+  uint32_t guard = 0;
+  while (node != kUMax) {
+    if (node >= num_tri - 1 || ++guard > num_node) {
+      raise_status(status, kStatusBadIndex);
+      return;
+    }
+    __threadfence();
+    const uint32_t old = atomicAdd(flags + node, h);
+    if (old == 0u) return;  // the sibling subtree is not finished yet
+    flags[node] = 0u;
+    __threadfence();
+    h = (old > h ? old : h) + 1;
+    const uint32_t c0 = __ldg(bvhnodes + static_cast<size_t>(node) * 3 + 1);
+    const uint32_t c1 = __ldg(bvhnodes + static_cast<size_t>(node) * 3 + 2);
+    if (c0 >= num_node || c1 >= num_node) {
+      raise_status(status, kStatusBadIndex);
+      return;
+    }
+    const Box u = box_union(box_load_cg(aabb + static_cast<size_t>(c0) * 6), box_load_cg(aabb + static_cast<size_t>(c1) * 6));
+    box_store(aabb + static_cast<size_t>(node) * 6, u);
+    node = __ldg(bvhnodes + static_cast<size_t>(node) * 3);
+  }
+  if (height_out) *height_out = h;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------- launchers
+
+void launch_centroid_aabb(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                          const float* vtx2xyz, float* partials, uint32_t* ticket, float* aabb_out,
+                          float* transform_out, uint32_t* status) {
+  const int grid = grid_for(num_tri, kThreads * 8, kAabbBlocks);
+  k_centroid_aabb<<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, partials, ticket, aabb_out,
+                                            transform_out, status);
+}
+
+void launch_morton_tri(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                       const float* vtx2xyz, const float* transform, uint32_t* codes, uint32_t* hist,
+                       uint32_t* status) {
+  const int grid = grid_for(num_tri, kThreads * 8, 152 * 16);
+  if (hist)
+    k_morton_tri<true><<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status);
+  else
+    k_morton_tri<false><<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, transform, codes, nullptr,
+                                                  status);
+}
+
+void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float* vtx2co, const float* transform,
+                       uint32_t* out) {
+  const int grid = grid_for(n, kThreads * 4, 152 * 16);
+  k_vtx2morton<<<grid, kThreads, 0, s>>>(n, num_dim, vtx2co, transform, out);
+}
+
+void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, const uint32_t* idx2obj,
+                     uint32_t* bvhnodes) {
+  if (n == 1) {
+    k_topology_single<<<1, 1, 0, s>>>(idx2obj, bvhnodes);
+    return;
+  }
+  const uint32_t grid = (n - 1 + kThreads - 1) / kThreads;
+  k_topology<<<grid, kThreads, 0, s>>>(n, idx2morton, idx2obj, bvhnodes);
+}
+
+void launch_refit(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,
+                  uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
+                  uint32_t* height_out, uint32_t* status) {
+  const uint32_t grid = (num_tri + kThreads - 1) / kThreads;
+  k_refit<<<grid, kThreads, 0, s>>>(num_tri, bvhnodes, tri2vtx, num_vtx, vtx2xyz0, vtx2xyz1, aabb, flags, height_out,
+                                    status);
+}
+
+}  // namespace dm

@@ -1,0 +1,352 @@
+// capi.cu — the library's C ABI (include/delmsh_gb300.h): argument checks,
+// scratch layout, and the launch sequences of the LBVH build and ray cast.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "../../include/delmsh_gb300.h"
+#include "dm_device.cuh"
+#include "dm_internal.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return fail(DM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define DM_CUDA(call)                                       \
+  do {                                                      \
+    const cudaError_t e_ = (call);                          \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call);     \
+  } while (0)
+
+#define DM_REQUIRE(cond, ...) \
+  do {                        \
+    if (!(cond)) return fail(DM_ERR_INVALID_ARGUMENT, __VA_ARGS__); \
+  } while (0)
+
+constexpr uint32_t kMaxElems = (1u << 30) - 1;  // sort look-back packs counts in 30 bits
+
+// Device status word: kernels OR error bits into it (see dm::DeviceStatusBits).
+__device__ uint32_t g_status_word;
+
+uint32_t* status_ptr() {
+  static std::mutex mu;
+  static uint32_t* cache[64] = {nullptr};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!cache[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_status_word) != cudaSuccess) return nullptr;
+    cache[dev] = static_cast<uint32_t*>(p);
+  }
+  return cache[dev];
+}
+
+inline size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Temporary device memory: the caller's, or stream-ordered allocation.
+struct Scratch {
+  void* ptr = nullptr;
+  cudaStream_t stream = nullptr;
+  bool owned = false;
+  ~Scratch() {
+    if (owned && ptr) cudaFreeAsync(ptr, stream);
+  }
+  int acquire(void* user, size_t user_bytes, size_t need, cudaStream_t s, bool* fresh) {
+    stream = s;
+    if (user) {
+      if (user_bytes < need)
+        return fail(DM_ERR_SCRATCH_TOO_SMALL, "scratch of %zu bytes is smaller than the %zu bytes needed", user_bytes,
+                    need);
+      if (reinterpret_cast<uintptr_t>(user) % 256 != 0) return fail(DM_ERR_INVALID_ARGUMENT, "scratch must be 256-byte aligned");
+      ptr = user;
+      if (fresh) *fresh = false;
+      return DM_OK;
+    }
+    const cudaError_t e = cudaMallocAsync(&ptr, need, s);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(scratch)");
+    owned = true;
+    if (fresh) *fresh = true;
+    return DM_OK;
+  }
+};
+
+inline cudaStream_t as_stream(uint64_t p) { return reinterpret_cast<cudaStream_t>(static_cast<uintptr_t>(p)); }
+
+// ------------------------------------------------------------ sort layout
+// [header: hist 8*256 u32 | tile counters 16 u32][lookback][keys tmp][vals tmp]
+struct SortLayout {
+  size_t hist = 0, counters = 0, lookback = 0, keys = 0, vals = 0, zero_bytes = 0, total = 0;
+};
+
+SortLayout sort_layout(uint32_t n, int num_pass, size_t key_bytes) {
+  SortLayout L;
+  L.hist = 0;
+  L.counters = 8 * 256 * 4;
+  L.lookback = align256(L.counters + 16 * 4);
+  L.zero_bytes = L.lookback + align256(dm::sort_lookback_words(n, num_pass) * 4);
+  L.keys = L.zero_bytes;
+  L.vals = L.keys + align256(static_cast<size_t>(n) * key_bytes);
+  L.total = L.vals + align256(static_cast<size_t>(n) * 4);
+  return L;
+}
+
+// -------------------------------------------------------- build layout
+struct BuildLayout {
+  size_t transform, aabb, ticket, height, sort_hdr, partials, codes, akeys, avals, bvals, flags, total, zero_bytes,
+      sort_bytes;
+  SortLayout sort;
+};
+
+BuildLayout build_layout(uint32_t T) {
+  BuildLayout L{};
+  L.transform = 0;
+  L.aabb = 64;
+  L.ticket = 96;
+  L.height = 100;
+  L.sort_hdr = 256;
+  L.sort = sort_layout(T, 4, 4);
+  L.sort_bytes = L.sort.zero_bytes;  // header + lookback (the tmp arrays are carved separately)
+  L.zero_bytes = L.sort_hdr + L.sort_bytes;
+  L.partials = align256(L.zero_bytes);
+  L.codes = L.partials + align256(dm::kAabbBlocks * 6 * 4);
+  L.akeys = L.codes + align256(static_cast<size_t>(T) * 4);
+  L.avals = L.akeys + align256(static_cast<size_t>(T) * 4);
+  L.bvals = L.avals + align256(static_cast<size_t>(T) * 4);
+  L.flags = L.bvals + align256(static_cast<size_t>(T) * 4);
+  L.total = L.flags + align256(static_cast<size_t>(T) * 4);
+  return L;
+}
+
+template <typename T>
+T* at(void* base, size_t off) {
+  return reinterpret_cast<T*>(static_cast<char*>(base) + off);
+}
+
+int check_mesh(uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz) {
+  DM_REQUIRE(num_tri >= 1, "num_tri must be >= 1 (got %u)", num_tri);
+  DM_REQUIRE(num_tri <= kMaxElems, "num_tri %u exceeds the supported maximum %u", num_tri, kMaxElems);
+  DM_REQUIRE(num_vtx >= 1, "num_vtx must be >= 1");
+  DM_REQUIRE(tri2vtx && vtx2xyz, "tri2vtx / vtx2xyz must not be NULL");
+  return DM_OK;
+}
+
+// The four onesweep passes over 30- or 32-bit keys: (k0, iota) -> A -> B -> A -> out.
+void sort4(cudaStream_t s, uint32_t n, const uint32_t* k0, uint32_t* ak, uint32_t* av, uint32_t* bk, uint32_t* bv,
+           uint32_t* ok, uint32_t* ov, uint32_t* hist, uint32_t* counters, uint32_t* lookback, uint32_t* status) {
+  const size_t lbw = dm::sort_lookback_words(n, 1);
+  dm::launch_onesweep_u32(s, n, 0, k0, nullptr, ak, av, hist, lookback, counters, status);
+  dm::launch_onesweep_u32(s, n, 8, ak, av, bk, bv, hist + 256, lookback + lbw, counters + 1, status);
+  dm::launch_onesweep_u32(s, n, 16, bk, bv, ak, av, hist + 512, lookback + 2 * lbw, counters + 2, status);
+  dm::launch_onesweep_u32(s, n, 24, ak, av, ok, ov, hist + 768, lookback + 3 * lbw, counters + 3, status);
+}
+
+int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz,
+               uint32_t* bvhnodes, float* aabb, float* transform_out, uint32_t* tri2morton_out, uint32_t* idx2tri_out,
+               uint32_t* idx2morton_out, uint32_t* height_out, void* scratch, size_t scratch_bytes) {
+  if (int e = check_mesh(T, tri2vtx, num_vtx, vtx2xyz)) return e;
+  DM_REQUIRE(bvhnodes && aabb, "bvhnodes / bvhnode2aabb must not be NULL");
+  cudaStream_t s = as_stream(stream_ptr);
+  const BuildLayout L = build_layout(T);
+  Scratch sc;
+  if (int e = sc.acquire(scratch, scratch_bytes, L.total, s, nullptr)) return e;
+  void* base = sc.ptr;
+  uint32_t* status = status_ptr();
+  DM_CUDA(cudaMemsetAsync(base, 0, L.zero_bytes, s));
+  DM_CUDA(cudaMemsetAsync(at<char>(base, L.flags), 0, static_cast<size_t>(T) * 4, s));
+  float* transform = at<float>(base, L.transform);
+  uint32_t* hist = at<uint32_t>(base, L.sort_hdr + L.sort.hist);
+  uint32_t* counters = at<uint32_t>(base, L.sort_hdr + L.sort.counters);
+  uint32_t* lookback = at<uint32_t>(base, L.sort_hdr + L.sort.lookback);
+  uint32_t* codes = at<uint32_t>(base, L.codes);
+  uint32_t* ak = at<uint32_t>(base, L.akeys);
+  uint32_t* av = at<uint32_t>(base, L.avals);
+  uint32_t* bv = at<uint32_t>(base, L.bvals);
+  uint32_t* flags = at<uint32_t>(base, L.flags);
+  uint32_t* height = at<uint32_t>(base, L.height);
+
+  dm::launch_centroid_aabb(s, T, tri2vtx, num_vtx, vtx2xyz, at<float>(base, L.partials),
+                           at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status);
+  dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status);
+  if (tri2morton_out) DM_CUDA(cudaMemcpyAsync(tri2morton_out, codes, size_t{4} * T, cudaMemcpyDeviceToDevice, s));
+  // codes -> (ak, av) -> (codes, bv) -> (ak, av) -> (ok, ov): the codes are
+  // dead after pass 0, so they hold the pass-1 keys and, by default, the final
+  // sorted keys; pass 3 only reads (ak, av).
+  uint32_t* ok = idx2morton_out ? idx2morton_out : codes;
+  uint32_t* ov = idx2tri_out ? idx2tri_out : bv;
+  sort4(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
+  dm::launch_topology(s, T, ok, ov, bvhnodes);
+  dm::launch_refit(s, T, bvhnodes, tri2vtx, num_vtx, vtx2xyz, nullptr, aabb, flags, height, status);
+  if (transform_out) DM_CUDA(cudaMemcpyAsync(transform_out, transform, 64, cudaMemcpyDeviceToDevice, s));
+  if (height_out) DM_CUDA(cudaMemcpyAsync(height_out, height, 4, cudaMemcpyDeviceToDevice, s));
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dm_version(void) { return "delmsh_gb300 0.1.0 (sm_103a)"; }
+
+const char* dm_last_error(void) { return g_last_error.c_str(); }
+
+int dm_device_status(uint32_t* bits, int clear) {
+  uint32_t* p = status_ptr();
+  if (!p) return fail(DM_ERR_CUDA, "device status word unavailable");
+  DM_CUDA(cudaDeviceSynchronize());
+  uint32_t v = 0;
+  DM_CUDA(cudaMemcpy(&v, p, 4, cudaMemcpyDeviceToHost));
+  if (clear) DM_CUDA(cudaMemset(p, 0, 4));
+  if (bits) *bits = v;
+  return DM_OK;
+}
+
+int dm_mortons_vtx2morton_from_vtx2co(uint64_t stream_ptr, uint32_t num_vtx, uint32_t num_dim, const float* vtx2co,
+                                      const float* transform_co2unit, uint32_t* vtx2morton) {
+  DM_REQUIRE(num_dim == 2 || num_dim == 3, "num_dim must be 2 or 3 (got %u)", num_dim);
+  DM_REQUIRE(transform_co2unit && vtx2morton && (vtx2co || num_vtx == 0), "NULL argument");
+  if (num_vtx == 0) return DM_OK;
+  dm::launch_vtx2morton(as_stream(stream_ptr), num_vtx, num_dim, vtx2co, transform_co2unit, vtx2morton);
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+size_t dm_array1d_argsort_scratch_bytes(uint32_t n) { return sort_layout(n, 4, 4).total; }
+
+int dm_array1d_argsort(uint64_t stream_ptr, uint32_t n, uint32_t* idx2val, uint32_t* jdx2idx, void* scratch,
+                       size_t scratch_bytes) {
+  DM_REQUIRE(n <= kMaxElems, "n %u exceeds the supported maximum %u", n, kMaxElems);
+  if (n == 0) return DM_OK;
+  DM_REQUIRE(idx2val && jdx2idx, "NULL argument");
+  cudaStream_t s = as_stream(stream_ptr);
+  const SortLayout L = sort_layout(n, 4, 4);
+  Scratch sc;
+  if (int e = sc.acquire(scratch, scratch_bytes, L.total, s, nullptr)) return e;
+  void* base = sc.ptr;
+  DM_CUDA(cudaMemsetAsync(base, 0, L.zero_bytes, s));
+  uint32_t* hist = at<uint32_t>(base, L.hist);
+  uint32_t* tk = at<uint32_t>(base, L.keys);
+  uint32_t* tv = at<uint32_t>(base, L.vals);
+  dm::launch_digit_hist_u32(s, n, idx2val, 4, hist);
+  sort4(s, n, idx2val, tk, tv, idx2val, jdx2idx, idx2val, jdx2idx, hist, at<uint32_t>(base, L.counters),
+        at<uint32_t>(base, L.lookback), status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+int dm_mortons_make_bvhnodes_from_sorted_mortons(uint64_t stream_ptr, uint32_t n, const uint32_t* idx2obj,
+                                                 const uint32_t* idx2morton, uint32_t* bvhnodes) {
+  DM_REQUIRE(n >= 1, "n must be >= 1");
+  DM_REQUIRE(n <= kMaxElems, "n %u exceeds the supported maximum %u", n, kMaxElems);
+  DM_REQUIRE(idx2obj && idx2morton && bvhnodes, "NULL argument");
+  dm::launch_topology(as_stream(stream_ptr), n, idx2morton, idx2obj, bvhnodes);
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+int dm_bvhnode2aabb_update_aabb(uint64_t stream_ptr, uint32_t num_bvhnode, float* bvhnode2aabb, uint32_t i_bvhnode,
+                                const uint32_t* bvhnodes, uint32_t num_elem, const uint32_t* elem2vtx,
+                                uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1,
+                                uint32_t* flags_scratch) {
+  if (int e = check_mesh(num_elem, elem2vtx, num_vtx, vtx2xyz0)) return e;
+  DM_REQUIRE(num_bvhnode == 2 * num_elem - 1, "num_bvhnode (%u) must be 2*num_elem-1 (%u)", num_bvhnode,
+             2 * num_elem - 1);
+  DM_REQUIRE(i_bvhnode == 0, "only i_bvhnode == 0 (the whole tree) is supported");
+  DM_REQUIRE(bvhnode2aabb && bvhnodes, "NULL argument");
+  cudaStream_t s = as_stream(stream_ptr);
+  Scratch sc;
+  uint32_t* flags = flags_scratch;
+  if (!flags) {
+    bool fresh = false;
+    if (int e = sc.acquire(nullptr, 0, align256(size_t{4} * num_elem), s, &fresh)) return e;
+    flags = static_cast<uint32_t*>(sc.ptr);
+    DM_CUDA(cudaMemsetAsync(flags, 0, size_t{4} * num_elem, s));
+  }
+  dm::launch_refit(s, num_elem, bvhnodes, elem2vtx, num_vtx, vtx2xyz0, vtx2xyz1, bvhnode2aabb, flags, nullptr,
+                   status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+size_t dm_trimesh3_build_scratch_bytes(uint32_t num_tri) { return build_layout(num_tri).total; }
+
+int dm_trimesh3_make_bvhnodes_bvhnode2aabb(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* tri2vtx,
+                                           uint32_t num_vtx, const float* vtx2xyz, uint32_t* bvhnodes,
+                                           float* bvhnode2aabb, void* scratch, size_t scratch_bytes) {
+  return build_impl(stream_ptr, num_tri, tri2vtx, num_vtx, vtx2xyz, bvhnodes, bvhnode2aabb, nullptr, nullptr, nullptr,
+                    nullptr, nullptr, scratch, scratch_bytes);
+}
+
+int dm_trimesh3_build_ex(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                         const float* vtx2xyz, uint32_t* bvhnodes, float* bvhnode2aabb, float* transform_out,
+                         uint32_t* tri2morton_out, uint32_t* idx2tri_out, uint32_t* idx2morton_out,
+                         uint32_t* height_out, void* scratch, size_t scratch_bytes) {
+  return build_impl(stream_ptr, num_tri, tri2vtx, num_vtx, vtx2xyz, bvhnodes, bvhnode2aabb, transform_out,
+                    tri2morton_out, idx2tri_out, idx2morton_out, height_out, scratch, scratch_bytes);
+}
+
+size_t dm_cast_scratch_bytes(uint32_t num_ray, uint32_t num_tri) { return dm::cast_scratch_bytes(num_ray, num_tri); }
+
+int dm_pix2tri_by_raycast(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, uint32_t* pix2tri, float* pix2t,
+                          uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz,
+                          const uint32_t* bvhnodes, const float* bvhnode2aabb, const float* transform_ndc2world,
+                          void* scratch, size_t scratch_bytes) {
+  if (int e = check_mesh(num_tri, tri2vtx, num_vtx, vtx2xyz)) return e;
+  DM_REQUIRE(bvhnodes && bvhnode2aabb && transform_ndc2world && pix2tri, "NULL argument");
+  const uint64_t num_pix = static_cast<uint64_t>(img_w) * img_h;
+  DM_REQUIRE(num_pix <= kMaxElems, "image of %llu pixels exceeds the supported maximum", (unsigned long long)num_pix);
+  if (num_pix == 0) return DM_OK;
+  cudaStream_t s = as_stream(stream_ptr);
+  const uint32_t n = static_cast<uint32_t>(num_pix);
+  Scratch sc;
+  if (int e = sc.acquire(scratch, scratch_bytes, dm::cast_scratch_bytes(n, num_tri), s, nullptr)) return e;
+  dm::CastScratch cs;
+  dm::cast_scratch_carve(sc.ptr, n, num_tri, &cs);
+  DM_CUDA(cudaMemsetAsync(cs.counters, 0, 8, s));
+  dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb};
+  dm::CastOut o{pix2tri, pix2t, nullptr};
+  dm::launch_cast_pixels(s, img_w, img_h, transform_ndc2world, m, o, cs, status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+int dm_search_bvh3_first_intersection_ray(uint64_t stream_ptr, uint32_t num_ray, const float* ray_org,
+                                          const float* ray_dir, uint32_t* hit_tri, float* hit_t, float* hit_bc,
+                                          uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                                          const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb,
+                                          void* scratch, size_t scratch_bytes) {
+  if (int e = check_mesh(num_tri, tri2vtx, num_vtx, vtx2xyz)) return e;
+  DM_REQUIRE(num_ray <= kMaxElems, "num_ray %u exceeds the supported maximum", num_ray);
+  if (num_ray == 0) return DM_OK;
+  DM_REQUIRE(ray_org && ray_dir && hit_tri && bvhnodes && bvhnode2aabb, "NULL argument");
+  cudaStream_t s = as_stream(stream_ptr);
+  Scratch sc;
+  if (int e = sc.acquire(scratch, scratch_bytes, dm::cast_scratch_bytes(num_ray, num_tri), s, nullptr)) return e;
+  dm::CastScratch cs;
+  dm::cast_scratch_carve(sc.ptr, num_ray, num_tri, &cs);
+  DM_CUDA(cudaMemsetAsync(cs.counters, 0, 8, s));
+  dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb};
+  dm::CastOut o{hit_tri, hit_t, hit_bc};
+  dm::launch_cast_rays(s, num_ray, ray_org, ray_dir, m, o, cs, status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+}  // extern "C"

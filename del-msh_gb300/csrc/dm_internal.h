@@ -1,0 +1,101 @@
+// dm_internal.h — host-side launchers shared between the library's
+// translation units.  Not part of the public C ABI (see include/delmsh_gb300.h).
+#pragma once
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace dm {
+
+// ---------------------------------------------------------------- build.cu
+constexpr int kAabbBlocks = 1024;  // upper bound on centroid-AABB reduction blocks
+
+// Centroid AABB (vtx2xyz.rs:19-37 over elem2center) and the fit transform
+// (16 floats, column-major).  partials: kAabbBlocks*6 floats; ticket: one u32
+// that is zero on entry and left zero.
+void launch_centroid_aabb(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                          const float* vtx2xyz, float* partials, uint32_t* ticket, float* aabb_out,
+                          float* transform_out, uint32_t* status);
+
+// Triangle-centroid Morton codes; when hist != nullptr also accumulates the
+// four 8-bit digit histograms (u32[4][256], zeroed by the caller).
+void launch_morton_tri(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                       const float* vtx2xyz, const float* transform, uint32_t* codes, uint32_t* hist,
+                       uint32_t* status);
+
+// mortons.cu:8-37 semantics with the CPU's clamping (num_dim 2 or 3).
+void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float* vtx2co, const float* transform,
+                       uint32_t* out);
+
+// bvhnodes_morton.rs:10-50 / bvhnodes_morton.cu:29-72.
+void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, const uint32_t* idx2obj,
+                     uint32_t* bvhnodes);
+
+// Vertex indices >= num_vtx are replaced by 0 and raise kStatusBadIndex.
+// Bottom-up refit (bvhnode2aabb.cu:7-65 semantics, values of
+// bvhnode2aabb3.rs:68-142).  flags: u32[num_tri-1], zero on entry, left zero.
+// height_out (optional): number of nodes on the longest root-to-leaf path.
+void launch_refit(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,
+                  uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags, uint32_t* height_out,
+                  uint32_t* status);
+
+// ----------------------------------------------------------------- sort.cu
+constexpr int kSortTile = 3840;  // keys per onesweep tile
+constexpr int kRadix = 256;
+
+inline uint32_t sort_num_tiles(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
+inline size_t sort_lookback_words(uint32_t n, int num_pass) {
+  return static_cast<size_t>(sort_num_tiles(n)) * kRadix * num_pass;
+}
+
+// Histogram of num_pass 8-bit digits of 32-bit keys (hist zeroed by caller).
+void launch_digit_hist_u32(cudaStream_t s, uint32_t n, const uint32_t* keys, int num_pass, uint32_t* hist);
+void launch_digit_hist_u64(cudaStream_t s, uint32_t n, const uint64_t* keys, int num_pass, uint32_t* hist);
+
+// One stable onesweep pass (digit at `shift`).  vals_in == nullptr means the
+// values are the input positions (iota).  lookback: sort_num_tiles(n)*256
+// words and tile_counter: 1 word, both zero on entry.
+void launch_onesweep_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in,
+                         const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
+                         uint32_t* lookback, uint32_t* tile_counter, uint32_t* status);
+void launch_onesweep_u64(cudaStream_t s, uint32_t n, uint32_t shift, const uint64_t* keys_in,
+                         const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
+                         uint32_t* lookback, uint32_t* tile_counter, uint32_t* status);
+
+// ----------------------------------------------------------------- cast.cu
+constexpr int kCastStack = 64;  // frames of the on-chip (local) traversal stack
+constexpr size_t kFrameBytes = 16;
+
+struct MeshView {
+  uint32_t num_tri;
+  uint32_t num_vtx;
+  const uint32_t* tri2vtx;
+  const float* vtx2xyz;
+  const uint32_t* bvhnodes;
+  const float* aabb;
+};
+
+struct CastOut {
+  uint32_t* hit_tri;  // u32 per ray (MAX = miss)
+  float* hit_t;       // optional
+  float* hit_bc;      // optional, 3 per ray (1-u-v, u, v)
+};
+
+struct CastScratch {
+  uint32_t* counters;  // 2 words, zero on entry (left zero)
+  uint32_t* list1;     // num_ray words
+  uint32_t* list2;     // num_ray words
+  void* pool;          // >= 16 * max(num_tri, 4096) bytes
+  size_t pool_bytes;
+};
+
+size_t cast_scratch_bytes(uint32_t num_ray, uint32_t num_tri);
+void cast_scratch_carve(void* base, uint32_t num_ray, uint32_t num_tri, CastScratch* out);
+
+// Pixels of an img_w x img_h image (ray_for_pixel.h) or explicit rays.
+void launch_cast_pixels(cudaStream_t s, uint32_t img_w, uint32_t img_h, const float* t_ndc2world, const MeshView& m,
+                        const CastOut& o, const CastScratch& sc, uint32_t* status);
+void launch_cast_rays(cudaStream_t s, uint32_t num_ray, const float* ray_org, const float* ray_dir,
+                      const MeshView& m, const CastOut& o, const CastScratch& sc, uint32_t* status);
+
+}  // namespace dm

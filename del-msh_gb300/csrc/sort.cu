@@ -1,0 +1,257 @@
+// sort.cu — stable LSD radix sort of (key, u32 value) pairs, onesweep style
+// (Adinets & Merrill, "Onesweep: A Faster Least Significant Digit Radix Sort
+// for GPUs", 2022): one upfront histogram of every digit, then one kernel per
+// 8-bit digit that ranks a tile with warp match/ballot operations, obtains its
+// global offsets through a decoupled look-back over preceding tiles, and
+// scatters through shared memory so that runs of equal digits are written
+// contiguously.  Stability (equal keys keep ascending input position) is what
+// makes the permutation equal to del-msh-cpu's `sort_by_key` over an iota
+// (mortons.rs:139-146).
+//
+// The look-back waits on flags written by tiles that started earlier (tile
+// ids are taken in launch order from an atomic counter), and every wait is
+// bounded: after kSpinLimit polls the kernel raises kStatusSpinTimeout and
+// carries on instead of hanging.
+#include "dm_device.cuh"
+#include "dm_internal.h"
+
+namespace dm {
+namespace {
+
+constexpr int kThreads = 256;  // == kRadix: thread d owns digit d in the per-digit steps
+constexpr int kWarps = kThreads / 32;
+constexpr int kKpt = kSortTile / kThreads;  // keys per thread (15)
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagInc = 2u << 30;
+constexpr uint32_t kValueMask = (1u << 30) - 1;
+constexpr uint32_t kSpinLimit = 1u << 22;
+static_assert(kThreads == kRadix, "one thread per digit");
+static_assert(kKpt * kThreads == kSortTile, "tile size");
+
+template <typename KeyT>
+__device__ __forceinline__ uint32_t digit_of(KeyT k, uint32_t shift) {
+  return static_cast<uint32_t>(k >> shift) & (kRadix - 1);
+}
+
+// Exclusive scan of one value per thread over the 256-thread block.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp /* kWarps */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < kWarps ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int off = 1; off < kWarps; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+      if (lane >= off) w += y;
+    }
+    if (lane < kWarps) s_warp[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  const uint32_t before = warp > 0 ? s_warp[warp - 1] : 0u;
+  const uint32_t r = before + x - v;
+  __syncthreads();  // s_warp may be reused right after
+  return r;
+}
+
+template <typename KeyT>
+struct SortSmem {
+  uint32_t whist[kWarps][kRadix];  // per-warp digit counts, then per-warp exclusive offsets
+  uint32_t gbase[kRadix];          // global start of each digit (upfront histogram scan)
+  uint32_t tstart[kRadix];         // start of each digit inside the tile
+  uint32_t excl[kRadix];           // this tile's offset inside each digit (look-back)
+  uint32_t scan[kWarps];
+  uint32_t tile;
+  KeyT keys[kSortTile];
+  uint32_t vals[kSortTile];
+};
+
+template <typename KeyT, bool kIota>
+__global__ void __launch_bounds__(kThreads) k_onesweep(const KeyT* __restrict__ keys_in,
+                                                      const uint32_t* __restrict__ vals_in, KeyT* __restrict__ keys_out,
+                                                      uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift,
+                                                      const uint32_t* __restrict__ hist, uint32_t* lookback,
+                                                      uint32_t* tile_counter, uint32_t* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SortSmem<KeyT>& S = *reinterpret_cast<SortSmem<KeyT>*>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  for (int i = tid; i < kWarps * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0u;
+  if (tid == 0) S.tile = atomicAdd(tile_counter, 1u);
+  const uint32_t gb = block_exclusive_scan(__ldg(hist + tid), S.scan);  // has __syncthreads
+  S.gbase[tid] = gb;
+  const uint32_t tile = S.tile;
+  const uint32_t tile_base = tile * kSortTile;
+  const uint32_t wbase = tile_base + static_cast<uint32_t>(warp) * 32u * kKpt;
+
+  // Load (warp-striped: key j of this lane is at wbase + 32*j + lane).
+  KeyT keys[kKpt];
+  uint32_t vals[kKpt];
+  uint32_t ranks[kKpt];
+#pragma unroll
+  for (int j = 0; j < kKpt; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    if (idx < n) {
+      keys[j] = keys_in[idx];
+      vals[j] = kIota ? idx : vals_in[idx];
+    } else {
+      keys[j] = 0;
+      vals[j] = 0;
+    }
+  }
+
+  // Rank inside the warp in (j, lane) order, i.e. input order.
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint32_t* my_hist = S.whist[warp];
+#pragma unroll
+  for (int j = 0; j < kKpt; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    const bool valid = idx < n;
+    const uint32_t d = valid ? digit_of(keys[j], shift) : static_cast<uint32_t>(kRadix);
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t before = valid ? my_hist[d] : 0u;
+    __syncwarp();
+    if (valid && lane == __ffs(peers) - 1) my_hist[d] = before + __popc(peers);
+    __syncwarp();
+    ranks[j] = before + __popc(peers & lt_mask);
+  }
+  __syncthreads();
+
+  // Thread d: per-warp exclusive offsets and the tile count of digit d.
+  const uint32_t d = tid;
+  uint32_t cnt = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) {
+    const uint32_t c = S.whist[w][d];
+    S.whist[w][d] = cnt;
+    cnt += c;
+  }
+
+  // Decoupled look-back for digit d.
+  volatile uint32_t* lb = lookback;
+  uint32_t excl = 0;
+  if (tile == 0) {
+    lb[d] = kFlagInc | cnt;
+  } else {
+    lb[static_cast<size_t>(tile) * kRadix + d] = kFlagAgg | cnt;
+    int64_t k = static_cast<int64_t>(tile) - 1;
+    uint32_t spins = 0;
+    while (k >= 0) {
+      const uint32_t v = lb[static_cast<size_t>(k) * kRadix + d];
+      const uint32_t flag = v & ~kValueMask;
+      if (flag == 0u) {
+        if (++spins > kSpinLimit) {
+          raise_status(status, kStatusSpinTimeout);
+          break;
+        }
+        __nanosleep(32);
+        continue;
+      }
+      excl += v & kValueMask;
+      if (flag == kFlagInc) break;
+      --k;
+    }
+    lb[static_cast<size_t>(tile) * kRadix + d] = kFlagInc | ((excl + cnt) & kValueMask);
+  }
+  S.excl[d] = excl;
+  const uint32_t ts = block_exclusive_scan(cnt, S.scan);  // has __syncthreads
+  S.tstart[d] = ts;
+  __syncthreads();
+
+  // Scatter into shared memory in (digit, input order).
+#pragma unroll
+  for (int j = 0; j < kKpt; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    if (idx < n) {
+      const uint32_t dg = digit_of(keys[j], shift);
+      const uint32_t pos = S.tstart[dg] + S.whist[warp][dg] + ranks[j];
+      S.keys[pos] = keys[j];
+      S.vals[pos] = vals[j];
+    }
+  }
+  __syncthreads();
+
+  // Write out: consecutive shared slots of one digit go to consecutive addresses.
+  const uint32_t tile_n = (n - tile_base) < static_cast<uint32_t>(kSortTile) ? (n - tile_base) : kSortTile;
+  for (uint32_t i = tid; i < tile_n; i += kThreads) {
+    const KeyT k = S.keys[i];
+    const uint32_t dg = digit_of(k, shift);
+    const uint32_t g = S.gbase[dg] + S.excl[dg] + (i - S.tstart[dg]);
+    if (g < n) {  // always true unless a look-back wait gave up (status already raised)
+      keys_out[g] = k;
+      vals_out[g] = S.vals[i];
+    }
+  }
+}
+
+template <typename KeyT>
+__global__ void __launch_bounds__(kThreads) k_digit_hist(uint32_t n, const KeyT* __restrict__ keys, int num_pass,
+                                                        uint32_t* __restrict__ hist) {
+  __shared__ uint32_t sh[8 * kRadix];
+  for (int i = threadIdx.x; i < num_pass * kRadix; i += kThreads) sh[i] = 0;
+  __syncthreads();
+  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < n; i += gridDim.x * kThreads) {
+    const KeyT k = keys[i];
+    for (int p = 0; p < num_pass; ++p) atomicAdd(&sh[p * kRadix + digit_of(k, 8u * p)], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < num_pass * kRadix; i += kThreads)
+    if (sh[i]) atomicAdd(hist + i, sh[i]);
+}
+
+template <typename KeyT>
+void onesweep(cudaStream_t s, uint32_t n, uint32_t shift, const KeyT* keys_in, const uint32_t* vals_in,
+              KeyT* keys_out, uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback, uint32_t* tile_counter,
+              uint32_t* status) {
+  if (n == 0) return;
+  const size_t smem = sizeof(SortSmem<KeyT>);
+  static bool configured[2] = {false, false};  // per instantiation pair; attribute is per function
+  if (!configured[0]) {
+    cudaFuncSetAttribute(k_onesweep<KeyT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaFuncSetAttribute(k_onesweep<KeyT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    configured[0] = true;
+  }
+  const uint32_t grid = sort_num_tiles(n);
+  if (vals_in == nullptr)
+    k_onesweep<KeyT, true><<<grid, kThreads, smem, s>>>(keys_in, nullptr, keys_out, vals_out, n, shift, hist, lookback,
+                                                         tile_counter, status);
+  else
+    k_onesweep<KeyT, false><<<grid, kThreads, smem, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, hist,
+                                                          lookback, tile_counter, status);
+}
+
+}  // namespace
+
+void launch_digit_hist_u32(cudaStream_t s, uint32_t n, const uint32_t* keys, int num_pass, uint32_t* hist) {
+  uint32_t grid = (n + kThreads * 16 - 1) / (kThreads * 16);
+  if (grid < 1) grid = 1;
+  if (grid > 152 * 8) grid = 152 * 8;
+  k_digit_hist<uint32_t><<<grid, kThreads, 0, s>>>(n, keys, num_pass, hist);
+}
+
+void launch_digit_hist_u64(cudaStream_t s, uint32_t n, const uint64_t* keys, int num_pass, uint32_t* hist) {
+  uint32_t grid = (n + kThreads * 16 - 1) / (kThreads * 16);
+  if (grid < 1) grid = 1;
+  if (grid > 152 * 8) grid = 152 * 8;
+  k_digit_hist<uint64_t><<<grid, kThreads, 0, s>>>(n, keys, num_pass, hist);
+}
+
+void launch_onesweep_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in,
+                         const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
+                         uint32_t* lookback, uint32_t* tile_counter, uint32_t* status) {
+  onesweep<uint32_t>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
+}
+
+void launch_onesweep_u64(cudaStream_t s, uint32_t n, uint32_t shift, const uint64_t* keys_in,
+                         const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
+                         uint32_t* lookback, uint32_t* tile_counter, uint32_t* status) {
+  onesweep<uint64_t>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
+}
+
+}  // namespace dm

@@ -1,0 +1,41 @@
+"""Per-pixel closest-hit triangle by BVH ray casting on CUDA tensors.
+
+Mirrors ``del_msh_dlpack/Pix2Tri/torch.py:8-61`` (by_raycasting).  Pixel
+(iw, ih) casts the ray of ray_for_pixel.h through ``transform_ndc2world``
+(row-major 4x4, transposed to column-major for the kernel as the reference
+does); hits follow del-msh-cpu's search_bvh3::first_intersection_ray.
+"""
+from __future__ import annotations
+
+from typing import Tuple
+
+import torch
+
+from .. import _native
+from ..util_torch import assert_shape_dtype_device, ptr, require_cuda, stream_ptr
+
+
+def by_raycasting(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor, bvhnodes: torch.Tensor, bvhnode2aabb: torch.Tensor,
+                  transform_ndc2world: torch.Tensor, img_shape: Tuple[int, int], return_depth: bool = False):
+    """Returns pix2tri (img_h, img_w) uint32 (u32::MAX where nothing is hit);
+    with return_depth also pix2t (img_h, img_w) float32, the ray coefficient of
+    the hit (+inf on a miss)."""
+    vtx2xyz = vtx2xyz.detach()
+    transform_ndc2world = transform_ndc2world.contiguous()
+    num_tri, num_vtx, num_bvhnode = tri2vtx.shape[0], vtx2xyz.shape[0], bvhnodes.shape[0]
+    device = tri2vtx.device
+    assert num_bvhnode == num_tri * 2 - 1
+    assert_shape_dtype_device(tri2vtx, (num_tri, 3), torch.uint32, device)
+    assert_shape_dtype_device(vtx2xyz, (num_vtx, 3), torch.float32, device)
+    assert_shape_dtype_device(bvhnodes, (num_bvhnode, 3), torch.uint32, device)
+    assert_shape_dtype_device(bvhnode2aabb, (num_bvhnode, 6), torch.float32, device)
+    assert_shape_dtype_device(transform_ndc2world, (4, 4), torch.float32, device)
+    require_cuda(device)
+    img_w, img_h = img_shape
+    pix2tri = torch.empty((img_h, img_w), dtype=torch.uint32, device=device)
+    pix2t = torch.empty((img_h, img_w), dtype=torch.float32, device=device) if return_depth else None
+    colmajor = transform_ndc2world.T.contiguous()
+    _native.call("dm_pix2tri_by_raycast", stream_ptr(device), img_w, img_h, ptr(pix2tri), ptr(pix2t), num_tri,
+                 ptr(tri2vtx.contiguous()), num_vtx, ptr(vtx2xyz.contiguous()), ptr(bvhnodes.contiguous()),
+                 ptr(bvhnode2aabb.contiguous()), ptr(colmajor), None, 0)
+    return (pix2tri, pix2t) if return_depth else pix2tri

@@ -1,0 +1,92 @@
+"""ctypes binding of ``libdelmsh_gb300.so`` (the C ABI in include/delmsh_gb300.h).
+
+There is no CPU fallback: if the library is missing or cannot be loaded the
+first call raises, naming the build step to run.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+u32, u64, f32p, u32p, vp, sz, i32 = C.c_uint32, C.c_uint64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_int
+
+_SIGNATURES = {
+    "dm_version": (C.c_char_p, []),
+    "dm_last_error": (C.c_char_p, []),
+    "dm_device_status": (i32, [C.POINTER(C.c_uint32), i32]),
+    "dm_mortons_vtx2morton_from_vtx2co": (i32, [u64, u32, u32, vp, vp, vp]),
+    "dm_array1d_argsort": (i32, [u64, u32, vp, vp, vp, sz]),
+    "dm_array1d_argsort_scratch_bytes": (sz, [u32]),
+    "dm_mortons_make_bvhnodes_from_sorted_mortons": (i32, [u64, u32, vp, vp, vp]),
+    "dm_bvhnode2aabb_update_aabb": (i32, [u64, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp]),
+    "dm_trimesh3_make_bvhnodes_bvhnode2aabb": (i32, [u64, u32, vp, u32, vp, vp, vp, vp, sz]),
+    "dm_trimesh3_build_scratch_bytes": (sz, [u32]),
+    "dm_trimesh3_build_ex": (i32, [u64, u32, vp, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, sz]),
+    "dm_pix2tri_by_raycast": (i32, [u64, u32, u32, vp, vp, u32, vp, u32, vp, vp, vp, vp, vp, sz]),
+    "dm_search_bvh3_first_intersection_ray": (i32, [u64, u32, vp, vp, vp, vp, vp, u32, vp, u32, vp, vp, vp, vp, sz]),
+    "dm_cast_scratch_bytes": (sz, [u32, u32]),
+}
+
+# entry points that return a status code
+STATUS_FUNCS = {k for k, (r, _) in _SIGNATURES.items() if r is i32 and k != "dm_device_status"}
+
+
+class DelMshError(RuntimeError):
+    """A non-zero status returned by the C ABI."""
+
+    def __init__(self, func: str, code: int, message: str):
+        super().__init__(f"{func} failed with status {code}: {message}")
+        self.code = code
+
+
+def lib_path():
+    return _build.LIB_PATH
+
+
+def load(build_if_missing: bool = False):
+    """Loads the library; with build_if_missing it first compiles it."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB_PATH
+        if not path.exists():
+            if build_if_missing:
+                _build.build()
+            else:
+                raise RuntimeError(f"{path} is missing: build it with `python -c \"import __graft_entry__ as g; "
+                                   f"g.build()\"` (or del_msh_gb300.build.build()); there is no CPU fallback")
+        L = C.CDLL(str(path))
+        for name, (res, args) in _SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return L
+
+
+def exported_symbols():
+    return sorted(_SIGNATURES)
+
+
+def call(name: str, *args):
+    """Calls a status-returning entry point and raises DelMshError on failure."""
+    L = load()
+    rc = getattr(L, name)(*args)
+    if rc != 0:
+        raise DelMshError(name, rc, L.dm_last_error().decode())
+    return rc
+
+
+def device_status(clear: bool = True) -> int:
+    L = load()
+    bits = C.c_uint32(0)
+    rc = L.dm_device_status(C.byref(bits), 1 if clear else 0)
+    if rc != 0:
+        raise DelMshError("dm_device_status", rc, L.dm_last_error().decode())
+    return bits.value

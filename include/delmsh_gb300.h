@@ -1,0 +1,153 @@
+/*
+ * delmsh_gb300.h — C ABI of the GB300 (sm_103a) LBVH build and BVH ray cast.
+ *
+ * Drop-in for del-msh's LBVH / ray-cast path: the same array layouts
+ *   tri2vtx      u32[num_tri*3]
+ *   vtx2xyz      f32[num_vtx*3]
+ *   bvhnodes     u32[(2*num_tri-1)*3]   [parent, left, right]; a leaf is
+ *                                        [parent, triangle, u32::MAX]; the root
+ *                                        is node 0 and its parent is u32::MAX;
+ *                                        branches are 0..T-2, leaves T-1..2T-2
+ *   bvhnode2aabb f32[(2*num_tri-1)*6]   [xmin, ymin, zmin, xmax, ymax, zmax]
+ *   matrices     f32[16] column-major (as del-msh's kernels read them)
+ * and the same results as del-msh-cpu on the same inputs (Morton codes,
+ * sorted permutation with ties by index, topology and AABBs bit-exact; hit
+ * triangle ids and hit t bit-exact to the CPU restatement).
+ *
+ * Conventions (those of the del-msh-dlpack GPU bindings):
+ *   - every array argument is a DEVICE pointer; outputs are caller-allocated;
+ *   - work is enqueued asynchronously on the CUDA stream `stream_ptr`
+ *     (a cudaStream_t cast to u64; 0 is the legacy default stream), like the
+ *     bindings' `stream_ptr: u64`;
+ *   - functions return DM_OK or an error code and never abort; the message of
+ *     the last error on the calling thread is dm_last_error().  Where the
+ *     reference panics (assert/unwrap on shapes) these return
+ *     DM_ERR_INVALID_ARGUMENT;
+ *   - `scratch` may be NULL: the function then allocates its temporary memory
+ *     stream-ordered (cudaMallocAsync / cudaFreeAsync on `stream_ptr`), as the
+ *     reference's bindings allocate theirs.  Otherwise it must hold at least
+ *     the matching *_scratch_bytes() bytes, 256-byte aligned;
+ *   - calls on distinct streams may run concurrently as long as they do not
+ *     share scratch memory.
+ */
+#ifndef DELMSH_GB300_H
+#define DELMSH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DM_OK 0
+#define DM_ERR_INVALID_ARGUMENT 1
+#define DM_ERR_CUDA 2
+#define DM_ERR_SCRATCH_TOO_SMALL 3
+#define DM_ERR_UNSUPPORTED 4
+
+/* Library version string. */
+const char* dm_version(void);
+
+/* Message of the last error returned on the calling thread ("" if none). */
+const char* dm_last_error(void);
+
+/* Reads the device status word of the current device (bits: 1 = a bounded
+ * wait gave up, 2 = a traversal stack tier was too small, 4 = an index read
+ * from an input array was out of range).  Synchronizes the device.  When
+ * `clear` is non-zero the word is reset to 0.  No reference counterpart: the
+ * reference's kernels use device asserts (mortons.cu:22-34,
+ * bvhnode2aabb.cu:21-48), which this library replaces by this word. */
+int dm_device_status(uint32_t* bits, int clear);
+
+/* Morton codes of points after a homogeneous transform (num_dim 2: 3x3, 3: 4x4
+ * column-major), clamped to the unit cube as del-msh-cpu does.
+ * Replaces: del-msh-dlpack/src/mortons.rs:18-77 mortons_vtx2morton_from_vtx2co
+ * (kernel del-msh-cuda-kernels/cuda/mortons.cu:8-37 vtx2morton;
+ * CPU del-msh-cpu/src/mortons.rs:171-212). */
+int dm_mortons_vtx2morton_from_vtx2co(uint64_t stream_ptr, uint32_t num_vtx, uint32_t num_dim,
+                                      const float* vtx2co, const float* transform_co2unit,
+                                      uint32_t* vtx2morton);
+
+/* Stable ascending sort of u32 values in place, writing the permutation
+ * (jdx2idx[j] = original position of the j-th smallest; ties keep ascending
+ * position).
+ * Replaces: del-msh-dlpack/src/array1d.rs:100-154 array1d_argsort (iota +
+ * thrust sort_by_key; CPU order of del-msh-cpu/src/mortons.rs:139-146). */
+int dm_array1d_argsort(uint64_t stream_ptr, uint32_t n, uint32_t* idx2val, uint32_t* jdx2idx, void* scratch,
+                       size_t scratch_bytes);
+size_t dm_array1d_argsort_scratch_bytes(uint32_t n);
+
+/* Karras binary radix tree over sorted Morton codes, in the bvhnodes layout;
+ * n == 1 gives the single leaf [MAX, idx2obj[0], MAX].
+ * Replaces: del-msh-dlpack/src/mortons.rs:80-135
+ * mortons_make_bvhnodes_from_sorted_mortons (kernel
+ * del-msh-cuda-kernels/cuda/bvhnodes_morton.cu:29-72;
+ * CPU del-msh-cpu/src/bvhnodes_morton.rs:10-50). */
+int dm_mortons_make_bvhnodes_from_sorted_mortons(uint64_t stream_ptr, uint32_t n, const uint32_t* idx2obj,
+                                                 const uint32_t* idx2morton, uint32_t* bvhnodes);
+
+/* AABB of every node of a triangle BVH (leaf = box of its triangle's three
+ * vertices, branch = union of its children), optionally also enclosing
+ * vtx2xyz1 (continuous collision detection; may be NULL).  This is also the
+ * refit of a deformed mesh: same bvhnodes, new vertices.  Only i_bvhnode == 0
+ * (the whole tree) is supported.  flags_scratch: u32[num_elem-1] that is zero
+ * before the first call and that every call leaves zero, or NULL.
+ * Replaces: del-msh-dlpack/src/bvhnode2aabb.rs:15-108 bvhnode2aabb_update_aabb
+ * (kernel del-msh-cuda-kernels/cuda/bvhnode2aabb.cu:7-65 from_trimesh3;
+ * CPU del-msh-cpu/src/bvhnode2aabb3.rs:68-142). */
+int dm_bvhnode2aabb_update_aabb(uint64_t stream_ptr, uint32_t num_bvhnode, float* bvhnode2aabb,
+                                uint32_t i_bvhnode, const uint32_t* bvhnodes, uint32_t num_elem,
+                                const uint32_t* elem2vtx, uint32_t num_vtx, const float* vtx2xyz0,
+                                const float* vtx2xyz1, uint32_t* flags_scratch);
+
+/* Whole LBVH build of a triangle mesh: centroids, centroid AABB, fit into the
+ * unit cube, Morton codes, stable radix sort, topology, AABBs.
+ * Replaces: del-msh-dlpack/del_msh_dlpack/TriMesh3/torch.py:233-285
+ * make_bvhnodes_bvhnode2aabb (CPU: del-msh-cpu/src/bvhnodes_morton.rs:151-159
+ * from_triangle_mesh + del-msh-cpu/src/bvhnode2aabb3.rs:168-195). */
+int dm_trimesh3_make_bvhnodes_bvhnode2aabb(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* tri2vtx,
+                                           uint32_t num_vtx, const float* vtx2xyz, uint32_t* bvhnodes,
+                                           float* bvhnode2aabb, void* scratch, size_t scratch_bytes);
+size_t dm_trimesh3_build_scratch_bytes(uint32_t num_tri);
+
+/* The same build with its intermediate results (each output may be NULL):
+ * transform_out f32[16] (fit transform, column-major), tri2morton_out u32[T],
+ * idx2tri_out / idx2morton_out u32[T] (the sorted permutation and codes, as
+ * mortons.rs:115-147 returns them), height_out u32[1] (nodes on the longest
+ * root-to-leaf path).  No single reference counterpart: these are the values
+ * of the intermediate steps of TriMesh3/torch.py:233-285. */
+int dm_trimesh3_build_ex(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                         const float* vtx2xyz, uint32_t* bvhnodes, float* bvhnode2aabb, float* transform_out,
+                         uint32_t* tri2morton_out, uint32_t* idx2tri_out, uint32_t* idx2morton_out,
+                         uint32_t* height_out, void* scratch, size_t scratch_bytes);
+
+/* Closest hit per pixel of an img_w x img_h image; pixel (iw, ih) casts the
+ * ray of ray_for_pixel.h (origin at ndc z=+1, towards z=-1).  pix2tri[ih*w+iw]
+ * = triangle or u32::MAX; pix2t (optional) = ray coefficient t of the hit
+ * (+inf on a miss).
+ * Replaces: del-msh-dlpack/src/pix2tri.rs:17-94 pix2tri_by_raycast (kernel
+ * del-msh-cuda-kernels/cuda/pix2tri.cu:13-76 pix_to_tri; the results are those
+ * of CPU del-msh-cpu/src/pix2tri.rs:3-48). */
+int dm_pix2tri_by_raycast(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, uint32_t* pix2tri, float* pix2t,
+                          uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz,
+                          const uint32_t* bvhnodes, const float* bvhnode2aabb, const float* transform_ndc2world,
+                          void* scratch, size_t scratch_bytes);
+
+/* Closest hit of each ray (ray_org, ray_dir f32[num_ray*3]); hit_t and hit_bc
+ * (barycentrics 1-u-v, u, v; f32[num_ray*3]) may be NULL.
+ * Replaces: del-msh-cpu/src/search_bvh3.rs:103-221 first_intersection_ray
+ * called once per ray. */
+int dm_search_bvh3_first_intersection_ray(uint64_t stream_ptr, uint32_t num_ray, const float* ray_org,
+                                          const float* ray_dir, uint32_t* hit_tri, float* hit_t, float* hit_bc,
+                                          uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                                          const float* vtx2xyz, const uint32_t* bvhnodes,
+                                          const float* bvhnode2aabb, void* scratch, size_t scratch_bytes);
+
+/* Scratch size of dm_pix2tri_by_raycast / dm_search_bvh3_first_intersection_ray. */
+size_t dm_cast_scratch_bytes(uint32_t num_ray, uint32_t num_tri);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DELMSH_GB300_H */

@@ -1,0 +1,743 @@
+/*
+ * oracle.c — CPU restatement of del-msh-cpu's LBVH build and BVH ray cast.
+ *
+ * TEST INFRASTRUCTURE ONLY (see oracle.h): the checker for the CUDA path and
+ * the timed CPU baseline.  Built with -O2 -ffp-contract=off so that every f32
+ * expression rounds exactly as the reference's Rust code does.
+ */
+#include "oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define OR_UMAX 0xFFFFFFFFu
+
+/* ------------------------------------------------------------------ Morton */
+
+/* mortons.rs:76-81 */
+uint32_t or_expand_bits3(uint32_t x) {
+  x = (x | (x << 16)) & 0x030000FFu;
+  x = (x | (x << 8)) & 0x0300F00Fu;
+  x = (x | (x << 4)) & 0x030C30C3u;
+  return (x | (x << 2)) & 0x09249249u;
+}
+
+/* mortons.rs:3-8 */
+static uint32_t expand_bits2(uint32_t x) {
+  x = (x | (x << 8)) & 0x00ff00ffu;
+  x = (x | (x << 4)) & 0x0f0f0f0fu;
+  x = (x | (x << 2)) & 0x33333333u;
+  return (x | (x << 1)) & 0x55555555u;
+}
+
+/* Rust `(v).clamp(0, hi) as u32`: clamp keeps NaN, and a NaN cast to u32 is 0. */
+static uint32_t quantize(float v, float hi) {
+  if (v < 0.0f) v = 0.0f;
+  else if (v > hi) v = hi;
+  if (v != v) return 0u;
+  return (uint32_t)v;
+}
+
+/* mortons.rs:94-102 */
+uint32_t or_morton_code3(float x, float y, float z) {
+  uint32_t ix = or_expand_bits3(quantize(x * 1024.0f, 1023.0f));
+  uint32_t iy = or_expand_bits3(quantize(y * 1024.0f, 1023.0f));
+  uint32_t iz = or_expand_bits3(quantize(z * 1024.0f, 1023.0f));
+  return ix * 4u + iy * 2u + iz;
+}
+
+/* mortons.rs:20-27 */
+uint32_t or_morton_code2(float x, float y) {
+  uint32_t ix = expand_bits2(quantize(x * 65536.0f, 65535.0f));
+  uint32_t iy = expand_bits2(quantize(y * 65536.0f, 65535.0f));
+  return ix * 2u + iy;
+}
+
+/* ------------------------------------------------------ centroids and AABB */
+
+/* elem2center.rs:25-54: cog starts at zero, nodes are summed in order 0,1,2,
+ * and the sum is multiplied by the f32 value of 1/3. */
+void or_tri2cntr(uint32_t num_tri, const uint32_t* tri2vtx, const float* vtx2xyz, float* tri2cntr) {
+  const float ratio = 1.0f / 3.0f;
+  for (uint32_t it = 0; it < num_tri; ++it) {
+    float cog[3] = {0.0f, 0.0f, 0.0f};
+    for (int in = 0; in < 3; ++in) {
+      const float* p = vtx2xyz + (size_t)tri2vtx[(size_t)it * 3 + in] * 3;
+      for (int d = 0; d < 3; ++d) cog[d] += p[d];
+    }
+    for (int d = 0; d < 3; ++d) tri2cntr[(size_t)it * 3 + d] = cog[d] * ratio;
+  }
+}
+
+/* aabb3::set_as_cube / add_point (del-geo-core, absent): box [p-eps, p+eps],
+ * widened by strict comparisons, so among equal values the first one stays. */
+static void aabb_set_as_cube(float a[6], const float p[3], float eps) {
+  for (int d = 0; d < 3; ++d) {
+    a[d] = p[d] - eps;
+    a[d + 3] = p[d] + eps;
+  }
+}
+static void aabb_add_point(float a[6], const float p[3], float eps) {
+  for (int d = 0; d < 3; ++d) {
+    const float lo = p[d] - eps, hi = p[d] + eps;
+    if (lo < a[d]) a[d] = lo;
+    if (hi > a[d + 3]) a[d + 3] = hi;
+  }
+}
+/* aabb3::from_two_aabbs (del-geo-core, absent): component-wise union; the
+ * first box's value stays on ties. */
+static void aabb_from_two(float o[6], const float a[6], const float b[6]) {
+  for (int d = 0; d < 3; ++d) {
+    o[d] = (b[d] < a[d]) ? b[d] : a[d];
+    o[d + 3] = (b[d + 3] > a[d + 3]) ? b[d + 3] : a[d + 3];
+  }
+}
+
+/* vtx2xyz.rs:19-37 (set_as_cube from the first point, then add_point over
+ * every point including the first), eps = 0 */
+void or_aabb3(uint32_t num_pnt, const float* pnt2xyz, float aabb[6]) {
+  aabb_set_as_cube(aabb, pnt2xyz, 0.0f);
+  for (uint32_t i = 0; i < num_pnt; ++i) aabb_add_point(aabb, pnt2xyz + (size_t)i * 3, 0.0f);
+}
+
+/* Mat44/torch.py:120-140: s = 1/max extent, translation = -center*s + 0.5,
+ * center = (min+max)*0.5.  Column-major 4x4. */
+void or_fit_into_unit_preserve_asp(const float aabb[6], float m[16]) {
+  float ext = aabb[3] - aabb[0];
+  const float ey = aabb[4] - aabb[1], ez = aabb[5] - aabb[2];
+  if (ey > ext) ext = ey;
+  if (ez > ext) ext = ez;
+  const float s = 1.0f / ext;
+  memset(m, 0, sizeof(float) * 16);
+  m[0] = s;
+  m[5] = s;
+  m[10] = s;
+  m[15] = 1.0f;
+  for (int d = 0; d < 3; ++d) {
+    const float c = (aabb[d] + aabb[d + 3]) * 0.5f;
+    m[12 + d] = -c * s + 0.5f;
+  }
+}
+
+/* column-major: out_i = (m[i]x + m[4+i]y + m[8+i]z + m[12+i]) / w, summed
+ * left to right. */
+void or_transform_homogeneous(const float m[16], const float p[3], float out[3]) {
+  const float w = m[3] * p[0] + m[7] * p[1] + m[11] * p[2] + m[15];
+  for (int i = 0; i < 3; ++i) out[i] = (m[i] * p[0] + m[4 + i] * p[1] + m[8 + i] * p[2] + m[12 + i]) / w;
+}
+
+static void transform_homogeneous2(const float m[9], const float p[2], float out[2]) {
+  const float w = m[2] * p[0] + m[5] * p[1] + m[8];
+  for (int i = 0; i < 2; ++i) out[i] = (m[i] * p[0] + m[3 + i] * p[1] + m[6 + i]) / w;
+}
+
+/* mortons.rs:171-212 */
+void or_vtx2morton(uint32_t num_vtx, uint32_t num_dim, const float* vtx2co, const float* transform,
+                   uint32_t* vtx2morton) {
+  for (uint32_t i = 0; i < num_vtx; ++i) {
+    if (num_dim == 3) {
+      float q[3];
+      or_transform_homogeneous(transform, vtx2co + (size_t)i * 3, q);
+      vtx2morton[i] = or_morton_code3(q[0], q[1], q[2]);
+    } else {
+      float q[2];
+      transform_homogeneous2(transform, vtx2co + (size_t)i * 2, q);
+      vtx2morton[i] = or_morton_code2(q[0], q[1]);
+    }
+  }
+}
+
+/* -------------------------------------------------------- stable argsort */
+
+/* bottom-up merge sort; the result ends in a */
+static void merge_sort_u64(uint64_t* a, uint64_t* tmp, size_t n) {
+  uint64_t* src = a;
+  uint64_t* dst = tmp;
+  for (size_t w = 1; w < n; w *= 2) {
+    for (size_t lo = 0; lo < n; lo += 2 * w) {
+      const size_t mid = lo + w < n ? lo + w : n, hi = lo + 2 * w < n ? lo + 2 * w : n;
+      size_t i = lo, j = mid, k = lo;
+      while (i < mid && j < hi) dst[k++] = (src[j] < src[i]) ? src[j++] : src[i++];
+      while (i < mid) dst[k++] = src[i++];
+      while (j < hi) dst[k++] = src[j++];
+    }
+    uint64_t* t = src;
+    src = dst;
+    dst = t;
+  }
+  if (src != a) memcpy(a, src, n * sizeof(uint64_t));
+}
+
+/* mortons.rs:139-146: iota, then a stable sort_by_key on the code, then the
+ * gather.  Sorting (code << 32 | index) gives the same permutation. */
+void or_argsort_stable(uint32_t n, const uint32_t* vtx2morton, uint32_t* idx2vtx, uint32_t* idx2morton) {
+  uint64_t* a = (uint64_t*)malloc(sizeof(uint64_t) * (n ? n : 1));
+  uint64_t* t = (uint64_t*)malloc(sizeof(uint64_t) * (n ? n : 1));
+  for (uint32_t i = 0; i < n; ++i) a[i] = ((uint64_t)vtx2morton[i] << 32) | i;
+  merge_sort_u64(a, t, n);
+  for (uint32_t i = 0; i < n; ++i) {
+    idx2vtx[i] = (uint32_t)(a[i] & 0xFFFFFFFFu);
+    idx2morton[i] = (uint32_t)(a[i] >> 32);
+  }
+  free(a);
+  free(t);
+}
+
+/* ------------------------------------------------------- radix tree */
+
+static int clz32(uint32_t v) { return v == 0 ? 32 : __builtin_clz(v); }
+
+/* mortons.rs:216-218 */
+static int64_t delta(uint32_t i0, uint32_t i1, const uint32_t* c) { return clz32(c[i0] ^ c[i1]); }
+
+/* mortons.rs:221-288 */
+void or_range_of_binary_radix_tree_node(const uint32_t* c, uint32_t n, uint32_t idx1, uint32_t* r0, uint32_t* r1) {
+  if (idx1 == 0) {
+    *r0 = 0;
+    *r1 = n - 1;
+    return;
+  }
+  if (idx1 == n - 1) {
+    *r0 = n - 1;
+    *r1 = n - 1;
+    return;
+  }
+  const uint32_t mc0 = c[idx1 - 1], mc1 = c[idx1], mc2 = c[idx1 + 1];
+  if (mc0 == mc1 && mc1 == mc2) {
+    uint32_t jdx = idx1 + 1;
+    while (jdx < n - 1) {
+      jdx += 1;
+      if (c[jdx] != mc1) {
+        *r0 = idx1;
+        *r1 = jdx - 1;
+        return;
+      }
+    }
+    *r0 = idx1;
+    *r1 = jdx;
+    return;
+  }
+  int64_t d = delta(idx1, idx1 + 1, c) - delta(idx1, idx1 - 1, c);
+  d = d > 0 ? 1 : -1;
+  const int64_t delta_min = delta(idx1, (uint32_t)((int64_t)idx1 - d), c);
+  int64_t lmax = 2;
+  for (;;) {
+    const int64_t jdx = (int64_t)idx1 + lmax * d;
+    if (jdx < 0 || jdx >= (int64_t)n) break;
+    if (delta(idx1, (uint32_t)jdx, c) <= delta_min) break;
+    lmax *= 2;
+  }
+  int64_t l = 0;
+  for (int64_t t = lmax / 2; t >= 1; t /= 2) {
+    const int64_t jdx = (int64_t)idx1 + (l + t) * d;
+    if (jdx >= 0 && jdx < (int64_t)n && delta(idx1, (uint32_t)jdx, c) > delta_min) l += t;
+  }
+  const uint32_t jdx = (uint32_t)((int64_t)idx1 + l * d);
+  if (idx1 <= jdx) {
+    *r0 = idx1;
+    *r1 = jdx;
+  } else {
+    *r0 = jdx;
+    *r1 = idx1;
+  }
+}
+
+/* mortons.rs:290-325 */
+uint32_t or_split_of_binary_radix_tree_node(const uint32_t* c, uint32_t start, uint32_t end) {
+  if (start == end) return OR_UMAX;
+  const uint32_t mc_start = c[start];
+  const int nbitcommon0 = clz32(mc_start ^ c[end]);
+  if (nbitcommon0 == 32) return start;
+  uint32_t split = start;
+  uint32_t step = end - start;
+  while (step > 1) {
+    step = (step + 1) / 2;
+    const uint32_t cand = split + step;
+    if (cand >= end) continue;
+    if (clz32(mc_start ^ c[cand]) > nbitcommon0) split = cand;
+  }
+  return split;
+}
+
+/* bvhnodes_morton.rs:10-50.  For n == 1 the reference leaves node 0 as a
+ * branch without children; here it becomes the single leaf [MAX, obj, MAX]. */
+void or_update_bvhnodes(uint32_t n, const uint32_t* idx2vtx, const uint32_t* idx2morton, uint32_t* bvhnodes) {
+  bvhnodes[0] = OR_UMAX;
+  if (n == 1) {
+    bvhnodes[1] = idx2vtx[0];
+    bvhnodes[2] = OR_UMAX;
+    return;
+  }
+  const uint32_t num_branch = n - 1;
+  for (uint32_t ib = 0; ib < num_branch; ++ib) {
+    uint32_t r0, r1;
+    or_range_of_binary_radix_tree_node(idx2morton, n, ib, &r0, &r1);
+    const uint32_t isplit = or_split_of_binary_radix_tree_node(idx2morton, r0, r1);
+    if (r0 == isplit) {
+      const uint32_t a = num_branch + isplit;
+      bvhnodes[ib * 3 + 1] = a;
+      bvhnodes[a * 3] = ib;
+      bvhnodes[a * 3 + 1] = idx2vtx[isplit];
+      bvhnodes[a * 3 + 2] = OR_UMAX;
+    } else {
+      bvhnodes[ib * 3 + 1] = isplit;
+      bvhnodes[isplit * 3] = ib;
+    }
+    if (r1 == isplit + 1) {
+      const uint32_t b = num_branch + isplit + 1;
+      bvhnodes[ib * 3 + 2] = b;
+      bvhnodes[b * 3] = ib;
+      bvhnodes[b * 3 + 1] = idx2vtx[isplit + 1];
+      bvhnodes[b * 3 + 2] = OR_UMAX;
+    } else {
+      bvhnodes[ib * 3 + 2] = isplit + 1;
+      bvhnodes[(isplit + 1) * 3] = ib;
+    }
+  }
+}
+
+void or_bvhnodes_from_triangle_mesh(uint32_t num_tri, const uint32_t* tri2vtx, const float* vtx2xyz,
+                                    uint32_t* bvhnodes, float* transform_out, uint32_t* tri2morton_out,
+                                    uint32_t* idx2tri_out, uint32_t* idx2morton_out) {
+  float* cntr = (float*)malloc(sizeof(float) * 3 * num_tri);
+  uint32_t* tri2morton = (uint32_t*)malloc(sizeof(uint32_t) * num_tri);
+  uint32_t* idx2tri = (uint32_t*)malloc(sizeof(uint32_t) * num_tri);
+  uint32_t* idx2morton = (uint32_t*)malloc(sizeof(uint32_t) * num_tri);
+  float aabb[6], m[16];
+  or_tri2cntr(num_tri, tri2vtx, vtx2xyz, cntr);
+  or_aabb3(num_tri, cntr, aabb);
+  or_fit_into_unit_preserve_asp(aabb, m);
+  or_vtx2morton(num_tri, 3, cntr, m, tri2morton);
+  or_argsort_stable(num_tri, tri2morton, idx2tri, idx2morton);
+  or_update_bvhnodes(num_tri, idx2tri, idx2morton, bvhnodes);
+  if (transform_out) memcpy(transform_out, m, sizeof(m));
+  if (tri2morton_out) memcpy(tri2morton_out, tri2morton, sizeof(uint32_t) * num_tri);
+  if (idx2tri_out) memcpy(idx2tri_out, idx2tri, sizeof(uint32_t) * num_tri);
+  if (idx2morton_out) memcpy(idx2morton_out, idx2morton, sizeof(uint32_t) * num_tri);
+  free(cntr);
+  free(tri2morton);
+  free(idx2tri);
+  free(idx2morton);
+}
+
+/* -------------------------------------------------------------- refit */
+
+/* bvhnode2aabb3.rs:68-142 (leaf: aabb3_indexed with eps 0, vtx2xyz.rs:39-61;
+ * optional CCD union with vtx2xyz1; branch: from_two_aabbs(child0, child1)). */
+void or_update_aabb_uniform_mesh(float* bvhnode2aabb, uint32_t i_bvhnode, const uint32_t* bvhnodes,
+                                 const uint32_t* tri2vtx, const float* vtx2xyz0, const float* vtx2xyz1) {
+  float* out = bvhnode2aabb + (size_t)i_bvhnode * 6;
+  if (bvhnodes[i_bvhnode * 3 + 2] == OR_UMAX) {
+    const uint32_t it = bvhnodes[i_bvhnode * 3 + 1];
+    const uint32_t* tv = tri2vtx + (size_t)it * 3;
+    float a0[6];
+    aabb_set_as_cube(a0, vtx2xyz0 + (size_t)tv[0] * 3, 0.0f);
+    aabb_add_point(a0, vtx2xyz0 + (size_t)tv[1] * 3, 0.0f);
+    aabb_add_point(a0, vtx2xyz0 + (size_t)tv[2] * 3, 0.0f);
+    if (vtx2xyz1) {
+      float a1[6];
+      aabb_set_as_cube(a1, vtx2xyz1 + (size_t)tv[0] * 3, 0.0f);
+      aabb_add_point(a1, vtx2xyz1 + (size_t)tv[1] * 3, 0.0f);
+      aabb_add_point(a1, vtx2xyz1 + (size_t)tv[2] * 3, 0.0f);
+      aabb_from_two(out, a0, a1);
+    } else {
+      memcpy(out, a0, sizeof(a0));
+    }
+    return;
+  }
+  const uint32_t c0 = bvhnodes[i_bvhnode * 3 + 1], c1 = bvhnodes[i_bvhnode * 3 + 2];
+  or_update_aabb_uniform_mesh(bvhnode2aabb, c0, bvhnodes, tri2vtx, vtx2xyz0, vtx2xyz1);
+  or_update_aabb_uniform_mesh(bvhnode2aabb, c1, bvhnodes, tri2vtx, vtx2xyz0, vtx2xyz1);
+  float tmp[6];
+  aabb_from_two(tmp, bvhnode2aabb + (size_t)c0 * 6, bvhnode2aabb + (size_t)c1 * 6);
+  memcpy(out, tmp, sizeof(tmp));
+}
+
+/* ---------------------------------------------------------- ray casting */
+
+/* ray_for_pixel.h:3-19 */
+void or_ray_for_pixel(uint32_t i_pix, uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], float org[3],
+                      float dir[3]) {
+  const uint32_t ih = i_pix / img_w;
+  const uint32_t iw = i_pix - ih * img_w;
+  const float x0 = 2.0f * ((float)iw + 0.5f) / (float)img_w - 1.0f;
+  const float y0 = 1.0f - 2.0f * ((float)ih + 0.5f) / (float)img_h;
+  const float a[3] = {x0, y0, 1.0f}, b[3] = {x0, y0, -1.0f};
+  float q0[3], q1[3];
+  or_transform_homogeneous(t_ndc2world, a, q0);
+  or_transform_homogeneous(t_ndc2world, b, q1);
+  for (int d = 0; d < 3; ++d) {
+    org[d] = q0[d];
+    dir[d] = q1[d] - q0[d];
+  }
+}
+
+static float dot3(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static void cross3(float o[3], const float a[3], const float b[3]) {
+  o[0] = a[1] * b[2] - a[2] * b[1];
+  o[1] = a[2] * b[0] - a[0] * b[2];
+  o[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+/* Moller & Trumbore, "Fast, Minimum Storage Ray/Triangle Intersection"
+ * (1997), without back-face culling: det == 0 is a miss, edges are
+ * inclusive, t >= 0 is a hit.  All comparisons reject NaN. */
+int or_tri3_ray(const float p0[3], const float p1[3], const float p2[3], const float org[3], const float dir[3],
+                float* t, float bc[3]) {
+  float e1[3], e2[3], tv[3], pv[3], qv[3];
+  for (int d = 0; d < 3; ++d) {
+    e1[d] = p1[d] - p0[d];
+    e2[d] = p2[d] - p0[d];
+    tv[d] = org[d] - p0[d];
+  }
+  cross3(pv, dir, e2);
+  const float det = dot3(e1, pv);
+  if (det == 0.0f) return 0;
+  const float inv_det = 1.0f / det;
+  const float u = dot3(tv, pv) * inv_det;
+  if (!(u >= 0.0f && u <= 1.0f)) return 0;
+  cross3(qv, tv, e1);
+  const float v = dot3(dir, qv) * inv_det;
+  if (!(v >= 0.0f && u + v <= 1.0f)) return 0;
+  const float tt = dot3(e2, qv) * inv_det;
+  if (!(tt >= 0.0f)) return 0;
+  *t = tt;
+  if (bc) {
+    bc[0] = 1.0f - u - v;
+    bc[1] = u;
+    bc[2] = v;
+  }
+  return 1;
+}
+
+int or_tri3_ray_f64(const float p0[3], const float p1[3], const float p2[3], const float org[3], const float dir[3],
+                    double* t) {
+  double e1[3], e2[3], tv[3], pv[3], qv[3], dd[3];
+  for (int d = 0; d < 3; ++d) {
+    e1[d] = (double)p1[d] - (double)p0[d];
+    e2[d] = (double)p2[d] - (double)p0[d];
+    tv[d] = (double)org[d] - (double)p0[d];
+    dd[d] = (double)dir[d];
+  }
+  pv[0] = dd[1] * e2[2] - dd[2] * e2[1];
+  pv[1] = dd[2] * e2[0] - dd[0] * e2[2];
+  pv[2] = dd[0] * e2[1] - dd[1] * e2[0];
+  const double det = e1[0] * pv[0] + e1[1] * pv[1] + e1[2] * pv[2];
+  if (det == 0.0) return 0;
+  const double inv_det = 1.0 / det;
+  qv[0] = tv[1] * e1[2] - tv[2] * e1[1];
+  qv[1] = tv[2] * e1[0] - tv[0] * e1[2];
+  qv[2] = tv[0] * e1[1] - tv[1] * e1[0];
+  *t = (e2[0] * qv[0] + e2[1] * qv[1] + e2[2] * qv[2]) * inv_det;
+  return 1;
+}
+
+/* Slab test (Kay & Kajiya 1986; Williams et al., "An Efficient and Robust
+ * Ray-Box Intersection Algorithm", 2005) with precomputed 1/dir.  An axis with
+ * dir == 0 is a hit iff the origin lies inside the slab.  Returns 1 and
+ * (t_enter, t_exit) iff t_enter <= t_exit and t_exit >= 0. */
+int or_aabb3_ray(const float aabb[6], const float org[3], const float inv_dir[3], const float dir[3], float* t_enter,
+                 float* t_exit) {
+  float tmin = -INFINITY, tmax = INFINITY;
+  for (int d = 0; d < 3; ++d) {
+    if (dir[d] != 0.0f) {
+      const float t0 = (aabb[d] - org[d]) * inv_dir[d];
+      const float t1 = (aabb[d + 3] - org[d]) * inv_dir[d];
+      const float tn = (t1 < t0) ? t1 : t0;
+      const float tf = (t1 < t0) ? t0 : t1;
+      if (tn > tmin) tmin = tn;
+      if (tf < tmax) tmax = tf;
+    } else if (org[d] < aabb[d] || org[d] > aabb[d + 3]) {
+      return 0;
+    }
+  }
+  if (!(tmin <= tmax) || tmax < 0.0f) return 0;
+  *t_enter = tmin;
+  *t_exit = tmax;
+  return 1;
+}
+
+typedef struct {
+  const uint32_t* tri2vtx;
+  const float* vtx2xyz;
+  const uint32_t* bvhnodes;
+  const float* aabb;
+  float org[3], dir[3], inv[3];
+} RayCtx;
+
+static void ray_ctx_init(RayCtx* c, const float org[3], const float dir[3]) {
+  for (int d = 0; d < 3; ++d) {
+    c->org[d] = org[d];
+    c->dir[d] = dir[d];
+    c->inv[d] = 1.0f / dir[d];
+  }
+}
+
+static int slab(const RayCtx* c, uint32_t node, float* te, float* tx) {
+  return or_aabb3_ray(c->aabb + (size_t)node * 6, c->org, c->inv, c->dir, te, tx);
+}
+
+/* Rust's lexicographic `<` on (f32, f32) tuples. */
+static int tuple_lt(float a0, float a1, float b0, float b1) { return (a0 == b0) ? (a1 < b1) : (a0 < b0); }
+
+static int tri_hit(const RayCtx* c, uint32_t it, float* t) {
+  const uint32_t* tv = c->tri2vtx + (size_t)it * 3;
+  return or_tri3_ray(c->vtx2xyz + (size_t)tv[0] * 3, c->vtx2xyz + (size_t)tv[1] * 3, c->vtx2xyz + (size_t)tv[2] * 3,
+                     c->org, c->dir, t, NULL);
+}
+
+/* search_bvh3.rs:103-221 */
+static int first_hit(const RayCtx* c, uint32_t node, float dis, float* t_out, uint32_t* tri_out) {
+  float te, tx;
+  if (!slab(c, node, &te, &tx)) return 0;
+  const uint32_t* bn = c->bvhnodes;
+  if (bn[node * 3 + 2] == OR_UMAX) {
+    const uint32_t it = bn[node * 3 + 1];
+    float t;
+    if (!tri_hit(c, it, &t)) return 0;
+    if (!(t < dis)) return 0;
+    *t_out = t;
+    *tri_out = it;
+    return 1;
+  }
+  const uint32_t l = bn[node * 3 + 1], r = bn[node * 3 + 2];
+  float tl0 = 0, tl1 = 0, tr0 = 0, tr1 = 0;
+  const int hl = slab(c, l, &tl0, &tl1), hr = slab(c, r, &tr0, &tr1);
+  int near_is_left;
+  if (hl && hr) near_is_left = tuple_lt(tl0, tl1, tr0, tr1);
+  else if (!hl && !hr) return 0;
+  else near_is_left = hl;
+  const uint32_t nn = near_is_left ? l : r, nf = near_is_left ? r : l;
+  float tn = 0, tf = 0;
+  uint32_t in = 0, iff = 0;
+  const int hn = first_hit(c, nn, dis, &tn, &in);
+  if (hn) {
+    float f0, f1;
+    if (slab(c, nf, &f0, &f1)) {
+      if (f0 > tn) {
+        *t_out = tn;
+        *tri_out = in;
+        return 1;
+      }
+    } else {
+      *t_out = tn;
+      *tri_out = in;
+      return 1;
+    }
+  }
+  const int hf = first_hit(c, nf, dis, &tf, &iff);
+  if (hn && hf) {
+    if (tn < tf) {
+      *t_out = tn;
+      *tri_out = in;
+    } else {
+      *t_out = tf;
+      *tri_out = iff;
+    }
+    return 1;
+  }
+  if (hn) {
+    *t_out = tn;
+    *tri_out = in;
+    return 1;
+  }
+  if (hf) {
+    *t_out = tf;
+    *tri_out = iff;
+    return 1;
+  }
+  return 0;
+}
+
+int or_first_intersection_ray(const float org[3], const float dir[3], const uint32_t* tri2vtx, const float* vtx2xyz,
+                              const uint32_t* bvhnodes, const float* bvhnode2aabb, uint32_t i_bvhnode, float dis,
+                              float* t_out, uint32_t* tri_out) {
+  RayCtx c = {tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, {0}, {0}, {0}};
+  ray_ctx_init(&c, org, dir);
+  return first_hit(&c, i_bvhnode, dis, t_out, tri_out);
+}
+
+static void all_hits(const RayCtx* c, uint32_t node, float* ht, uint32_t* hi, uint32_t cap, uint32_t* cnt) {
+  float te, tx;
+  if (!slab(c, node, &te, &tx)) return;
+  const uint32_t* bn = c->bvhnodes;
+  if (bn[node * 3 + 2] == OR_UMAX) {
+    float t;
+    const uint32_t it = bn[node * 3 + 1];
+    if (!tri_hit(c, it, &t)) return;
+    if (*cnt < cap) {
+      ht[*cnt] = t;
+      hi[*cnt] = it;
+    }
+    *cnt += 1;
+    return;
+  }
+  all_hits(c, bn[node * 3 + 1], ht, hi, cap, cnt);
+  all_hits(c, bn[node * 3 + 2], ht, hi, cap, cnt);
+}
+
+/* search_bvh3.rs:12-53 */
+uint32_t or_intersections_ray(const float org[3], const float dir[3], const uint32_t* tri2vtx, const float* vtx2xyz,
+                              const uint32_t* bvhnodes, const float* bvhnode2aabb, float* hit_t, uint32_t* hit_tri,
+                              uint32_t cap) {
+  RayCtx c = {tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, {0}, {0}, {0}};
+  ray_ctx_init(&c, org, dir);
+  uint32_t cnt = 0;
+  all_hits(&c, 0, hit_t, hit_tri, cap, &cnt);
+  return cnt;
+}
+
+/* ------------------------------------------------ multi-threaded drivers */
+
+typedef struct {
+  uint32_t num;
+  int mode; /* 0: pixels, 1: ray arrays */
+  uint32_t img_w, img_h;
+  const float* t_ndc2world;
+  const float* ray_org;
+  const float* ray_dir;
+  const uint32_t* tri2vtx;
+  const float* vtx2xyz;
+  const uint32_t* bvhnodes;
+  const float* aabb;
+  uint32_t* out_tri;
+  float* out_t;
+  uint32_t next; /* work counter, chunks of 64 */
+} CastJob;
+
+static void* cast_worker(void* arg) {
+  CastJob* job = (CastJob*)arg;
+  for (;;) {
+    const uint32_t start = __atomic_fetch_add(&job->next, 64u, __ATOMIC_RELAXED);
+    if (start >= job->num) break;
+    const uint32_t end = start + 64 < job->num ? start + 64 : job->num;
+    for (uint32_t i = start; i < end; ++i) {
+      float org[3], dir[3];
+      if (job->mode == 0) {
+        or_ray_for_pixel(i, job->img_w, job->img_h, job->t_ndc2world, org, dir);
+      } else {
+        for (int d = 0; d < 3; ++d) {
+          org[d] = job->ray_org[(size_t)i * 3 + d];
+          dir[d] = job->ray_dir[(size_t)i * 3 + d];
+        }
+      }
+      float t = INFINITY;
+      uint32_t it = OR_UMAX;
+      if (!or_first_intersection_ray(org, dir, job->tri2vtx, job->vtx2xyz, job->bvhnodes, job->aabb, 0, INFINITY, &t,
+                                     &it)) {
+        t = INFINITY;
+        it = OR_UMAX;
+      }
+      job->out_tri[i] = it;
+      if (job->out_t) job->out_t[i] = t;
+    }
+  }
+  return NULL;
+}
+
+static void run_cast_job(CastJob* job, int num_threads) {
+  if (num_threads < 1) num_threads = 1;
+  if (num_threads == 1) {
+    cast_worker(job);
+    return;
+  }
+  pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * num_threads);
+  pthread_attr_t attr;
+  pthread_attr_init(&attr);
+  pthread_attr_setstacksize(&attr, (size_t)64 << 20); /* deep trees recurse deeply */
+  for (int i = 0; i < num_threads; ++i) pthread_create(&th[i], &attr, cast_worker, job);
+  for (int i = 0; i < num_threads; ++i) pthread_join(th[i], NULL);
+  pthread_attr_destroy(&attr);
+  free(th);
+}
+
+/* pix2tri.rs:3-48 */
+void or_pix2tri_by_raycast(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], const uint32_t* tri2vtx,
+                           const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb,
+                           uint32_t* pix2tri, float* pix2t, int num_threads) {
+  CastJob job = {img_w * img_h, 0, img_w, img_h, t_ndc2world, NULL, NULL, tri2vtx, vtx2xyz,
+                 bvhnodes, bvhnode2aabb, pix2tri, pix2t, 0};
+  run_cast_job(&job, num_threads);
+}
+
+void or_cast_rays(uint32_t num_ray, const float* ray_org, const float* ray_dir, const uint32_t* tri2vtx,
+                  const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb, uint32_t* hit_tri,
+                  float* hit_t, int num_threads) {
+  CastJob job = {num_ray, 1, 0, 0, NULL, ray_org, ray_dir, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, hit_tri, hit_t, 0};
+  run_cast_job(&job, num_threads);
+}
+
+/* ------------------------------------------------------------ checkers */
+
+/* bvhnodes.rs:3-36 (iterative; a malformed tree fails instead of looping) */
+int or_check_bvh_topology(const uint32_t* bvhnodes, uint32_t num_leaf) {
+  const uint32_t num_node = 2 * num_leaf - 1;
+  uint32_t* cnt = (uint32_t*)calloc(num_leaf, sizeof(uint32_t));
+  uint32_t* stack = (uint32_t*)malloc(sizeof(uint32_t) * (num_node + 1));
+  int ok = 1;
+  uint32_t sp = 0, visits = 0;
+  stack[sp++] = 0;
+  while (sp > 0 && ok) {
+    const uint32_t n = stack[--sp];
+    if (n >= num_node || ++visits > num_node) {
+      ok = 0;
+      break;
+    }
+    if (bvhnodes[n * 3 + 2] == OR_UMAX) {
+      const uint32_t v = bvhnodes[n * 3 + 1];
+      if (v >= num_leaf) ok = 0;
+      else cnt[v] += 1;
+      continue;
+    }
+    stack[sp++] = bvhnodes[n * 3 + 2];
+    stack[sp++] = bvhnodes[n * 3 + 1];
+  }
+  for (uint32_t i = 0; ok && i < num_leaf; ++i)
+    if (cnt[i] != 1) ok = 0;
+  for (uint32_t i = 0; ok && i < num_leaf; ++i)
+    if (bvhnodes[(num_leaf - 1 + i) * 3 + 2] != OR_UMAX) ok = 0;
+  free(cnt);
+  free(stack);
+  return ok;
+}
+
+/* mortons.rs:330-352 */
+int or_check_morton_code_range_split(const uint32_t* c, uint32_t n) {
+  for (uint32_t i = 0; i + 1 < n; ++i)
+    if (c[i] > c[i + 1]) return 0;
+  for (uint32_t ini = 0; ini + 1 < n; ++ini) {
+    uint32_t r0, r1, a0, a1, b0, b1;
+    or_range_of_binary_radix_tree_node(c, n, ini, &r0, &r1);
+    const uint32_t isplit = or_split_of_binary_radix_tree_node(c, r0, r1);
+    or_range_of_binary_radix_tree_node(c, n, isplit, &a0, &a1);
+    or_range_of_binary_radix_tree_node(c, n, isplit + 1, &b0, &b1);
+    if (r0 != a0 || r1 != b1) return 0;
+    const uint32_t last1 = (isplit == r0) ? isplit : a1;
+    const uint32_t first1 = (isplit + 1 == r1) ? isplit + 1 : b0;
+    if (last1 + 1 != first1) return 0;
+  }
+  return 1;
+}
+
+uint32_t or_tree_height(const uint32_t* bvhnodes, uint32_t num_leaf) {
+  const uint32_t num_node = 2 * num_leaf - 1;
+  uint32_t* stack = (uint32_t*)malloc(sizeof(uint32_t) * 2 * (num_node + 1));
+  uint32_t sp = 0, best = 0, visits = 0;
+  stack[sp++] = 0;
+  stack[sp++] = 1;
+  while (sp > 0) {
+    const uint32_t depth = stack[--sp];
+    const uint32_t n = stack[--sp];
+    if (n >= num_node || ++visits > num_node) break;
+    if (depth > best) best = depth;
+    if (bvhnodes[n * 3 + 2] == OR_UMAX) continue;
+    stack[sp++] = bvhnodes[n * 3 + 1];
+    stack[sp++] = depth + 1;
+    stack[sp++] = bvhnodes[n * 3 + 2];
+    stack[sp++] = depth + 1;
+  }
+  free(stack);
+  return best;
+}

@@ -1,0 +1,168 @@
+"""GPU parity of the LBVH build stages against the oracle and the reference's
+own golden vectors.  Integer results and f32 AABBs are compared bit for bit."""
+import numpy as np
+import pytest
+
+from helpers import bits, to_dev, to_np
+
+from del_msh_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _status_clear():
+    from del_msh_gb300 import _native
+    return _native.device_status(clear=True)
+
+
+def test_morton_points_match_reference_code(cuda, golden_dir):
+    torch = cuda
+    from del_msh_gb300.Mortons import torch as Mortons
+    g = np.load(golden_dir / "ref_morton.npz")
+    got = Mortons.make_vtx2morton_from_vtx2co(to_dev(g["pts"], torch), torch.eye(4, device="cuda:0"))
+    assert np.array_equal(to_np(got, torch), g["codes"])
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_morton_points_with_transform(cuda, oracle, dim):
+    # del-msh-dlpack/tests/test_mortons.py:64-98 (a transform vs pre-transformed points)
+    torch = cuda
+    from del_msh_gb300.Mortons import torch as Mortons
+    rng = np.random.default_rng(dim)
+    pts = (rng.random((20_000, dim)) * 3.0 - 1.0).astype(np.float32)
+    m = np.eye(dim + 1, dtype=np.float32)
+    m[:dim, :dim] /= 3.0
+    m[:dim, dim] = 1.0 / 3.0
+    got = to_np(Mortons.make_vtx2morton_from_vtx2co(to_dev(pts, torch), to_dev(m, torch)), torch)
+    ref = oracle.vtx2morton(pts, np.ascontiguousarray(m.T).reshape(-1))
+    assert np.array_equal(got, ref)
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 100, 3839, 3840, 3841, 65_537, 1_000_003])
+def test_argsort_stable(cuda, n):
+    torch = cuda
+    from del_msh_gb300.Array1D import torch as Array1D
+    rng = np.random.default_rng(n)
+    vals = rng.integers(0, 1 << 32, n, dtype=np.uint64).astype(np.uint32)
+    if n > 10:
+        vals[rng.random(n) < 0.3] = 0xFFFFFFFF
+        vals[rng.random(n) < 0.2] = 7
+    idx, srt = Array1D.argsort(to_dev(vals, torch))
+    ref = np.argsort(vals, kind="stable").astype(np.uint32)
+    assert np.array_equal(to_np(idx, torch), ref)
+    assert np.array_equal(to_np(srt, torch), vals[ref])
+
+
+def test_argsort_all_equal(cuda):
+    torch = cuda
+    from del_msh_gb300.Array1D import torch as Array1D
+    vals = np.full(200_000, 42, np.uint32)
+    idx, srt = Array1D.argsort(to_dev(vals, torch))
+    assert np.array_equal(to_np(idx, torch), np.arange(200_000, dtype=np.uint32))
+
+
+def test_topology_matches_reference_code(cuda, golden_dir):
+    torch = cuda
+    from del_msh_gb300.Mortons import torch as Mortons
+    g = np.load(golden_dir / "ref_topology.npz")
+    for name in sorted({k.split("__")[0] for k in g.files}):
+        got = Mortons.make_bvhnodes_from_sorted_mortons(to_dev(g[f"{name}__idx2obj"], torch),
+                                                        to_dev(g[f"{name}__idx2morton"], torch))
+        assert np.array_equal(to_np(got, torch), g[f"{name}__bvhnodes"]), name
+
+
+def test_topology_single_object(cuda):
+    torch = cuda
+    from del_msh_gb300.Mortons import torch as Mortons
+    got = Mortons.make_bvhnodes_from_sorted_mortons(to_dev(np.array([5], np.uint32), torch),
+                                                    to_dev(np.array([77], np.uint32), torch))
+    assert to_np(got, torch).tolist() == [[0xFFFFFFFF, 5, 0xFFFFFFFF]]
+
+
+def _build_ex(torch, tri, vtx):
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    r = TriMesh3.make_bvhnodes_bvhnode2aabb_ex(to_dev(tri, torch), to_dev(vtx, torch))
+    out = {k: (to_np(v, torch) if hasattr(v, "device") else v) for k, v in r.items()}
+    out["transform"] = np.ascontiguousarray(out["transform"].T).reshape(-1)  # back to column-major
+    return out
+
+
+def _compare_build(got, ref, T):
+    for k in ("transform", "tri2morton", "idx2tri", "idx2morton", "bvhnodes", "bvhnode2aabb"):
+        assert np.array_equal(bits(got[k]), bits(ref[k])), k
+
+
+def test_build_cfg1_matches_golden(cuda, golden_dir):
+    torch = cuda
+    g = np.load(golden_dir / "oracle_cfg1.npz")
+    got = _build_ex(torch, g["tri2vtx"], g["vtx2xyz"])
+    _compare_build(got, {k: g[k] for k in g.files}, g["tri2vtx"].shape[0])
+    assert _status_clear() == 0
+
+
+@pytest.mark.parametrize("case", ["torus", "soup", "ico", "tiny2", "tiny3", "same_tris", "flat"])
+def test_build_matches_oracle(cuda, oracle, case):
+    torch = cuda
+    if case == "torus":
+        tri, vtx = W.displaced_torus(256, seed=3)
+    elif case == "soup":
+        tri, vtx = W.clustered_soup(200_000, seed=4)
+    elif case == "ico":
+        tri, vtx = W.jittered_icosphere(5, seed=5)
+    elif case == "tiny2":
+        tri, vtx = W.icosphere(0)
+        tri = tri[:2]
+    elif case == "tiny3":
+        tri, vtx = W.icosphere(0)
+        tri = tri[:3]
+    elif case == "same_tris":
+        tri = np.tile(np.array([[0, 1, 2]], np.uint32), (5000, 1))
+        vtx = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    else:  # all vertices on the plane z = 0
+        rng = np.random.default_rng(8)
+        vtx = np.concatenate([rng.random((3000, 2)), np.zeros((3000, 1))], 1).astype(np.float32)
+        tri = rng.integers(0, 3000, (4000, 3)).astype(np.uint32)
+    ref = oracle.build(tri, vtx)
+    got = _build_ex(torch, tri, vtx)
+    _compare_build(got, ref, tri.shape[0])
+    assert got["height"] == oracle.tree_height(ref["bvhnodes"], tri.shape[0])
+    assert _status_clear() == 0
+
+
+def test_build_single_triangle(cuda):
+    torch = cuda
+    tri = np.array([[0, 1, 2]], np.uint32)
+    vtx = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 2]], np.float32)
+    got = _build_ex(torch, tri, vtx)
+    assert got["bvhnodes"].tolist() == [[0xFFFFFFFF, 0, 0xFFFFFFFF]]
+    assert got["bvhnode2aabb"].tolist() == [[0, 0, 0, 1, 1, 2]]
+
+
+def test_refit_deformed_and_ccd(cuda, oracle):
+    torch = cuda
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    tri, vtx = W.displaced_torus(128, seed=1)
+    ref = oracle.build(tri, vtx)
+    d_tri, d_vtx = to_dev(tri, torch), to_dev(vtx, torch)
+    bvh, aabb = TriMesh3.make_bvhnodes_bvhnode2aabb(d_tri, d_vtx)
+    flags = torch.zeros((tri.shape[0],), dtype=torch.int32, device="cuda:0").view(torch.uint32)
+    rng = np.random.default_rng(2)
+    phase = rng.uniform(0, 6.28, vtx.shape[0])
+    for frame in range(3):
+        v1 = (vtx + 0.01 * np.sin(phase + frame)[:, None]).astype(np.float32)
+        TriMesh3.update_bvhnode2aabb(d_tri, to_dev(v1, torch), bvh, aabb, flags=flags)
+        assert np.array_equal(bits(to_np(aabb, torch)), bits(oracle.bvhnode2aabb(ref["bvhnodes"], tri, v1)))
+        assert not to_np(flags, torch).any()  # the refit leaves its arrival flags zero
+    v2 = (vtx * 1.01).astype(np.float32)
+    TriMesh3.update_bvhnode2aabb(d_tri, d_vtx, bvh, aabb, vtx2xyz1=to_dev(v2, torch))
+    assert np.array_equal(bits(to_np(aabb, torch)), bits(oracle.bvhnode2aabb(ref["bvhnodes"], tri, vtx, v2)))
+    assert _status_clear() == 0
+
+
+def test_cpu_tensors_are_rejected():
+    import torch
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    tri = torch.zeros((1, 3), dtype=torch.uint32)
+    vtx = torch.zeros((3, 3), dtype=torch.float32)
+    with pytest.raises(NotImplementedError):
+        TriMesh3.make_bvhnodes_bvhnode2aabb(tri, vtx)

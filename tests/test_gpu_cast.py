@@ -1,0 +1,166 @@
+"""GPU parity of BVH ray casting: hit triangle ids and hit t bit-exact to the
+oracle (del-msh-cpu's near-first recursive search), plus the reference's own
+property tests and the full-size configurations."""
+import math
+
+import numpy as np
+import pytest
+
+from helpers import bits, to_dev, to_np
+
+from del_msh_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+UMAX = 0xFFFFFFFF
+
+
+def _dev_mesh(torch, tri, vtx):
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    d_tri, d_vtx = to_dev(tri, torch), to_dev(vtx, torch)
+    bvh, aabb = TriMesh3.make_bvhnodes_bvhnode2aabb(d_tri, d_vtx)
+    return d_tri, d_vtx, bvh, aabb
+
+
+def _cast_pixels(torch, mesh, m_colmajor, w, h):
+    from del_msh_gb300.Pix2Tri import torch as Pix2Tri
+    m_rowmajor = np.ascontiguousarray(np.asarray(m_colmajor, np.float32).reshape(4, 4).T)
+    p2t, tt = Pix2Tri.by_raycasting(*mesh, to_dev(m_rowmajor, torch), (w, h), return_depth=True)
+    return to_np(p2t, torch), to_np(tt, torch)
+
+
+def _status():
+    from del_msh_gb300 import _native
+    return _native.device_status(clear=True)
+
+
+def test_cast_cfg1_matches_golden(cuda, golden_dir):
+    torch = cuda
+    g = np.load(golden_dir / "oracle_cfg1.npz")
+    mesh = _dev_mesh(torch, g["tri2vtx"], g["vtx2xyz"])
+    p2t, tt = _cast_pixels(torch, mesh, g["ndc2world"], 256, 256)
+    assert np.array_equal(p2t, g["pix2tri"])
+    assert np.array_equal(bits(tt), bits(g["pix2t"]))
+    assert _status() == 0
+
+
+def test_cast_pinhole_torus_matches_oracle(cuda, oracle):
+    torch = cuda
+    tri, vtx = W.displaced_torus(256, seed=11)
+    ref = oracle.build(tri, vtx)
+    m = W.pinhole_ndc2world(W.random_viewpoint(3.0, seed=11), aspect=16 / 9)
+    mesh = _dev_mesh(torch, tri, vtx)
+    p2t, tt = _cast_pixels(torch, mesh, m, 480, 270)
+    r_p2t, r_tt = oracle.pix2tri(tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"], m, 480, 270)
+    assert (p2t != UMAX).mean() > 0.05
+    assert np.array_equal(p2t, r_p2t)
+    assert np.array_equal(bits(tt), bits(r_tt))
+    assert _status() == 0
+
+
+def test_cast_rays_duplicate_soup_deep_tiers(cuda, oracle):
+    """Clustered soup: duplicate Morton codes make chains deeper than the
+    on-chip stack, so the overflow tiers run; ids and t stay bit-exact."""
+    torch = cuda
+    from del_msh_gb300.SearchBvh3 import torch as SearchBvh3
+    tri, vtx = W.clustered_soup(300_000, num_cluster=8, seed=12)
+    ref = oracle.build(tri, vtx)
+    assert oracle.tree_height(ref["bvhnodes"], tri.shape[0]) > 70
+    org, d = W.cube_boundary_rays(60_000, seed=12)
+    # aim a third of the rays at cluster centroids so they go deep
+    cen = oracle.tri2cntr(tri, vtx)[np.random.default_rng(0).integers(0, tri.shape[0], 20_000)]
+    d[:20_000] = cen - org[:20_000]
+    d = d.astype(np.float32)
+    mesh = _dev_mesh(torch, tri, vtx)
+    hit, t, bc = SearchBvh3.first_intersection_ray(to_dev(org, torch), to_dev(d, torch), *mesh, return_bc=True)
+    r_hit, r_t = oracle.cast_rays(org, d, tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"])
+    assert (r_hit != UMAX).sum() > 1000
+    assert np.array_equal(to_np(hit, torch), r_hit)
+    assert np.array_equal(bits(to_np(t, torch)), bits(r_t))
+    bc = to_np(bc, torch)
+    ok = r_hit != UMAX
+    assert np.allclose(bc[ok].sum(1), 1.0, atol=1e-5)
+    assert _status() == 0
+
+
+def test_sphere_rays_inside_unit_ball(cuda):
+    # search_bvh3.rs:247-303
+    torch = cuda
+    from del_msh_gb300.SearchBvh3 import torch as SearchBvh3
+    tri, vtx = W.icosphere(5)
+    mesh = _dev_mesh(torch, tri, vtx)
+    rng = np.random.default_rng(0)
+    n = 1000
+    org = np.stack([rng.random(n) * 2 - 1, rng.random(n) * 2 - 1, np.ones(n)], 1).astype(np.float32)
+    d = np.tile(np.array([0, 0, -1], np.float32), (n, 1))
+    hit, t = SearchBvh3.first_intersection_ray(to_dev(org, torch), to_dev(d, torch), *mesh)
+    hit, t = to_np(hit, torch), to_np(t, torch)
+    m = hit != UMAX
+    p = org[m] + t[m, None] * d[m]
+    assert np.all(np.linalg.norm(p, axis=1) < 1.0 + 1e-6)
+    assert m.sum() > 600
+
+
+def test_silhouette_ratio(cuda):
+    # del-msh-dlpack/tests/test_trimesh.py:54-99
+    torch = cuda
+    tri, vtx = W.icosphere(6, radius=0.8)
+    mesh = _dev_mesh(torch, tri, vtx)
+    p2t, _ = _cast_pixels(torch, mesh, np.eye(4, dtype=np.float32).reshape(-1), 300, 300)
+    assert abs(float((p2t != UMAX).mean()) - 0.8 * 0.8 * math.pi * 0.25) < 2e-3
+
+
+def test_t_error_against_f64(cuda, oracle):
+    """FP64 ray/triangle error of the GPU t (which equals the oracle's)."""
+    torch = cuda
+    g = W.jittered_icosphere(3, seed=0)
+    tri, vtx = g
+    mesh = _dev_mesh(torch, tri, vtx)
+    m = W.ortho_ndc2world()
+    p2t, tt = _cast_pixels(torch, mesh, m, 128, 128)
+    worst = 0.0
+    for i in np.flatnonzero(p2t.reshape(-1) != UMAX)[::7]:
+        o, d = oracle.ray_for_pixel(int(i), 128, 128, m)
+        it = p2t.reshape(-1)[i]
+        t64 = oracle.tri3_ray_f64(vtx[tri[it][0]], vtx[tri[it][1]], vtx[tri[it][2]], o, d)
+        worst = max(worst, abs(float(tt.reshape(-1)[i]) - t64) / abs(t64))
+    assert worst < 1e-6 * 10  # f32 rounding of the MT formula; reported in the bench
+
+
+def test_full_config2_torus(cuda, oracle):
+    """2,097,152-triangle displaced torus, 1920x1080 pinhole camera: build
+    and cast bit-exact to the oracle at full size."""
+    torch = cuda
+    tri, vtx = W.displaced_torus(1024, seed=0)
+    m = W.pinhole_ndc2world(W.random_viewpoint(3.0, seed=0), aspect=1920 / 1080)
+    ref = oracle.build(tri, vtx)
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    got = TriMesh3.make_bvhnodes_bvhnode2aabb_ex(to_dev(tri, torch), to_dev(vtx, torch))
+    assert np.array_equal(to_np(got["bvhnodes"], torch), ref["bvhnodes"])
+    assert np.array_equal(bits(to_np(got["bvhnode2aabb"], torch)), bits(ref["bvhnode2aabb"]))
+    mesh = (to_dev(tri, torch), to_dev(vtx, torch), got["bvhnodes"], got["bvhnode2aabb"])
+    p2t, tt = _cast_pixels(torch, mesh, m, 1920, 1080)
+    r_p2t, r_tt = oracle.pix2tri(tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"], m, 1920, 1080)
+    assert np.array_equal(p2t, r_p2t)
+    assert np.array_equal(bits(tt), bits(r_tt))
+    assert _status() == 0
+
+
+def test_full_config3_soup(cuda, oracle):
+    """4,194,304-triangle clustered soup with duplicate Morton codes: sort,
+    topology and AABBs bit-exact at full size; 1M boundary rays bit-exact."""
+    torch = cuda
+    from del_msh_gb300.SearchBvh3 import torch as SearchBvh3
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    tri, vtx = W.clustered_soup(4_194_304, seed=0)
+    ref = oracle.build(tri, vtx)
+    got = TriMesh3.make_bvhnodes_bvhnode2aabb_ex(to_dev(tri, torch), to_dev(vtx, torch))
+    for k in ("idx2tri", "idx2morton", "bvhnodes"):
+        assert np.array_equal(to_np(got[k], torch), ref[k]), k
+    assert np.array_equal(bits(to_np(got["bvhnode2aabb"], torch)), bits(ref["bvhnode2aabb"]))
+    org, d = W.cube_boundary_rays(1_048_576, seed=0)
+    mesh = (to_dev(tri, torch), to_dev(vtx, torch), got["bvhnodes"], got["bvhnode2aabb"])
+    hit, t = SearchBvh3.first_intersection_ray(to_dev(org, torch), to_dev(d, torch), *mesh)
+    r_hit, r_t = oracle.cast_rays(org, d, tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"])
+    assert np.array_equal(to_np(hit, torch), r_hit)
+    assert np.array_equal(bits(to_np(t, torch)), bits(r_t))
+    assert _status() == 0
