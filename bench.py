@@ -1,0 +1,400 @@
+#!/usr/bin/env python
+"""Benchmark of the LBVH build + BVH ray cast on one GB300 (or N replicas).
+
+Workload (one "step"): the 2,097,152-triangle displaced torus (1024x1024 quad
+grid, R=1, r=0.3, seeded radial displacement of amplitude 0.02 with 8 integer
+frequencies in 1..64) gets a full LBVH build (centroids, fit, Morton codes,
+radix sort, topology, AABBs) and a 1920x1080 pinhole cast (60 degree vertical
+FOV from a seeded viewpoint on the radius-3 sphere), writing the hit triangle
+id and hit t of every pixel.  Inputs are seeded synthetic meshes of that shape.
+
+Metric: rays/s of the whole step (build included), the aggregate over all
+ranks.  Also reported: build-only triangles/s, cast-only rays/s, per-stage
+times, the HBM roofline of the dominant kernel, an end-to-end figure through
+the public torch API with host buffers, and the oracle (CPU restatement of
+del-msh-cpu) timed on the host cores.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With --impl reference the CPU restatement of del-msh-cpu's path (the oracle)
+runs the same workload on the host cores (build on one thread as in the
+reference, cast on every host thread as rayon does) and prints the same line.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "del-msh_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+import numpy as np  # noqa: E402
+
+METRIC = "rays/s (LBVH build + cast per step)"
+UNIT = "rays/s"
+IMG_W, IMG_H = 1920, 1080
+NDIV = 1024
+SEED = 0
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload():
+    from del_msh_gb300 import workloads as W
+    tri, vtx = W.displaced_torus(NDIV, seed=SEED)
+    m = W.pinhole_ndc2world(W.random_viewpoint(3.0, seed=SEED), aspect=IMG_W / IMG_H)
+    return tri, vtx, m
+
+
+def config_dict(tri, vtx):
+    return {
+        "workload": "displaced torus 1024x1024 grid (2,097,152 tris) LBVH build + 1920x1080 pinhole cast",
+        "num_tri": int(tri.shape[0]), "num_vtx": int(vtx.shape[0]), "rays_per_step": IMG_W * IMG_H,
+        "seed": SEED, "l2": "flushed between timed steps (256 MiB write)",
+    }
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def algorithmic_bytes(T: int, V: int, R: int):
+    """Compulsory DRAM bytes per launch of each stage (u32/f32 = 4 B)."""
+    return {
+        "morton": (12 * T + 12 * V) + (12 * T + 12 * V + 8 * T),  # centroid AABB pass + Morton pass
+        "sort": 68 * T,  # 4T histogram + 4 passes x (8T read + 8T write)
+        "topology": 8 * T + 24 * T,
+        "refit": 24 * T + 12 * T + 12 * V + 48 * T + 8 * T,
+        "build": 224 * T + 36 * V,
+        "cast": 8 * R + 72 * T + 12 * T + 12 * V,  # outputs + one read of tree and mesh
+    }
+
+
+# --------------------------------------------------------------- clocks
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-f", self.path], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in pathlib.Path(self.path).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# -------------------------------------------------------------- CPU side
+
+def cpu_step(O, tri, vtx, m, threads: int):
+    """One oracle step: build on one thread (as del-msh-cpu), cast on `threads`."""
+    t0 = time.perf_counter()
+    r = O.build(tri, vtx)
+    t1 = time.perf_counter()
+    O.pix2tri(tri, vtx, r["bvhnodes"], r["bvhnode2aabb"], m, IMG_W, IMG_H, threads=threads)
+    t2 = time.perf_counter()
+    return t1 - t0, t2 - t1
+
+
+def cpu_baseline(tri, vtx, m, reps: int = 3):
+    from oracle import build as obuild
+    from oracle import oracle as O
+    obuild.build_oracle()
+    threads = O.default_threads()
+    cpu_step(O, tri, vtx, m, threads)  # warm-up
+    builds, casts = [], []
+    for _ in range(reps):
+        b, c = cpu_step(O, tri, vtx, m, threads)
+        builds.append(b)
+        casts.append(c)
+    b, c = statistics.median(builds), statistics.median(casts)
+    return {"value": IMG_W * IMG_H / (b + c), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"the full step (build on 1 thread, 1920x1080 cast on {threads} threads), median of {reps}",
+            "build_tris_per_s": tri.shape[0] / b, "cast_rays_per_s": IMG_W * IMG_H / c}
+
+
+# ------------------------------------------------------------- GPU side
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from oracle import build as obuild
+    from oracle import oracle as O
+    obuild.build_oracle()
+    tri, vtx, m = workload()
+    threads = O.default_threads()
+    for _ in range(args.warmup):
+        cpu_step(O, tri, vtx, m, threads)
+    t0 = time.perf_counter()
+    builds, casts = [], []
+    for _ in range(args.steps):
+        b, c = cpu_step(O, tri, vtx, m, threads)
+        builds.append(b)
+        casts.append(c)
+    total = time.perf_counter() - t0
+    step_s = total / args.steps
+    value = IMG_W * IMG_H / step_s
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32/u32", "data": "synthetic (seeded displaced torus)",
+        "config": config_dict(tri, vtx), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{args.steps} full steps (build on 1 thread as del-msh-cpu, cast on {threads} "
+                                   f"threads as its rayon loop)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "build_tris_per_s": tri.shape[0] / statistics.mean(builds),
+        "cast_rays_per_s": IMG_W * IMG_H / statistics.mean(casts),
+        "note": "del-msh-cpu (Rust) cannot be built here; the oracle is its C restatement, bit-exact on this path",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+        pg = dist
+    from del_msh_gb300 import _native
+    from del_msh_gb300.Pix2Tri import torch as Pix2Tri
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+
+    L = _native.load(build_if_missing=True)
+    tri, vtx, m = workload()
+    T, V, R = tri.shape[0], vtx.shape[0], IMG_W * IMG_H
+    d_tri = torch.from_numpy(tri.view(np.int32)).to(dev).view(torch.uint32)
+    d_vtx = torch.from_numpy(vtx).to(dev)
+    d_m = torch.from_numpy(m).to(dev)  # column-major, as the C ABI reads it
+    bvh = torch.empty((2 * T - 1, 3), dtype=torch.int32, device=dev)
+    aabb = torch.empty((2 * T - 1, 6), dtype=torch.float32, device=dev)
+    pix2tri = torch.empty((IMG_H, IMG_W), dtype=torch.int32, device=dev)
+    pix2t = torch.empty((IMG_H, IMG_W), dtype=torch.float32, device=dev)
+    bs = L.dm_trimesh3_build_scratch_bytes(T)
+    cs = L.dm_cast_scratch_bytes(R, T)
+    b_scratch = torch.empty((bs,), dtype=torch.uint8, device=dev)
+    c_scratch = torch.empty((cs,), dtype=torch.uint8, device=dev)
+    flush = torch.empty((L2_FLUSH_BYTES,), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def build():
+        _native.call("dm_trimesh3_make_bvhnodes_bvhnode2aabb", sp, T, d_tri.data_ptr(), V, d_vtx.data_ptr(),
+                     bvh.data_ptr(), aabb.data_ptr(), b_scratch.data_ptr(), bs)
+
+    def cast():
+        _native.call("dm_pix2tri_by_raycast", sp, IMG_W, IMG_H, pix2tri.data_ptr(), pix2t.data_ptr(), T,
+                     d_tri.data_ptr(), V, d_vtx.data_ptr(), bvh.data_ptr(), aabb.data_ptr(), d_m.data_ptr(),
+                     c_scratch.data_ptr(), cs)
+
+    for _ in range(max(args.warmup, 3)):
+        flush.zero_()
+        build()
+        cast()
+    torch.cuda.synchronize()
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.zero_()  # L2 flush, outside the event pair
+        ev[k][0].record(stream)
+        build()
+        ev[k][1].record(stream)
+        cast()
+        ev[k][2].record(stream)
+    barrier()
+    wall = time.perf_counter() - wall0
+    clocks = sampler.stop()
+    build_ms = [ev[k][0].elapsed_time(ev[k][1]) for k in range(args.steps)]
+    cast_ms = [ev[k][1].elapsed_time(ev[k][2]) for k in range(args.steps)]
+    step_ms = statistics.mean(b + c for b, c in zip(build_ms, cast_ms))
+    build_mean, cast_mean = statistics.mean(build_ms), statistics.mean(cast_ms)
+
+    # correctness guard on the timed outputs: status word clean
+    status = _native.device_status(clear=True)
+
+    # per-stage breakdown of the build (CUDA events between stages)
+    stage = (ctypes.c_float * 4)()
+    stage_runs = []
+    for _ in range(max(3, min(args.steps, 20))):
+        flush.zero_()
+        _native.call("dm_trimesh3_build_profiled", sp, T, d_tri.data_ptr(), V, d_vtx.data_ptr(), bvh.data_ptr(),
+                     aabb.data_ptr(), b_scratch.data_ptr(), bs, ctypes.cast(stage, ctypes.c_void_p))
+        stage_runs.append(list(stage))
+    stage_ms = {k: statistics.mean(r[i] for r in stage_runs)
+                for i, k in enumerate(("morton", "sort", "topology", "refit"))}
+
+    # end to end through the public torch API with host buffers
+    h_tri = torch.from_numpy(tri.view(np.int32)).pin_memory()
+    h_vtx = torch.from_numpy(vtx).pin_memory()
+    m_row = torch.from_numpy(np.ascontiguousarray(m.reshape(4, 4).T)).to(dev)
+    e_tri = torch.empty_like(d_tri.view(torch.int32))
+    e_vtx = torch.empty_like(d_vtx)
+    h_p2t = torch.empty((IMG_H, IMG_W), dtype=torch.int32).pin_memory()
+    h_tt = torch.empty((IMG_H, IMG_W), dtype=torch.float32).pin_memory()
+
+    def e2e_step():
+        e_tri.copy_(h_tri, non_blocking=True)
+        e_vtx.copy_(h_vtx, non_blocking=True)
+        t_tri = e_tri.view(torch.uint32)
+        b2, a2 = TriMesh3.make_bvhnodes_bvhnode2aabb(t_tri, e_vtx)
+        p2, t2 = Pix2Tri.by_raycasting(t_tri, e_vtx, b2, a2, m_row, (IMG_W, IMG_H), return_depth=True)
+        h_p2t.copy_(p2.view(torch.int32), non_blocking=True)
+        h_tt.copy_(t2, non_blocking=True)
+
+    for _ in range(3):
+        e2e_step()
+    barrier()
+    e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        e_ev[k][0].record(stream)
+        e2e_step()
+        e_ev[k][1].record(stream)
+    barrier()
+    e2e_ms = statistics.mean(a.elapsed_time(b) for a, b in e_ev)
+    ok = bool(np.array_equal(h_p2t.numpy(), pix2tri.cpu().numpy()))
+
+    if pg is not None:
+        t = torch.tensor([step_ms, e2e_ms, build_mean, cast_mean], device=dev)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        step_ms, e2e_ms, build_mean, cast_mean = (float(x) for x in t.tolist())
+    if rank != 0:
+        if pg is not None:
+            pg.destroy_process_group()
+        return 0
+
+    nbytes = algorithmic_bytes(T, V, R)
+    peak, peak_kind = peaks()
+    stage_all = dict(stage_ms, cast=cast_mean)
+    dom = max(stage_all, key=stage_all.get)
+    dom_ms = stage_all[dom]
+    traffic = read_traffic(dom)
+    achieved = nbytes[dom] / (dom_ms * 1e-3) / 1e9
+    build_gbs = nbytes["build"] / (build_mean * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": world * R / (step_ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/u32", "data": "synthetic (seeded displaced torus)",
+        "config": config_dict(tri, vtx),
+        "build_tris_per_s": world * T / (build_mean * 1e-3), "cast_rays_per_s": world * R / (cast_mean * 1e-3),
+        "build_ms": build_mean, "cast_ms": cast_mean, "stage_ms": stage_ms,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
+                     "algorithmic_bytes": nbytes[dom]},
+        "build_roofline": {"achieved": build_gbs, "peak": peak, "unit": "GB/s", "frac": build_gbs / peak,
+                           "algorithmic_bytes": nbytes["build"]},
+        "e2e": {"value": world * R / (e2e_ms * 1e-3), "unit": UNIT,
+                "h2d_bytes_per_step": int(tri.nbytes + vtx.nbytes), "d2h_bytes_per_step": int(8 * R),
+                "ms_per_step": e2e_ms, "api": "TriMesh3.torch + Pix2Tri.torch", "matches_device_run": ok},
+        "gpu_launches": args.steps * 11,
+        "clocks": clocks,
+        "device_status": status,
+        "wall_s": wall,
+    }
+    if not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(tri, vtx, np.asarray(m))
+    print(json.dumps(line), flush=True)
+    if pg is not None:
+        pg.destroy_process_group()
+    return 0
+
+
+def read_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/ncu_config2.md lines `traffic <kernel> <bytes>`), else None."""
+    p = ROOT / "profiles" / "ncu_config2.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.strip().strip("`").split()
+        if len(parts) == 3 and parts[0] == "traffic" and parts[1] == kernel:
+            return float(parts[2])
+    return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -157,9 +157,12 @@ void sort4(cudaStream_t s, uint32_t n, const uint32_t* k0, uint32_t* ak, uint32_
   dm::launch_onesweep_u32(s, n, 24, ak, av, ok, ov, hist + 768, lookback + 3 * lbw, counters + 3, status);
 }
 
+// ev (optional, 5 events): recorded before the first stage and after each of
+// Morton, sort, topology and refit.
 int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz,
                uint32_t* bvhnodes, float* aabb, float* transform_out, uint32_t* tri2morton_out, uint32_t* idx2tri_out,
-               uint32_t* idx2morton_out, uint32_t* height_out, void* scratch, size_t scratch_bytes) {
+               uint32_t* idx2morton_out, uint32_t* height_out, void* scratch, size_t scratch_bytes,
+               cudaEvent_t* ev = nullptr) {
   if (int e = check_mesh(T, tri2vtx, num_vtx, vtx2xyz)) return e;
   DM_REQUIRE(bvhnodes && aabb, "bvhnodes / bvhnode2aabb must not be NULL");
   cudaStream_t s = as_stream(stream_ptr);
@@ -181,6 +184,7 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   uint32_t* flags = at<uint32_t>(base, L.flags);
   uint32_t* height = at<uint32_t>(base, L.height);
 
+  if (ev) DM_CUDA(cudaEventRecord(ev[0], s));
   dm::launch_centroid_aabb(s, T, tri2vtx, num_vtx, vtx2xyz, at<float>(base, L.partials),
                            at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status);
   dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status);
@@ -190,9 +194,13 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   // sorted keys; pass 3 only reads (ak, av).
   uint32_t* ok = idx2morton_out ? idx2morton_out : codes;
   uint32_t* ov = idx2tri_out ? idx2tri_out : bv;
+  if (ev) DM_CUDA(cudaEventRecord(ev[1], s));
   sort4(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
+  if (ev) DM_CUDA(cudaEventRecord(ev[2], s));
   dm::launch_topology(s, T, ok, ov, bvhnodes);
+  if (ev) DM_CUDA(cudaEventRecord(ev[3], s));
   dm::launch_refit(s, T, bvhnodes, tri2vtx, num_vtx, vtx2xyz, nullptr, aabb, flags, height, status);
+  if (ev) DM_CUDA(cudaEventRecord(ev[4], s));
   if (transform_out) DM_CUDA(cudaMemcpyAsync(transform_out, transform, 64, cudaMemcpyDeviceToDevice, s));
   if (height_out) DM_CUDA(cudaMemcpyAsync(height_out, height, 4, cudaMemcpyDeviceToDevice, s));
   DM_CUDA(cudaGetLastError());
@@ -300,6 +308,23 @@ int dm_trimesh3_build_ex(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* 
                          uint32_t* height_out, void* scratch, size_t scratch_bytes) {
   return build_impl(stream_ptr, num_tri, tri2vtx, num_vtx, vtx2xyz, bvhnodes, bvhnode2aabb, transform_out,
                     tri2morton_out, idx2tri_out, idx2morton_out, height_out, scratch, scratch_bytes);
+}
+
+int dm_trimesh3_build_profiled(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                               const float* vtx2xyz, uint32_t* bvhnodes, float* bvhnode2aabb, void* scratch,
+                               size_t scratch_bytes, float* stage_ms) {
+  DM_REQUIRE(stage_ms, "stage_ms must not be NULL");
+  cudaEvent_t ev[5] = {};
+  for (auto& e : ev) DM_CUDA(cudaEventCreate(&e));
+  int rc = build_impl(stream_ptr, num_tri, tri2vtx, num_vtx, vtx2xyz, bvhnodes, bvhnode2aabb, nullptr, nullptr,
+                      nullptr, nullptr, nullptr, scratch, scratch_bytes, ev);
+  if (rc == DM_OK) {
+    const cudaError_t e = cudaEventSynchronize(ev[4]);
+    if (e != cudaSuccess) rc = cuda_fail(e, "cudaEventSynchronize");
+    for (int i = 0; rc == DM_OK && i < 4; ++i) cudaEventElapsedTime(stage_ms + i, ev[i], ev[i + 1]);
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  return rc;
 }
 
 size_t dm_cast_scratch_bytes(uint32_t num_ray, uint32_t num_tri) { return dm::cast_scratch_bytes(num_ray, num_tri); }

@@ -27,6 +27,7 @@ _SIGNATURES = {
     "dm_trimesh3_make_bvhnodes_bvhnode2aabb": (i32, [u64, u32, vp, u32, vp, vp, vp, vp, sz]),
     "dm_trimesh3_build_scratch_bytes": (sz, [u32]),
     "dm_trimesh3_build_ex": (i32, [u64, u32, vp, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, sz]),
+    "dm_trimesh3_build_profiled": (i32, [u64, u32, vp, u32, vp, vp, vp, vp, sz, vp]),
     "dm_pix2tri_by_raycast": (i32, [u64, u32, u32, vp, vp, u32, vp, u32, vp, vp, vp, vp, vp, sz]),
     "dm_search_bvh3_first_intersection_ray": (i32, [u64, u32, vp, vp, vp, vp, vp, u32, vp, u32, vp, vp, vp, vp, sz]),
     "dm_cast_scratch_bytes": (sz, [u32, u32]),

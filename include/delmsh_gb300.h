@@ -122,6 +122,14 @@ int dm_trimesh3_build_ex(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* 
                          uint32_t* tri2morton_out, uint32_t* idx2tri_out, uint32_t* idx2morton_out,
                          uint32_t* height_out, void* scratch, size_t scratch_bytes);
 
+/* The whole build with CUDA-event timing of its stages; synchronizes the
+ * stream.  stage_ms (host, 4 floats): [0] centroid AABB + Morton codes (with
+ * the sort's digit histogram), [1] radix sort, [2] topology, [3] AABB refit.
+ * Diagnostics for benchmarks; no reference counterpart. */
+int dm_trimesh3_build_profiled(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                               const float* vtx2xyz, uint32_t* bvhnodes, float* bvhnode2aabb, void* scratch,
+                               size_t scratch_bytes, float* stage_ms);
+
 /* Closest hit per pixel of an img_w x img_h image; pixel (iw, ih) casts the
  * ray of ray_for_pixel.h (origin at ndc z=+1, towards z=-1).  pix2tri[ih*w+iw]
  * = triangle or u32::MAX; pix2t (optional) = ray coefficient t of the hit

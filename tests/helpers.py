@@ -16,4 +16,9 @@ def to_np(t, torch):
 
 
 def bits(a):
+    """Raw bits for exact comparison; every NaN is mapped to one pattern (NaN
+    payloads differ between x86, Arm and CUDA and carry no information here)."""
+    a = np.array(a, copy=True)
+    if a.dtype == np.float32:
+        a[np.isnan(a)] = np.float32("nan")
     return np.ascontiguousarray(a).view(np.uint32)

@@ -15,12 +15,17 @@ def _status_clear():
     return _native.device_status(clear=True)
 
 
-def test_morton_points_match_reference_code(cuda, golden_dir):
+def test_morton_points_match_reference_code(cuda, oracle, golden_dir):
+    """Finite points through the identity transform give the reference's own
+    morton_code3 values; every point (NaN / inf included, where 0*inf makes
+    the homogeneous w NaN) gives the oracle's value."""
     torch = cuda
     from del_msh_gb300.Mortons import torch as Mortons
     g = np.load(golden_dir / "ref_morton.npz")
-    got = Mortons.make_vtx2morton_from_vtx2co(to_dev(g["pts"], torch), torch.eye(4, device="cuda:0"))
-    assert np.array_equal(to_np(got, torch), g["codes"])
+    got = to_np(Mortons.make_vtx2morton_from_vtx2co(to_dev(g["pts"], torch), torch.eye(4, device="cuda:0")), torch)
+    finite = np.isfinite(g["pts"]).all(1)
+    assert np.array_equal(got[finite], g["codes"][finite])
+    assert np.array_equal(got, oracle.vtx2morton(g["pts"], np.eye(4, dtype=np.float32).reshape(-1)))
 
 
 @pytest.mark.parametrize("dim", [2, 3])
