@@ -209,6 +209,22 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
 
 }  // namespace
 
+namespace dm {
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+uint32_t* device_status_word() { return status_ptr(); }
+
+}  // namespace dm
+
 extern "C" {
 
 const char* dm_version(void) { return "delmsh_gb300 0.1.0 (sm_103a)"; }

@@ -7,6 +7,12 @@
 
 namespace dm {
 
+// ----------------------------------------------------------------- capi.cu
+// Records the message that dm_last_error() returns on this thread; returns code.
+int set_error(int code, const char* fmt, ...);
+// Device address of the library's status word on the current device (or nullptr).
+uint32_t* device_status_word();
+
 // ---------------------------------------------------------------- build.cu
 constexpr int kAabbBlocks = 1024;  // upper bound on centroid-AABB reduction blocks
 

@@ -24,6 +24,7 @@ _SIGNATURES = {
     "dm_array1d_argsort_scratch_bytes": (sz, [u32]),
     "dm_mortons_make_bvhnodes_from_sorted_mortons": (i32, [u64, u32, vp, vp, vp]),
     "dm_bvhnode2aabb_update_aabb": (i32, [u64, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp]),
+    "dm_bvhnode2aabb_update_aabb_noalloc": (i32, [u64, u32, vp, vp, u32, vp, u32, vp, vp]),
     "dm_trimesh3_make_bvhnodes_bvhnode2aabb": (i32, [u64, u32, vp, u32, vp, vp, vp, vp, sz]),
     "dm_trimesh3_build_scratch_bytes": (sz, [u32]),
     "dm_trimesh3_build_ex": (i32, [u64, u32, vp, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, sz]),

@@ -101,6 +101,20 @@ int dm_bvhnode2aabb_update_aabb(uint64_t stream_ptr, uint32_t num_bvhnode, float
                                 const uint32_t* elem2vtx, uint32_t num_vtx, const float* vtx2xyz0,
                                 const float* vtx2xyz1, uint32_t* flags_scratch);
 
+/* dm_bvhnode2aabb_update_aabb for callers that cannot allocate device memory
+ * (a per-frame refit loop under a no-allocation rule, a plugin whose host owns
+ * the CUDA allocator, an FFI caller holding only its own arrays): the arrival
+ * flags live in a static device array inside the library instead of caller
+ * scratch or a temporary allocation, and the call allocates nothing.  Meshes
+ * of 1..4194305 triangles (16 MiB of flags, held by every GPU that loads the
+ * library until exit); larger ones return DM_ERR_INVALID_ARGUMENT.  The first
+ * call on a device looks up the array's address (do it before any stream
+ * capture).  Calls share the array: each clears the part it uses, and calls
+ * that overlap on the GPU race.  No counterpart in the reference. */
+int dm_bvhnode2aabb_update_aabb_noalloc(uint64_t stream_ptr, uint32_t num_bvhnode, float* bvhnode2aabb,
+                                        const uint32_t* bvhnodes, uint32_t num_elem, const uint32_t* elem2vtx,
+                                        uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1);
+
 /* Whole LBVH build of a triangle mesh: centroids, centroid AABB, fit into the
  * unit cube, Morton codes, stable radix sort, topology, AABBs.
  * Replaces: del-msh-dlpack/del_msh_dlpack/TriMesh3/torch.py:233-285
