@@ -2,6 +2,7 @@
 // (with the radix sort's digit histogram fused in), Karras topology and the
 // bottom-up AABB refit.  All of them are HBM-bound integer / min-max work.
 #include <cfloat>
+#include <cuda/atomic>
 
 #include "dm_device.cuh"
 #include "dm_internal.h"
@@ -369,6 +370,10 @@ __device__ __forceinline__ Box leaf_box(const uint32_t* __restrict__ tri2vtx, ui
 // from_two_aabbs(child0, child1).  The arrival word also carries the height
 // of the first-arriving subtree, so the climb yields the tree height for free,
 // and the second arriver clears the word so the flags stay zero between calls.
+// The arrival is an acquire-release atomic: it publishes the arriving child's
+// box (stored just before) and, for the second arriver, makes the sibling's
+// box visible, without a full memory fence per level.  The climbing thread
+// keeps its own child's box in registers and loads only the sibling's.
 __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint32_t* __restrict__ bvhnodes,
                                                    const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
                                                    const float* __restrict__ vtx2xyz0,
@@ -387,6 +392,7 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
   if (vtx2xyz1) b = box_union(b, leaf_box(tri2vtx, num_vtx, vtx2xyz1, it, status));
   box_store(aabb + static_cast<size_t>(leaf) * 6, b);
   uint32_t h = 1;
+  uint32_t prev = leaf;
   uint32_t node = __ldg(bvhnodes + static_cast<size_t>(leaf) * 3);
   uint32_t guard = 0;
   while (node != kUMax) {
@@ -394,21 +400,25 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
       raise_status(status, kStatusBadIndex);
       return;
     }
-    __threadfence();
-    const uint32_t old = atomicAdd(flags + node, h);
-    if (old == 0u) return;  // the sibling subtree is not finished yet
-    flags[node] = 0u;
-    __threadfence();
-    h = (old > h ? old : h) + 1;
+    // the record is read-only: fetch it while the arrival atomic is in flight
+    const uint32_t parent = __ldg(bvhnodes + static_cast<size_t>(node) * 3);
     const uint32_t c0 = __ldg(bvhnodes + static_cast<size_t>(node) * 3 + 1);
     const uint32_t c1 = __ldg(bvhnodes + static_cast<size_t>(node) * 3 + 2);
-    if (c0 >= num_node || c1 >= num_node) {
+    cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrival(flags[node]);
+    const uint32_t old = arrival.fetch_add(h, cuda::memory_order_acq_rel);
+    if (old == 0u) return;  // the sibling subtree is not finished yet
+    flags[node] = 0u;
+    h = (old > h ? old : h) + 1;
+    if (c0 >= num_node || c1 >= num_node || (c0 != prev && c1 != prev)) {
       raise_status(status, kStatusBadIndex);
       return;
     }
-    const Box u = box_union(box_load_cg(aabb + static_cast<size_t>(c0) * 6), box_load_cg(aabb + static_cast<size_t>(c1) * 6));
-    box_store(aabb + static_cast<size_t>(node) * 6, u);
-    node = __ldg(bvhnodes + static_cast<size_t>(node) * 3);
+    const bool mine_first = (c0 == prev);
+    const Box sib = box_load_cg(aabb + static_cast<size_t>(mine_first ? c1 : c0) * 6);
+    b = mine_first ? box_union(b, sib) : box_union(sib, b);
+    box_store(aabb + static_cast<size_t>(node) * 6, b);
+    prev = node;
+    node = parent;
   }
   if (height_out) *height_out = h;
 }

@@ -360,7 +360,7 @@ int dm_pix2tri_by_raycast(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, u
   if (int e = sc.acquire(scratch, scratch_bytes, dm::cast_scratch_bytes(n, num_tri), s, nullptr)) return e;
   dm::CastScratch cs;
   dm::cast_scratch_carve(sc.ptr, n, num_tri, &cs);
-  DM_CUDA(cudaMemsetAsync(cs.counters, 0, 8, s));
+  DM_CUDA(cudaMemsetAsync(cs.counters, 0, 16, s));
   dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb};
   dm::CastOut o{pix2tri, pix2t, nullptr};
   dm::launch_cast_pixels(s, img_w, img_h, transform_ndc2world, m, o, cs, status_ptr());
@@ -382,7 +382,7 @@ int dm_search_bvh3_first_intersection_ray(uint64_t stream_ptr, uint32_t num_ray,
   if (int e = sc.acquire(scratch, scratch_bytes, dm::cast_scratch_bytes(num_ray, num_tri), s, nullptr)) return e;
   dm::CastScratch cs;
   dm::cast_scratch_carve(sc.ptr, num_ray, num_tri, &cs);
-  DM_CUDA(cudaMemsetAsync(cs.counters, 0, 8, s));
+  DM_CUDA(cudaMemsetAsync(cs.counters, 0, 16, s));
   dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb};
   dm::CastOut o{hit_tri, hit_t, hit_bc};
   dm::launch_cast_rays(s, num_ray, ray_org, ray_dir, m, o, cs, status_ptr());

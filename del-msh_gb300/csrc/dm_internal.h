@@ -88,7 +88,7 @@ struct CastOut {
 };
 
 struct CastScratch {
-  uint32_t* counters;  // 2 words, zero on entry (left zero)
+  uint32_t* counters;  // 4 words, zero on entry: work counter, two overflow counts
   uint32_t* list1;     // num_ray words
   uint32_t* list2;     // num_ray words
   void* pool;          // >= 16 * max(num_tri, 4096) bytes

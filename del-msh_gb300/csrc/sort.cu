@@ -73,7 +73,7 @@ struct SortSmem {
 };
 
 template <typename KeyT, bool kIota>
-__global__ void __launch_bounds__(kThreads) k_onesweep(const KeyT* __restrict__ keys_in,
+__global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_onesweep(const KeyT* __restrict__ keys_in,
                                                       const uint32_t* __restrict__ vals_in, KeyT* __restrict__ keys_out,
                                                       uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift,
                                                       const uint32_t* __restrict__ hist, uint32_t* lookback,
