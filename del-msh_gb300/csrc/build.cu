@@ -237,20 +237,28 @@ __global__ void __launch_bounds__(kThreads) k_vtx2morton(uint32_t n, uint32_t nu
 
 // ----------------------------------------------------------------- topology
 
-__device__ __forceinline__ int delta_of(const uint32_t* __restrict__ c, uint32_t i, uint32_t j) {
-  return __clz(__ldg(c + i) ^ __ldg(c + j));
-}
+// Code / object accessors: the single-mesh arrays, or a segment of the
+// batched sort's (mesh << 30 | code) keys and global triangle indices.
+struct Codes32 {
+  const uint32_t* p;
+  __device__ __forceinline__ uint32_t operator()(uint32_t i) const { return __ldg(p + i); }
+};
+struct Objs32 {
+  const uint32_t* p;
+  __device__ __forceinline__ uint32_t operator()(uint32_t i) const { return __ldg(p + i); }
+};
 
 // Last index of the run of value v that contains position `from` (sorted c).
 // Equal to the linear scan of mortons.rs:235-245, found by galloping search.
-__device__ __forceinline__ uint32_t run_end(const uint32_t* __restrict__ c, uint32_t n, uint32_t from, uint32_t v) {
+template <typename Codes>
+__device__ __forceinline__ uint32_t run_end(const Codes& c, uint32_t n, uint32_t from, uint32_t v) {
   uint32_t lo = from;  // c[lo] == v
   uint32_t step = 1;
   uint32_t hi = n;     // first index known to differ (or n)
   for (;;) {
     const uint64_t probe = static_cast<uint64_t>(lo) + step;
     if (probe >= n) break;
-    if (__ldg(c + probe) != v) {
+    if (c(static_cast<uint32_t>(probe)) != v) {
       hi = static_cast<uint32_t>(probe);
       break;
     }
@@ -259,23 +267,25 @@ __device__ __forceinline__ uint32_t run_end(const uint32_t* __restrict__ c, uint
   }
   while (hi - lo > 1) {  // invariant: c[lo] == v, hi == n or c[hi] != v
     const uint32_t mid = lo + (hi - lo) / 2;
-    if (__ldg(c + mid) == v) lo = mid;
+    if (c(mid) == v) lo = mid;
     else hi = mid;
   }
   return lo;
 }
 
-// mortons.rs:221-288 (range) and 290-325 (split), bvhnodes_morton.rs:24-47.
-__global__ void __launch_bounds__(kThreads) k_topology(uint32_t n, const uint32_t* __restrict__ c,
-                                                      const uint32_t* __restrict__ idx2obj, uint32_t* bvhnodes) {
-  const uint32_t ib = blockIdx.x * kThreads + threadIdx.x;
-  if (ib >= n - 1) return;
+// One branch ib of the radix tree over n sorted codes: mortons.rs:221-288
+// (range), 290-325 (split) and bvhnodes_morton.rs:24-47 (writes).  The
+// branch index is always one end of its range; the other end is written to
+// other_end[ib] when other_end != nullptr (used by the windowed refit).
+template <typename Codes, typename Objs>
+__device__ __forceinline__ void topology_node(uint32_t n, const Codes& c, const Objs& obj, uint32_t* bvhnodes,
+                                              uint32_t ib, uint32_t* other_end) {
   uint32_t r0, r1;
   if (ib == 0) {
     r0 = 0;
     r1 = n - 1;
   } else {
-    const uint32_t mc0 = __ldg(c + ib - 1), mc1 = __ldg(c + ib), mc2 = __ldg(c + ib + 1);
+    const uint32_t mc0 = c(ib - 1), mc1 = c(ib), mc2 = c(ib + 1);
     if (mc0 == mc1 && mc1 == mc2) {
       r0 = ib;
       r1 = run_end(c, n, ib + 1, mc1);
@@ -287,37 +297,34 @@ __global__ void __launch_bounds__(kThreads) k_topology(uint32_t n, const uint32_
       for (;;) {
         const int64_t j = static_cast<int64_t>(ib) + lmax * d;
         if (j < 0 || j >= static_cast<int64_t>(n)) break;
-        if (delta_of(c, ib, static_cast<uint32_t>(j)) <= delta_min) break;
+        if (__clz(mc1 ^ c(static_cast<uint32_t>(j))) <= delta_min) break;
         lmax *= 2;
       }
       int64_t l = 0;
       for (int64_t t = lmax / 2; t >= 1; t /= 2) {
         const int64_t j = static_cast<int64_t>(ib) + (l + t) * d;
-        if (j >= 0 && j < static_cast<int64_t>(n) && delta_of(c, ib, static_cast<uint32_t>(j)) > delta_min) l += t;
+        if (j >= 0 && j < static_cast<int64_t>(n) && __clz(mc1 ^ c(static_cast<uint32_t>(j))) > delta_min) l += t;
       }
       const uint32_t j = static_cast<uint32_t>(static_cast<int64_t>(ib) + l * d);
       r0 = ib <= j ? ib : j;
       r1 = ib <= j ? j : ib;
     }
   }
-  // split
-  uint32_t isplit;
+  uint32_t isplit = r0;
   {
-    const uint32_t mc_start = __ldg(c + r0);
-    const int common = __clz(mc_start ^ __ldg(c + r1));
-    if (common == 32) {
-      isplit = r0;
-    } else {
-      isplit = r0;
+    const uint32_t mc_start = c(r0);
+    const int common = __clz(mc_start ^ c(r1));
+    if (common != 32) {
       uint32_t step = r1 - r0;
       while (step > 1) {
         step = (step + 1) / 2;
         const uint32_t cand = isplit + step;
         if (cand >= r1) continue;
-        if (__clz(mc_start ^ __ldg(c + cand)) > common) isplit = cand;
+        if (__clz(mc_start ^ c(cand)) > common) isplit = cand;
       }
     }
   }
+  if (other_end) other_end[ib] = (r0 == ib) ? r1 : r0;
   const uint32_t nb = n - 1;
   uint32_t* me = bvhnodes + static_cast<size_t>(ib) * 3;
   if (r0 == isplit) {
@@ -325,7 +332,7 @@ __global__ void __launch_bounds__(kThreads) k_topology(uint32_t n, const uint32_
     me[1] = a;
     uint32_t* la = bvhnodes + static_cast<size_t>(a) * 3;
     la[0] = ib;
-    la[1] = __ldg(idx2obj + isplit);
+    la[1] = obj(isplit);
     la[2] = kUMax;
   } else {
     me[1] = isplit;
@@ -336,13 +343,21 @@ __global__ void __launch_bounds__(kThreads) k_topology(uint32_t n, const uint32_
     me[2] = b;
     uint32_t* lb = bvhnodes + static_cast<size_t>(b) * 3;
     lb[0] = ib;
-    lb[1] = __ldg(idx2obj + isplit + 1);
+    lb[1] = obj(isplit + 1);
     lb[2] = kUMax;
   } else {
     me[2] = isplit + 1;
     bvhnodes[static_cast<size_t>(isplit + 1) * 3] = ib;
   }
   if (ib == 0) me[0] = kUMax;
+}
+
+__global__ void __launch_bounds__(kThreads) k_topology(uint32_t n, const uint32_t* __restrict__ c,
+                                                      const uint32_t* __restrict__ idx2obj, uint32_t* bvhnodes,
+                                                      uint32_t* other_end) {
+  const uint32_t ib = blockIdx.x * kThreads + threadIdx.x;
+  if (ib >= n - 1) return;
+  topology_node(n, Codes32{c}, Objs32{idx2obj}, bvhnodes, ib, other_end);
 }
 
 // A single object: the one-leaf tree [MAX, obj, MAX] (the reference leaves
@@ -423,6 +438,122 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
   if (height_out) *height_out = h;
 }
 
+// Windowed refit.  Block b owns the kWinLeaves sorted leaves starting at
+// b*kWinLeaves (global leaf order, across the meshes of a batch).  A branch
+// whose whole leaf range lies in the window (known from other_end: a branch
+// index is one end of its range) gets both arrivals from this block, so its
+// arrival counter and both child boxes live in shared memory and need only
+// block-scope ordering; only branches whose range crosses a window edge (about
+// 2 per window per tree level above the window) use the global acquire-release
+// arrival of k_refit.  Values and merge order are those of k_refit.
+constexpr int kWinLeaves = 1024;
+constexpr int kWinThreads = 256;
+
+struct WinSmem {
+  uint32_t flag[kWinLeaves];
+  Box leaf[kWinLeaves];
+  Box node[kWinLeaves];
+};
+
+__device__ __forceinline__ uint32_t mesh_of_leaf(const Segments& seg, uint32_t i) {
+  uint32_t lo = 0, hi = seg.num_mesh;  // tri_off[lo] <= i < tri_off[hi]
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) / 2;
+    if (__ldg(seg.tri_off + mid) <= i) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+template <bool kBatch>
+__global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, Segments seg, uint32_t num_vtx_single,
+                                                          const uint32_t* __restrict__ bvhnodes_all,
+                                                          const uint32_t* __restrict__ other_all,
+                                                          const uint32_t* __restrict__ tri2vtx_all,
+                                                          const float* __restrict__ vtx0_all,
+                                                          const float* __restrict__ vtx1_all, float* aabb_all,
+                                                          uint32_t* gflags_all, uint32_t* height_out,
+                                                          uint32_t* status) {
+  extern __shared__ __align__(16) unsigned char win_raw[];
+  WinSmem& S = *reinterpret_cast<WinSmem*>(win_raw);
+  const uint32_t wA = blockIdx.x * kWinLeaves;
+  for (int k = threadIdx.x; k < kWinLeaves; k += kWinThreads) S.flag[k] = 0u;
+  __syncthreads();
+  for (uint32_t k = threadIdx.x; k < static_cast<uint32_t>(kWinLeaves); k += kWinThreads) {
+    const uint32_t i = wA + k;
+    if (i >= total_tri) break;
+    uint32_t m = 0, t0 = 0, T = total_tri, v0 = 0, V = num_vtx_single;
+    if (kBatch) {
+      m = mesh_of_leaf(seg, i);
+      t0 = __ldg(seg.tri_off + m);
+      T = __ldg(seg.tri_off + m + 1) - t0;
+      v0 = __ldg(seg.vtx_off + m);
+      V = __ldg(seg.vtx_off + m + 1) - v0;
+    }
+    const size_t node_off = 2ull * t0 - m, int_off = static_cast<size_t>(t0) - m;
+    const uint32_t* bn = bvhnodes_all + 3 * node_off;
+    const uint32_t* oe = other_all + int_off;
+    float* aabb = aabb_all + 6 * node_off;
+    uint32_t* gflags = gflags_all + int_off;
+    const uint32_t* t2v = tri2vtx_all + 3ull * t0;
+    const float* x0 = vtx0_all + 3ull * v0;
+    const float* x1 = vtx1_all ? vtx1_all + 3ull * v0 : nullptr;
+    const uint32_t num_node = 2 * T - 1;
+    const uint32_t leaf = T - 1 + (i - t0);
+    const uint32_t it = __ldg(bn + static_cast<size_t>(leaf) * 3 + 1);
+    if (it >= T) {
+      raise_status(status, kStatusBadIndex);
+      continue;
+    }
+    Box b = leaf_box(t2v, V, x0, it, status);
+    if (x1) b = box_union(b, leaf_box(t2v, V, x1, it, status));
+    box_store(aabb + static_cast<size_t>(leaf) * 6, b);
+    S.leaf[k] = b;
+    uint32_t h = 1, prev = leaf, guard = 0;
+    uint32_t node = __ldg(bn + static_cast<size_t>(leaf) * 3);
+    while (node != kUMax) {
+      if (node >= T - 1 || ++guard > num_node) {
+        raise_status(status, kStatusBadIndex);
+        break;
+      }
+      const uint32_t parent = __ldg(bn + static_cast<size_t>(node) * 3);
+      const uint32_t c0 = __ldg(bn + static_cast<size_t>(node) * 3 + 1);
+      const uint32_t c1 = __ldg(bn + static_cast<size_t>(node) * 3 + 2);
+      const uint32_t other = __ldg(oe + node);
+      const uint32_t lo = node < other ? node : other, hi = node < other ? other : node;
+      const bool local = (t0 + lo >= wA) && (t0 + hi < wA + kWinLeaves);
+      uint32_t old;
+      if (local) {
+        __threadfence_block();  // this thread's shared box is visible before the arrival
+        old = atomicAdd(&S.flag[t0 + node - wA], h);
+        if (old == 0u) break;
+        __threadfence_block();
+      } else {
+        cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrival(gflags[node]);
+        old = arrival.fetch_add(h, cuda::memory_order_acq_rel);
+        if (old == 0u) break;
+        gflags[node] = 0u;
+      }
+      h = (old > h ? old : h) + 1;
+      if (c0 >= num_node || c1 >= num_node || (c0 != prev && c1 != prev)) {
+        raise_status(status, kStatusBadIndex);
+        break;
+      }
+      const bool mine_first = (c0 == prev);
+      const uint32_t sib = mine_first ? c1 : c0;
+      Box sb;
+      if (local) sb = (sib >= T - 1) ? S.leaf[t0 + (sib - (T - 1)) - wA] : S.node[t0 + sib - wA];
+      else sb = box_load_cg(aabb + static_cast<size_t>(sib) * 6);
+      b = mine_first ? box_union(b, sb) : box_union(sb, b);
+      box_store(aabb + static_cast<size_t>(node) * 6, b);
+      if (local) S.node[t0 + node - wA] = b;
+      prev = node;
+      node = parent;
+    }
+    if (node == kUMax && height_out) height_out[m] = h;
+  }
+}
+
 }  // namespace
 
 // ------------------------------------------------------------- launchers
@@ -453,13 +584,31 @@ void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float
 }
 
 void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, const uint32_t* idx2obj,
-                     uint32_t* bvhnodes) {
+                     uint32_t* bvhnodes, uint32_t* other_end) {
   if (n == 1) {
     k_topology_single<<<1, 1, 0, s>>>(idx2obj, bvhnodes);
     return;
   }
   const uint32_t grid = (n - 1 + kThreads - 1) / kThreads;
-  k_topology<<<grid, kThreads, 0, s>>>(n, idx2morton, idx2obj, bvhnodes);
+  k_topology<<<grid, kThreads, 0, s>>>(n, idx2morton, idx2obj, bvhnodes, other_end);
+}
+
+void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
+                           const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
+                           const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
+                           uint32_t* height_out, uint32_t* status) {
+  if (total_tri == 0) return;
+  const int smem = static_cast<int>(sizeof(WinSmem));
+  const uint32_t grid = (total_tri + kWinLeaves - 1) / kWinLeaves;
+  if (seg.tri_off) {
+    cudaFuncSetAttribute(k_refit_win<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k_refit_win<true><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
+                                                      vtx2xyz0, vtx2xyz1, aabb, flags, height_out, status);
+  } else {
+    cudaFuncSetAttribute(k_refit_win<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    k_refit_win<false><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
+                                                       vtx2xyz0, vtx2xyz1, aabb, flags, height_out, status);
+  }
 }
 
 void launch_refit(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,

@@ -197,9 +197,11 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   if (ev) DM_CUDA(cudaEventRecord(ev[1], s));
   sort4(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
   if (ev) DM_CUDA(cudaEventRecord(ev[2], s));
-  dm::launch_topology(s, T, ok, ov, bvhnodes);
+  uint32_t* other_end = ak;  // the sort's A buffers are dead after pass 3
+  dm::launch_topology(s, T, ok, ov, bvhnodes, other_end);
   if (ev) DM_CUDA(cudaEventRecord(ev[3], s));
-  dm::launch_refit(s, T, bvhnodes, tri2vtx, num_vtx, vtx2xyz, nullptr, aabb, flags, height, status);
+  dm::launch_refit_windowed(s, T, dm::Segments{1, nullptr, nullptr}, num_vtx, bvhnodes, other_end, tri2vtx, vtx2xyz,
+                            nullptr, aabb, flags, height, status);
   if (ev) DM_CUDA(cudaEventRecord(ev[4], s));
   if (transform_out) DM_CUDA(cudaMemcpyAsync(transform_out, transform, 64, cudaMemcpyDeviceToDevice, s));
   if (height_out) DM_CUDA(cudaMemcpyAsync(height_out, height, 4, cudaMemcpyDeviceToDevice, s));

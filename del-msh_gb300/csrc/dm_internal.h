@@ -33,9 +33,11 @@ void launch_morton_tri(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx
 void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float* vtx2co, const float* transform,
                        uint32_t* out);
 
-// bvhnodes_morton.rs:10-50 / bvhnodes_morton.cu:29-72.
+// bvhnodes_morton.rs:10-50 / bvhnodes_morton.cu:29-72.  other_end (optional,
+// u32[n-1]): for each branch the end of its leaf range that is not its own
+// index (a branch index is always one end of its range).
 void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, const uint32_t* idx2obj,
-                     uint32_t* bvhnodes);
+                     uint32_t* bvhnodes, uint32_t* other_end = nullptr);
 
 // Vertex indices >= num_vtx are replaced by 0 and raise kStatusBadIndex.
 // Bottom-up refit (bvhnode2aabb.cu:7-65 semantics, values of
@@ -44,6 +46,25 @@ void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, con
 void launch_refit(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,
                   uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags, uint32_t* height_out,
                   uint32_t* status);
+
+// Meshes of a batch stored back to back: mesh m owns triangles
+// tri_off[m]..tri_off[m+1]-1 and vertices vtx_off[m]..vtx_off[m+1]-1, and its
+// nodes start at node 2*tri_off[m]-m (branch words at tri_off[m]-m); indices
+// stored inside a mesh's arrays are local to that mesh.  A single mesh is
+// {1, nullptr, nullptr}.  Every mesh has at least one triangle.
+struct Segments {
+  uint32_t num_mesh;
+  const uint32_t* tri_off;  // device, num_mesh+1 entries
+  const uint32_t* vtx_off;  // device, num_mesh+1 entries
+};
+
+// Refit of trees built by launch_topology with other_end: the same boxes as
+// launch_refit, with most merges done in shared memory (see k_refit_win).
+// height_out (optional) receives one height per mesh.
+void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
+                           const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
+                           const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
+                           uint32_t* height_out, uint32_t* status);
 
 // ----------------------------------------------------------------- sort.cu
 constexpr int kSortTile = 3840;  // keys per onesweep tile

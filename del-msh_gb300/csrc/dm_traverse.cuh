@@ -100,11 +100,18 @@ struct GlobalStack {
 
 // Per-ray traversal state between steps.
 struct Trav {
-  uint32_t node;   // node to enter next
-  uint32_t sp;     // frames in use
-  uint32_t steps;  // node entries so far (bounded by the node count)
-  Hit best;        // accumulator of the current level
+  uint32_t node;         // node to enter next
+  uint32_t left, right;  // its record (bvhnodes[node*3+1], [node*3+2]), fetched ahead
+  uint32_t sp;           // frames in use
+  uint32_t steps;        // node entries so far (bounded by the node count)
+  Hit best;              // accumulator of the current level
 };
+
+__device__ __forceinline__ void load_record(const uint32_t* __restrict__ bn, uint32_t n, uint32_t& left,
+                                            uint32_t& right) {
+  left = __ldg(bn + static_cast<size_t>(n) * 3 + 1);
+  right = __ldg(bn + static_cast<size_t>(n) * 3 + 2);
+}
 
 enum StepResult : int { kStepContinue = 0, kStepDone = 1, kStepOverflow = 2 };
 
@@ -114,13 +121,16 @@ __device__ __forceinline__ bool trav_begin(const MeshView& m, const Ray& r, Trav
   s.sp = 0;
   s.steps = 0;
   s.best = Hit{INFINITY, kUMax};
+  load_record(m.bvhnodes, 0, s.left, s.right);
   float te, tx;
   return node_slab(m, r, 0, te, tx);
 }
 
 // One node entry and the ascent that follows it.  On kStepDone the ray's
-// result is s.best.  A malformed tree (child index out of range, or more node
-// entries than the tree has nodes) finishes the ray and sets `bad`.
+// result is s.best.  The records of both children are fetched together with
+// their boxes, so descending costs one dependent memory round trip per level.
+// A malformed tree (child index out of range, or more node entries than the
+// tree has nodes) finishes the ray and sets `bad`.
 template <typename StackT>
 __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT stack, uint32_t cap, Trav& s,
                                          bool& bad) {
@@ -131,19 +141,19 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
     return kStepDone;
   }
   bool ascend = false;
-  const uint32_t node = s.node;
-  const uint32_t right = __ldg(bn + static_cast<size_t>(node) * 3 + 2);
-  if (right == kUMax) {  // a leaf reached as the root or as a far child
-    const uint32_t it = __ldg(bn + static_cast<size_t>(node) * 3 + 1);
+  if (s.right == kUMax) {  // a leaf reached as the root or as a far child
     float t, u, v;
-    if (leaf_hit(m, r, it, t, u, v, bad)) s.best = pick(s.best, Hit{t, it});
+    if (leaf_hit(m, r, s.left, t, u, v, bad)) s.best = pick(s.best, Hit{t, s.left});
     ascend = true;
   } else {
-    const uint32_t left = __ldg(bn + static_cast<size_t>(node) * 3 + 1);
+    const uint32_t left = s.left, right = s.right;
     if (left >= num_node || right >= num_node) {
       bad = true;
       return kStepDone;
     }
+    uint32_t ll, lr, rl, rr;
+    load_record(bn, left, ll, lr);
+    load_record(bn, right, rl, rr);
     float l0 = 0.f, l1 = 0.f, r0 = 0.f, r1 = 0.f;
     const bool hl = node_slab(m, r, left, l0, l1);
     const bool hr = node_slab(m, r, right, r0, r1);
@@ -153,22 +163,32 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
       const bool near_left = (hl && hr) ? tuple_lt(l0, l1, r0, r1) : hl;
       const uint32_t nn = near_left ? left : right;
       const uint32_t nf = near_left ? right : left;
+      const uint32_t n_l = near_left ? ll : rl, n_r = near_left ? lr : rr;
+      const uint32_t f_l = near_left ? rl : ll, f_r = near_left ? rr : lr;
       const bool has_far = hl && hr;
       const float far_enter = near_left ? r0 : l0;
-      if (__ldg(bn + static_cast<size_t>(nn) * 3 + 2) == kUMax) {  // near child is a leaf
-        const uint32_t it = __ldg(bn + static_cast<size_t>(nn) * 3 + 1);
+      if (n_r == kUMax) {  // near child is a leaf holding triangle n_l
         float t, u, v;
-        const bool h = leaf_hit(m, r, it, t, u, v, bad);
-        if (h) s.best = pick(s.best, Hit{t, it});
-        if (!has_far || (h && far_enter > t)) ascend = true;
-        else s.node = nf;
+        const bool h = leaf_hit(m, r, n_l, t, u, v, bad);
+        if (h) s.best = pick(s.best, Hit{t, n_l});
+        if (!has_far || (h && far_enter > t)) {
+          ascend = true;
+        } else {
+          s.node = nf;
+          s.left = f_l;
+          s.right = f_r;
+        }
       } else if (!has_far) {
         s.node = nn;  // R(node) == R(near): no pending decision, no frame
+        s.left = n_l;
+        s.right = n_r;
       } else {
         if (s.sp >= cap) return kStepOverflow;
         stack.store(s.sp++, make_uint4(nf, __float_as_uint(far_enter), __float_as_uint(s.best.t), s.best.id));
         s.best = Hit{INFINITY, kUMax};
         s.node = nn;
+        s.left = n_l;
+        s.right = n_r;
       }
     }
   }
@@ -180,6 +200,11 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
     s.best = pick(saved, s.best);
     if (!skip) {
       s.node = f.x;
+      if (s.node >= num_node) {
+        bad = true;
+        return kStepDone;
+      }
+      load_record(bn, s.node, s.left, s.right);
       return kStepContinue;
     }
   }

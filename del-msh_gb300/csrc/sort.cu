@@ -140,22 +140,39 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
     lb[d] = kFlagInc | cnt;
   } else {
     lb[static_cast<size_t>(tile) * kRadix + d] = kFlagAgg | cnt;
+    // Walk back over the predecessors kWindow at a time (independent loads in
+    // flight together), consuming them in order until an inclusive prefix.
+    constexpr int kWindow = 8;
     int64_t k = static_cast<int64_t>(tile) - 1;
     uint32_t spins = 0;
-    while (k >= 0) {
-      const uint32_t v = lb[static_cast<size_t>(k) * kRadix + d];
-      const uint32_t flag = v & ~kValueMask;
-      if (flag == 0u) {
+    bool done = false;
+    while (!done && k >= 0) {
+      uint32_t v[kWindow];
+#pragma unroll
+      for (int j = 0; j < kWindow; ++j) {
+        const uint32_t pad = kFlagInc;  // below tile 0: never consumed (tile 0 publishes an inclusive prefix)
+        v[j] = (k - j >= 0) ? static_cast<uint32_t>(lb[static_cast<size_t>(k - j) * kRadix + d]) : pad;
+      }
+      bool stalled = false;
+#pragma unroll
+      for (int j = 0; j < kWindow; ++j) {
+        if (done || stalled || k < 0) continue;
+        const uint32_t flag = v[j] & ~kValueMask;
+        if (flag == 0u) {
+          stalled = true;  // predecessor k not published yet: re-read from k
+          continue;
+        }
+        excl += v[j] & kValueMask;
+        if (flag == kFlagInc) done = true;
+        else --k;
+      }
+      if (stalled) {
         if (++spins > kSpinLimit) {
           raise_status(status, kStatusSpinTimeout);
           break;
         }
         __nanosleep(32);
-        continue;
       }
-      excl += v & kValueMask;
-      if (flag == kFlagInc) break;
-      --k;
     }
     lb[static_cast<size_t>(tile) * kRadix + d] = kFlagInc | ((excl + cnt) & kValueMask);
   }
