@@ -370,6 +370,86 @@ def run_ours(args):
     return 0
 
 
+def run_batched(args):
+    """Config 4: 4096 seeded jittered icospheres / tori, triangle counts
+    log-uniform in [64, 65536], each with its own 64x64 orthographic image.
+    One step = build every tree + cast every image.  Timed three ways on the
+    same GPU: the plain path (one launch sequence per mesh through the
+    single-mesh entry points), the batched entry points called eagerly, and
+    the batched step replayed from a CUDA graph."""
+    import torch
+    from del_msh_gb300 import _native
+    from del_msh_gb300 import workloads as W
+    from del_msh_gb300.batch import MeshBatch, PlainPath, ortho_transforms
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    _native.load(build_if_missing=True)
+    t0 = time.perf_counter()
+    meshes = W.ragged_batch(num_mesh=args.num_mesh, tmin=64, tmax=65536, seed=SEED)
+    gen_s = time.perf_counter() - t0
+    b = MeshBatch(meshes, dev)
+    tf = torch.from_numpy(ortho_transforms(meshes)).to(dev)
+    b.alloc_cast(64, 64)
+    plain = PlainPath(b)
+    plain.alloc_cast(64, 64)
+    R = b.num_mesh * 64 * 64
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, steps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for a, z in evs:
+            a.record(stream)
+            fn()
+            z.record(stream)
+        torch.cuda.synchronize()
+        wall = (time.perf_counter() - w0) / steps
+        return statistics.mean(a.elapsed_time(z) for a, z in evs), wall * 1e3
+
+    def plain_step():
+        plain.build()
+        plain.cast_pixels(tf)
+
+    def batch_step():
+        b.build()
+        b.cast_pixels(tf)
+
+    for _ in range(max(1, args.warmup // 2)):
+        plain_step()
+        batch_step()
+    b.capture(tf)
+    b.replay()
+    torch.cuda.synchronize()
+    plain_ms, plain_wall = timed(plain_step, max(2, args.steps // 10))
+    eager_ms, eager_wall = timed(batch_step, args.steps)
+    graph_ms, graph_wall = timed(b.replay, args.steps)
+    match = bool(torch.equal(b.pix2tri.view(torch.int32), plain.pix2tri.view(torch.int32)) and
+                 torch.equal(b.pix2t, plain.pix2t))
+    status = _native.device_status(clear=True)
+    plain_eff = max(plain_ms, plain_wall)
+    line = {
+        "metric": "rays/s (batched LBVH build + cast of ragged meshes)", "unit": UNIT,
+        "value": R / (graph_ms * 1e-3), "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": graph_ms, "higher_is_better": True, "dtype": "f32/u32",
+        "data": "synthetic (seeded jittered icospheres / tori)",
+        "config": {"workload": f"{b.num_mesh} ragged meshes, triangle counts log-uniform in [64, 65536], "
+                               f"64x64 orthographic rays each", "num_mesh": b.num_mesh,
+                   "total_tri": b.total_tri, "rays_per_step": R, "generation_s": gen_s},
+        "plain": {"ms_per_step_device": plain_ms, "ms_per_step_wall": plain_wall,
+                  "rays_per_s": R / (plain_eff * 1e-3), "tris_per_s": b.total_tri / (plain_eff * 1e-3)},
+        "batched_eager": {"ms_per_step": eager_ms, "ms_per_step_wall": eager_wall,
+                          "rays_per_s": R / (max(eager_ms, eager_wall) * 1e-3)},
+        "batched_graph": {"ms_per_step": graph_ms, "ms_per_step_wall": graph_wall,
+                          "rays_per_s": R / (max(graph_ms, graph_wall) * 1e-3),
+                          "tris_per_s": b.total_tri / (graph_ms * 1e-3)},
+        "speedup_vs_plain": plain_eff / max(graph_ms, graph_wall),
+        "outputs_identical_to_plain": match, "device_status": status,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def read_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from the committed ncu summary
     (profiles/ncu_config2.md lines `traffic <kernel> <bytes>`), else None."""
@@ -390,9 +470,13 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--workload", choices=["single", "batched"], default="single")
+    ap.add_argument("--num-mesh", type=int, default=4096, help="meshes of the batched workload")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "batched":
+        return run_batched(args)
     return run_ours(args)
 
 

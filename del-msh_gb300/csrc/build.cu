@@ -6,6 +6,7 @@
 
 #include "dm_device.cuh"
 #include "dm_internal.h"
+#include "dm_lbvh.cuh"
 
 namespace dm {
 namespace {
@@ -237,121 +238,6 @@ __global__ void __launch_bounds__(kThreads) k_vtx2morton(uint32_t n, uint32_t nu
 
 // ----------------------------------------------------------------- topology
 
-// Code / object accessors: the single-mesh arrays, or a segment of the
-// batched sort's (mesh << 30 | code) keys and global triangle indices.
-struct Codes32 {
-  const uint32_t* p;
-  __device__ __forceinline__ uint32_t operator()(uint32_t i) const { return __ldg(p + i); }
-};
-struct Objs32 {
-  const uint32_t* p;
-  __device__ __forceinline__ uint32_t operator()(uint32_t i) const { return __ldg(p + i); }
-};
-
-// Last index of the run of value v that contains position `from` (sorted c).
-// Equal to the linear scan of mortons.rs:235-245, found by galloping search.
-template <typename Codes>
-__device__ __forceinline__ uint32_t run_end(const Codes& c, uint32_t n, uint32_t from, uint32_t v) {
-  uint32_t lo = from;  // c[lo] == v
-  uint32_t step = 1;
-  uint32_t hi = n;     // first index known to differ (or n)
-  for (;;) {
-    const uint64_t probe = static_cast<uint64_t>(lo) + step;
-    if (probe >= n) break;
-    if (c(static_cast<uint32_t>(probe)) != v) {
-      hi = static_cast<uint32_t>(probe);
-      break;
-    }
-    lo = static_cast<uint32_t>(probe);
-    step <<= 1;
-  }
-  while (hi - lo > 1) {  // invariant: c[lo] == v, hi == n or c[hi] != v
-    const uint32_t mid = lo + (hi - lo) / 2;
-    if (c(mid) == v) lo = mid;
-    else hi = mid;
-  }
-  return lo;
-}
-
-// One branch ib of the radix tree over n sorted codes: mortons.rs:221-288
-// (range), 290-325 (split) and bvhnodes_morton.rs:24-47 (writes).  The
-// branch index is always one end of its range; the other end is written to
-// other_end[ib] when other_end != nullptr (used by the windowed refit).
-template <typename Codes, typename Objs>
-__device__ __forceinline__ void topology_node(uint32_t n, const Codes& c, const Objs& obj, uint32_t* bvhnodes,
-                                              uint32_t ib, uint32_t* other_end) {
-  uint32_t r0, r1;
-  if (ib == 0) {
-    r0 = 0;
-    r1 = n - 1;
-  } else {
-    const uint32_t mc0 = c(ib - 1), mc1 = c(ib), mc2 = c(ib + 1);
-    if (mc0 == mc1 && mc1 == mc2) {
-      r0 = ib;
-      r1 = run_end(c, n, ib + 1, mc1);
-    } else {
-      const int dd = __clz(mc1 ^ mc2) - __clz(mc1 ^ mc0);
-      const int d = dd > 0 ? 1 : -1;
-      const int delta_min = __clz(mc1 ^ (d > 0 ? mc0 : mc2));
-      int64_t lmax = 2;
-      for (;;) {
-        const int64_t j = static_cast<int64_t>(ib) + lmax * d;
-        if (j < 0 || j >= static_cast<int64_t>(n)) break;
-        if (__clz(mc1 ^ c(static_cast<uint32_t>(j))) <= delta_min) break;
-        lmax *= 2;
-      }
-      int64_t l = 0;
-      for (int64_t t = lmax / 2; t >= 1; t /= 2) {
-        const int64_t j = static_cast<int64_t>(ib) + (l + t) * d;
-        if (j >= 0 && j < static_cast<int64_t>(n) && __clz(mc1 ^ c(static_cast<uint32_t>(j))) > delta_min) l += t;
-      }
-      const uint32_t j = static_cast<uint32_t>(static_cast<int64_t>(ib) + l * d);
-      r0 = ib <= j ? ib : j;
-      r1 = ib <= j ? j : ib;
-    }
-  }
-  uint32_t isplit = r0;
-  {
-    const uint32_t mc_start = c(r0);
-    const int common = __clz(mc_start ^ c(r1));
-    if (common != 32) {
-      uint32_t step = r1 - r0;
-      while (step > 1) {
-        step = (step + 1) / 2;
-        const uint32_t cand = isplit + step;
-        if (cand >= r1) continue;
-        if (__clz(mc_start ^ c(cand)) > common) isplit = cand;
-      }
-    }
-  }
-  if (other_end) other_end[ib] = (r0 == ib) ? r1 : r0;
-  const uint32_t nb = n - 1;
-  uint32_t* me = bvhnodes + static_cast<size_t>(ib) * 3;
-  if (r0 == isplit) {
-    const uint32_t a = nb + isplit;
-    me[1] = a;
-    uint32_t* la = bvhnodes + static_cast<size_t>(a) * 3;
-    la[0] = ib;
-    la[1] = obj(isplit);
-    la[2] = kUMax;
-  } else {
-    me[1] = isplit;
-    bvhnodes[static_cast<size_t>(isplit) * 3] = ib;
-  }
-  if (r1 == isplit + 1) {
-    const uint32_t b = nb + isplit + 1;
-    me[2] = b;
-    uint32_t* lb = bvhnodes + static_cast<size_t>(b) * 3;
-    lb[0] = ib;
-    lb[1] = obj(isplit + 1);
-    lb[2] = kUMax;
-  } else {
-    me[2] = isplit + 1;
-    bvhnodes[static_cast<size_t>(isplit + 1) * 3] = ib;
-  }
-  if (ib == 0) me[0] = kUMax;
-}
-
 __global__ void __launch_bounds__(kThreads) k_topology(uint32_t n, const uint32_t* __restrict__ c,
                                                       const uint32_t* __restrict__ idx2obj, uint32_t* bvhnodes,
                                                       uint32_t* other_end) {
@@ -446,11 +332,15 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
 // block-scope ordering; only branches whose range crosses a window edge (about
 // 2 per window per tree level above the window) use the global acquire-release
 // arrival of k_refit.  Values and merge order are those of k_refit.
-constexpr int kWinLeaves = 1024;
+constexpr int kWinLeaves = 512;
 constexpr int kWinThreads = 256;
 
+// Every branch whose range lies in the window has its index in the window,
+// so the records and other ends of branches wA..wA+kWinLeaves-1 are loaded
+// into shared memory once (coalesced) and the in-window climb reads no L2.
 struct WinSmem {
   uint32_t flag[kWinLeaves];
+  uint32_t rec[kWinLeaves][4];  // parent, left, right, other end
   Box leaf[kWinLeaves];
   Box node[kWinLeaves];
 };
@@ -477,7 +367,26 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, S
   extern __shared__ __align__(16) unsigned char win_raw[];
   WinSmem& S = *reinterpret_cast<WinSmem*>(win_raw);
   const uint32_t wA = blockIdx.x * kWinLeaves;
-  for (int k = threadIdx.x; k < kWinLeaves; k += kWinThreads) S.flag[k] = 0u;
+  for (int k = threadIdx.x; k < kWinLeaves; k += kWinThreads) {
+    S.flag[k] = 0u;
+    const uint32_t g = wA + k;  // position in the global leaf order
+    if (g >= total_tri) continue;
+    uint32_t m = 0, t0 = 0, T = total_tri;
+    if (kBatch) {
+      m = mesh_of_leaf(seg, g);
+      t0 = __ldg(seg.tri_off + m);
+      T = __ldg(seg.tri_off + m + 1) - t0;
+    }
+    if (g < t0 || T > 0x7FFFFFFFu) continue;  // only with invalid offsets
+    const uint32_t n = g - t0;  // branch n of mesh m, if it exists
+    if (n + 1 >= T) continue;
+    const size_t node_off = 2ull * t0 - m, int_off = static_cast<size_t>(t0) - m;
+    const uint32_t* r = bvhnodes_all + 3 * (node_off + n);
+    S.rec[k][0] = __ldg(r);
+    S.rec[k][1] = __ldg(r + 1);
+    S.rec[k][2] = __ldg(r + 2);
+    S.rec[k][3] = __ldg(other_all + int_off + n);
+  }
   __syncthreads();
   for (uint32_t k = threadIdx.x; k < static_cast<uint32_t>(kWinLeaves); k += kWinThreads) {
     const uint32_t i = wA + k;
@@ -489,6 +398,10 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, S
       T = __ldg(seg.tri_off + m + 1) - t0;
       v0 = __ldg(seg.vtx_off + m);
       V = __ldg(seg.vtx_off + m + 1) - v0;
+    }
+    if (i < t0 || i - t0 >= T || T > 0x7FFFFFFFu) {  // only with invalid offsets
+      raise_status(status, kStatusBadIndex);
+      continue;
     }
     const size_t node_off = 2ull * t0 - m, int_off = static_cast<size_t>(t0) - m;
     const uint32_t* bn = bvhnodes_all + 3 * node_off;
@@ -516,10 +429,20 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, S
         raise_status(status, kStatusBadIndex);
         break;
       }
-      const uint32_t parent = __ldg(bn + static_cast<size_t>(node) * 3);
-      const uint32_t c0 = __ldg(bn + static_cast<size_t>(node) * 3 + 1);
-      const uint32_t c1 = __ldg(bn + static_cast<size_t>(node) * 3 + 2);
-      const uint32_t other = __ldg(oe + node);
+      uint32_t parent, c0, c1, other;
+      const bool in_win = (t0 + node >= wA) && (t0 + node < wA + kWinLeaves);
+      if (in_win) {
+        const uint32_t* r = S.rec[t0 + node - wA];
+        parent = r[0];
+        c0 = r[1];
+        c1 = r[2];
+        other = r[3];
+      } else {
+        parent = __ldg(bn + static_cast<size_t>(node) * 3);
+        c0 = __ldg(bn + static_cast<size_t>(node) * 3 + 1);
+        c1 = __ldg(bn + static_cast<size_t>(node) * 3 + 2);
+        other = __ldg(oe + node);
+      }
       const uint32_t lo = node < other ? node : other, hi = node < other ? other : node;
       const bool local = (t0 + lo >= wA) && (t0 + hi < wA + kWinLeaves);
       uint32_t old;
@@ -600,12 +523,20 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   if (total_tri == 0) return;
   const int smem = static_cast<int>(sizeof(WinSmem));
   const uint32_t grid = (total_tri + kWinLeaves - 1) / kWinLeaves;
-  if (seg.tri_off) {
+  // the attribute is per device; set it once so that later calls (possibly
+  // under stream capture) make no further runtime configuration calls
+  static bool configured[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !configured[dev]) {
     cudaFuncSetAttribute(k_refit_win<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_refit_win<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    configured[dev] = true;
+  }
+  if (seg.tri_off) {
     k_refit_win<true><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
                                                       vtx2xyz0, vtx2xyz1, aabb, flags, height_out, status);
   } else {
-    cudaFuncSetAttribute(k_refit_win<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     k_refit_win<false><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
                                                        vtx2xyz0, vtx2xyz1, aabb, flags, height_out, status);
   }

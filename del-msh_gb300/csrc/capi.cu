@@ -5,6 +5,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <utility>
 
 #include "../../include/delmsh_gb300.h"
 #include "dm_device.cuh"
@@ -209,6 +210,42 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   return DM_OK;
 }
 
+
+// ------------------------------------------------------------ batch layout
+struct BatchLayout {
+  int num_pass;
+  size_t hist, counters, lookback, zero_bytes, transforms, keys_a, vals_a, keys_b, vals_b, other, flags, total;
+};
+
+BatchLayout batch_layout(uint32_t num_mesh, uint32_t total_tri) {
+  BatchLayout L{};
+  L.num_pass = dm::batch_num_pass(num_mesh);
+  L.hist = 0;
+  L.counters = 8 * 256 * 4;
+  L.lookback = align256(L.counters + 16 * 4);
+  L.zero_bytes = L.lookback + align256(dm::sort_lookback_words(total_tri, L.num_pass) * 4);
+  L.transforms = L.zero_bytes;
+  L.keys_a = L.transforms + align256(size_t{64} * num_mesh);
+  L.vals_a = L.keys_a + align256(size_t{8} * total_tri);
+  L.keys_b = L.vals_a + align256(size_t{4} * total_tri);
+  L.vals_b = L.keys_b + align256(size_t{8} * total_tri);
+  L.other = L.vals_b + align256(size_t{4} * total_tri);
+  L.flags = L.other + align256(size_t{4} * total_tri);
+  L.total = L.flags + align256(size_t{4} * total_tri);
+  return L;
+}
+
+int check_batch(uint32_t num_mesh, const uint32_t* mesh2tri, const uint32_t* mesh2vtx, uint32_t total_tri,
+                uint32_t total_vtx, const uint32_t* tri2vtx, const float* vtx2xyz) {
+  DM_REQUIRE(num_mesh >= 1, "num_mesh must be >= 1");
+  DM_REQUIRE(total_tri >= num_mesh, "every mesh needs at least one triangle (total_tri %u < num_mesh %u)", total_tri,
+             num_mesh);
+  DM_REQUIRE(total_tri <= kMaxElems, "total_tri %u exceeds the supported maximum %u", total_tri, kMaxElems);
+  DM_REQUIRE(num_mesh <= (1u << 22), "num_mesh %u exceeds the supported maximum 4194304", num_mesh);
+  DM_REQUIRE(total_vtx >= 1 && mesh2tri && mesh2vtx && tri2vtx && vtx2xyz, "NULL argument or empty vertex array");
+  return DM_OK;
+}
+
 }  // namespace
 
 namespace dm {
@@ -388,6 +425,82 @@ int dm_search_bvh3_first_intersection_ray(uint64_t stream_ptr, uint32_t num_ray,
   dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb};
   dm::CastOut o{hit_tri, hit_t, hit_bc};
   dm::launch_cast_rays(s, num_ray, ray_org, ray_dir, m, o, cs, status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+size_t dm_batch_build_scratch_bytes(uint32_t num_mesh, uint32_t total_tri) {
+  return batch_layout(num_mesh, total_tri).total;
+}
+
+int dm_batch_trimesh3_build(uint64_t stream_ptr, uint32_t num_mesh, const uint32_t* mesh2tri,
+                            const uint32_t* mesh2vtx, uint32_t total_tri, uint32_t total_vtx,
+                            const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t* bvhnodes, float* bvhnode2aabb,
+                            uint32_t* heights, void* scratch, size_t scratch_bytes) {
+  if (int e = check_batch(num_mesh, mesh2tri, mesh2vtx, total_tri, total_vtx, tri2vtx, vtx2xyz)) return e;
+  DM_REQUIRE(bvhnodes && bvhnode2aabb, "NULL argument");
+  cudaStream_t s = as_stream(stream_ptr);
+  const BatchLayout L = batch_layout(num_mesh, total_tri);
+  Scratch sc;
+  if (int e = sc.acquire(scratch, scratch_bytes, L.total, s, nullptr)) return e;
+  void* base = sc.ptr;
+  uint32_t* status = status_ptr();
+  DM_CUDA(cudaMemsetAsync(base, 0, L.zero_bytes, s));
+  DM_CUDA(cudaMemsetAsync(at<char>(base, L.flags), 0, size_t{4} * total_tri, s));
+  const dm::Segments seg{num_mesh, mesh2tri, mesh2vtx};
+  float* transforms = at<float>(base, L.transforms);
+  uint32_t* hist = at<uint32_t>(base, L.hist);
+  uint32_t* counters = at<uint32_t>(base, L.counters);
+  uint32_t* lookback = at<uint32_t>(base, L.lookback);
+  uint64_t* ka = at<uint64_t>(base, L.keys_a);
+  uint64_t* kb = at<uint64_t>(base, L.keys_b);
+  uint32_t* va = at<uint32_t>(base, L.vals_a);
+  uint32_t* vb = at<uint32_t>(base, L.vals_b);
+  dm::launch_batch_fit(s, seg, tri2vtx, vtx2xyz, transforms, status);
+  dm::launch_batch_morton(s, total_tri, seg, tri2vtx, vtx2xyz, transforms, ka, hist, L.num_pass, status);
+  const size_t lbw = dm::sort_lookback_words(total_tri, 1);
+  uint64_t *ks = ka, *kd = kb;
+  uint32_t *vs = nullptr, *vd = vb;
+  for (int p = 0; p < L.num_pass; ++p) {
+    dm::launch_onesweep_u64(s, total_tri, 8u * p, ks, vs, kd, vd, hist + 256 * p, lookback + lbw * p, counters + p,
+                            status);
+    std::swap(ks, kd);
+    vs = vd;
+    vd = (vd == vb) ? va : vb;
+  }
+  dm::launch_batch_topology(s, total_tri, seg, ks, vs, bvhnodes, at<uint32_t>(base, L.other));
+  dm::launch_refit_windowed(s, total_tri, seg, 0, bvhnodes, at<uint32_t>(base, L.other), tri2vtx, vtx2xyz, nullptr,
+                            bvhnode2aabb, at<uint32_t>(base, L.flags), heights, status);
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+size_t dm_batch_cast_scratch_bytes(uint32_t num_ray, uint32_t max_tri_per_mesh) {
+  return dm::cast_scratch_bytes(num_ray, max_tri_per_mesh);
+}
+
+int dm_batch_pix2tri_by_raycast(uint64_t stream_ptr, uint32_t num_mesh, const uint32_t* mesh2tri,
+                                const uint32_t* mesh2vtx, uint32_t total_tri, uint32_t total_vtx,
+                                uint32_t max_tri_per_mesh, const uint32_t* tri2vtx, const float* vtx2xyz,
+                                const uint32_t* bvhnodes, const float* bvhnode2aabb, uint32_t img_w, uint32_t img_h,
+                                const float* transforms_ndc2world, uint32_t* pix2tri, float* pix2t, void* scratch,
+                                size_t scratch_bytes) {
+  if (int e = check_batch(num_mesh, mesh2tri, mesh2vtx, total_tri, total_vtx, tri2vtx, vtx2xyz)) return e;
+  DM_REQUIRE(bvhnodes && bvhnode2aabb && transforms_ndc2world && pix2tri, "NULL argument");
+  DM_REQUIRE(max_tri_per_mesh >= 1 && max_tri_per_mesh <= total_tri, "max_tri_per_mesh must be in 1..total_tri");
+  const uint64_t num_ray = static_cast<uint64_t>(img_w) * img_h * num_mesh;
+  DM_REQUIRE(num_ray <= kMaxElems, "%llu rays exceed the supported maximum", (unsigned long long)num_ray);
+  if (num_ray == 0) return DM_OK;
+  cudaStream_t s = as_stream(stream_ptr);
+  Scratch sc;
+  const uint32_t n = static_cast<uint32_t>(num_ray);
+  if (int e = sc.acquire(scratch, scratch_bytes, dm::cast_scratch_bytes(n, max_tri_per_mesh), s, nullptr)) return e;
+  dm::CastScratch cs;
+  dm::cast_scratch_carve(sc.ptr, n, max_tri_per_mesh, &cs);
+  DM_CUDA(cudaMemsetAsync(cs.counters, 0, 16, s));
+  dm::CastOut o{pix2tri, pix2t, nullptr};
+  dm::launch_batch_cast_pixels(s, dm::Segments{num_mesh, mesh2tri, mesh2vtx}, max_tri_per_mesh, tri2vtx, vtx2xyz,
+                               bvhnodes, bvhnode2aabb, img_w, img_h, transforms_ndc2world, o, cs, status_ptr());
   DM_CUDA(cudaGetLastError());
   return DM_OK;
 }

@@ -89,6 +89,17 @@ void launch_onesweep_u64(cudaStream_t s, uint32_t n, uint32_t shift, const uint6
                          const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
                          uint32_t* lookback, uint32_t* tile_counter, uint32_t* status);
 
+// ---------------------------------------------------------------- batch.cu
+// Number of 8-bit passes sorting (mesh << 30 | code) keys of num_mesh meshes.
+int batch_num_pass(uint32_t num_mesh);
+void launch_batch_fit(cudaStream_t s, const Segments& seg, const uint32_t* tri2vtx, const float* vtx2xyz,
+                      float* transforms, uint32_t* status);
+void launch_batch_morton(cudaStream_t s, uint32_t total_tri, const Segments& seg, const uint32_t* tri2vtx,
+                         const float* vtx2xyz, const float* transforms, uint64_t* keys, uint32_t* hist, int num_pass,
+                         uint32_t* status);
+void launch_batch_topology(cudaStream_t s, uint32_t total_tri, const Segments& seg, const uint64_t* keys,
+                           const uint32_t* vals, uint32_t* bvhnodes, uint32_t* other_end);
+
 // ----------------------------------------------------------------- cast.cu
 constexpr int kCastStack = 64;  // frames of the on-chip (local) traversal stack
 constexpr size_t kFrameBytes = 16;
@@ -124,5 +135,12 @@ void launch_cast_pixels(cudaStream_t s, uint32_t img_w, uint32_t img_h, const fl
                         const CastOut& o, const CastScratch& sc, uint32_t* status);
 void launch_cast_rays(cudaStream_t s, uint32_t num_ray, const float* ray_org, const float* ray_dir,
                       const MeshView& m, const CastOut& o, const CastScratch& sc, uint32_t* status);
+
+// img_w x img_h pixels per mesh of a batch, per-mesh ndc->world transforms
+// (16 floats each); output slot of pixel p of mesh m is m*img_w*img_h + p.
+void launch_batch_cast_pixels(cudaStream_t s, const Segments& seg, uint32_t max_tri, const uint32_t* tri2vtx,
+                              const float* vtx2xyz, const uint32_t* bvhnodes, const float* aabb, uint32_t img_w,
+                              uint32_t img_h, const float* transforms, const CastOut& o, const CastScratch& sc,
+                              uint32_t* status);
 
 }  // namespace dm

@@ -1,0 +1,123 @@
+// dm_lbvh.cuh — the per-branch Karras radix-tree construction shared by the
+// single-mesh build (build.cu) and the batched build (batch.cu).
+#pragma once
+#include "dm_device.cuh"
+
+namespace dm {
+
+// Code / object accessors: the single-mesh arrays, or a segment of the
+// batched sort's (mesh << 30 | code) keys and global triangle indices.
+struct Codes32 {
+  const uint32_t* p;
+  __device__ __forceinline__ uint32_t operator()(uint32_t i) const { return __ldg(p + i); }
+};
+struct Objs32 {
+  const uint32_t* p;
+  __device__ __forceinline__ uint32_t operator()(uint32_t i) const { return __ldg(p + i); }
+};
+
+// Last index of the run of value v that contains position `from` (sorted c).
+// Equal to the linear scan of mortons.rs:235-245, found by galloping search.
+template <typename Codes>
+__device__ __forceinline__ uint32_t run_end(const Codes& c, uint32_t n, uint32_t from, uint32_t v) {
+  uint32_t lo = from;  // c[lo] == v
+  uint32_t step = 1;
+  uint32_t hi = n;     // first index known to differ (or n)
+  for (;;) {
+    const uint64_t probe = static_cast<uint64_t>(lo) + step;
+    if (probe >= n) break;
+    if (c(static_cast<uint32_t>(probe)) != v) {
+      hi = static_cast<uint32_t>(probe);
+      break;
+    }
+    lo = static_cast<uint32_t>(probe);
+    step <<= 1;
+  }
+  while (hi - lo > 1) {  // invariant: c[lo] == v, hi == n or c[hi] != v
+    const uint32_t mid = lo + (hi - lo) / 2;
+    if (c(mid) == v) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// One branch ib of the radix tree over n sorted codes: mortons.rs:221-288
+// (range), 290-325 (split) and bvhnodes_morton.rs:24-47 (writes).  The
+// branch index is always one end of its range; the other end is written to
+// other_end[ib] when other_end != nullptr (used by the windowed refit).
+template <typename Codes, typename Objs>
+__device__ __forceinline__ void topology_node(uint32_t n, const Codes& c, const Objs& obj, uint32_t* bvhnodes,
+                                              uint32_t ib, uint32_t* other_end) {
+  uint32_t r0, r1;
+  if (ib == 0) {
+    r0 = 0;
+    r1 = n - 1;
+  } else {
+    const uint32_t mc0 = c(ib - 1), mc1 = c(ib), mc2 = c(ib + 1);
+    if (mc0 == mc1 && mc1 == mc2) {
+      r0 = ib;
+      r1 = run_end(c, n, ib + 1, mc1);
+    } else {
+      const int dd = __clz(mc1 ^ mc2) - __clz(mc1 ^ mc0);
+      const int d = dd > 0 ? 1 : -1;
+      const int delta_min = __clz(mc1 ^ (d > 0 ? mc0 : mc2));
+      int64_t lmax = 2;
+      for (;;) {
+        const int64_t j = static_cast<int64_t>(ib) + lmax * d;
+        if (j < 0 || j >= static_cast<int64_t>(n)) break;
+        if (__clz(mc1 ^ c(static_cast<uint32_t>(j))) <= delta_min) break;
+        lmax *= 2;
+      }
+      int64_t l = 0;
+      for (int64_t t = lmax / 2; t >= 1; t /= 2) {
+        const int64_t j = static_cast<int64_t>(ib) + (l + t) * d;
+        if (j >= 0 && j < static_cast<int64_t>(n) && __clz(mc1 ^ c(static_cast<uint32_t>(j))) > delta_min) l += t;
+      }
+      const uint32_t j = static_cast<uint32_t>(static_cast<int64_t>(ib) + l * d);
+      r0 = ib <= j ? ib : j;
+      r1 = ib <= j ? j : ib;
+    }
+  }
+  uint32_t isplit = r0;
+  {
+    const uint32_t mc_start = c(r0);
+    const int common = __clz(mc_start ^ c(r1));
+    if (common != 32) {
+      uint32_t step = r1 - r0;
+      while (step > 1) {
+        step = (step + 1) / 2;
+        const uint32_t cand = isplit + step;
+        if (cand >= r1) continue;
+        if (__clz(mc_start ^ c(cand)) > common) isplit = cand;
+      }
+    }
+  }
+  if (other_end) other_end[ib] = (r0 == ib) ? r1 : r0;
+  const uint32_t nb = n - 1;
+  uint32_t* me = bvhnodes + static_cast<size_t>(ib) * 3;
+  if (r0 == isplit) {
+    const uint32_t a = nb + isplit;
+    me[1] = a;
+    uint32_t* la = bvhnodes + static_cast<size_t>(a) * 3;
+    la[0] = ib;
+    la[1] = obj(isplit);
+    la[2] = kUMax;
+  } else {
+    me[1] = isplit;
+    bvhnodes[static_cast<size_t>(isplit) * 3] = ib;
+  }
+  if (r1 == isplit + 1) {
+    const uint32_t b = nb + isplit + 1;
+    me[2] = b;
+    uint32_t* lb = bvhnodes + static_cast<size_t>(b) * 3;
+    lb[0] = ib;
+    lb[1] = obj(isplit + 1);
+    lb[2] = kUMax;
+  } else {
+    me[2] = isplit + 1;
+    bvhnodes[static_cast<size_t>(isplit + 1) * 3] = ib;
+  }
+  if (ib == 0) me[0] = kUMax;
+}
+
+}  // namespace dm

@@ -228,11 +228,13 @@ void onesweep(cudaStream_t s, uint32_t n, uint32_t shift, const KeyT* keys_in, c
               uint32_t* status) {
   if (n == 0) return;
   const size_t smem = sizeof(SortSmem<KeyT>);
-  static bool configured[2] = {false, false};  // per instantiation pair; attribute is per function
-  if (!configured[0]) {
+  static bool configured[64] = {false};  // the attribute is per device and function
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !configured[dev]) {
     cudaFuncSetAttribute(k_onesweep<KeyT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
     cudaFuncSetAttribute(k_onesweep<KeyT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    configured[0] = true;
+    configured[dev] = true;
   }
   const uint32_t grid = sort_num_tiles(n);
   if (vals_in == nullptr)

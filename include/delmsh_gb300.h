@@ -169,6 +169,39 @@ int dm_search_bvh3_first_intersection_ray(uint64_t stream_ptr, uint32_t num_ray,
 /* Scratch size of dm_pix2tri_by_raycast / dm_search_bvh3_first_intersection_ray. */
 size_t dm_cast_scratch_bytes(uint32_t num_ray, uint32_t num_tri);
 
+/* ---- batches: many independent meshes of uneven sizes in one call ----
+ * The meshes are stored back to back.  mesh2tri / mesh2vtx are device
+ * u32[num_mesh+1] prefix offsets (mesh m owns triangles mesh2tri[m] ..
+ * mesh2tri[m+1]-1 and vertices mesh2vtx[m] .. mesh2vtx[m+1]-1; every mesh has
+ * at least one triangle), and tri2vtx holds vertex indices local to each
+ * mesh.  Mesh m's tree occupies nodes 2*mesh2tri[m]-m .. 2*mesh2tri[m+1]-m-2
+ * of bvhnodes / bvhnode2aabb, with node and triangle indices local to the
+ * mesh: each slice is bit for bit what dm_trimesh3_make_bvhnodes_bvhnode2aabb
+ * returns for that mesh alone.  All launches are stream-ordered with no host
+ * synchronization, so a sequence of batch calls given caller scratch can be
+ * captured in a CUDA graph.  No reference counterpart: the reference builds
+ * and casts one mesh per call (TriMesh3/torch.py:233-285, Pix2Tri/torch.py:8-61). */
+
+/* Builds every mesh's LBVH.  heights (optional, device u32[num_mesh]) gets
+ * each tree's height. */
+int dm_batch_trimesh3_build(uint64_t stream_ptr, uint32_t num_mesh, const uint32_t* mesh2tri,
+                            const uint32_t* mesh2vtx, uint32_t total_tri, uint32_t total_vtx,
+                            const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t* bvhnodes, float* bvhnode2aabb,
+                            uint32_t* heights, void* scratch, size_t scratch_bytes);
+size_t dm_batch_build_scratch_bytes(uint32_t num_mesh, uint32_t total_tri);
+
+/* Casts an img_w x img_h image per mesh through that mesh's column-major
+ * transforms_ndc2world[16*m .. 16*m+15]; pix2tri / pix2t (optional) hold
+ * num_mesh images of img_h x img_w, pixel p of mesh m at m*img_w*img_h + p.
+ * max_tri_per_mesh bounds the largest mesh (it sizes the deep-stack pool). */
+int dm_batch_pix2tri_by_raycast(uint64_t stream_ptr, uint32_t num_mesh, const uint32_t* mesh2tri,
+                                const uint32_t* mesh2vtx, uint32_t total_tri, uint32_t total_vtx,
+                                uint32_t max_tri_per_mesh, const uint32_t* tri2vtx, const float* vtx2xyz,
+                                const uint32_t* bvhnodes, const float* bvhnode2aabb, uint32_t img_w, uint32_t img_h,
+                                const float* transforms_ndc2world, uint32_t* pix2tri, float* pix2t, void* scratch,
+                                size_t scratch_bytes);
+size_t dm_batch_cast_scratch_bytes(uint32_t num_ray, uint32_t max_tri_per_mesh);
+
 #ifdef __cplusplus
 }
 #endif
