@@ -450,6 +450,65 @@ def run_batched(args):
     return 0
 
 
+def run_served(args):
+    """Served configuration: a pool of 512 seeded icospheres / tori (triangle
+    counts log-uniform in [1k, 1M]), Poisson arrivals, 20% build + 512x512
+    cast, 60% refit + re-cast after a per-frame deformation of the resident
+    tree, 20% cast of 16k random rays; 120 GB HBM budget with LRU eviction.
+    The request server and the plain serial path run the same traces at the
+    same offered loads on the same GPU; latency counts from the scheduled
+    arrival to the completion of the result download."""
+    import torch
+    from del_msh_gb300 import _native
+    from del_msh_gb300.serve import Server, ServedWorkload, latency_stats
+    torch.cuda.set_device(0)
+    _native.load(build_if_missing=True)
+    t0 = time.perf_counter()
+    wl = ServedWorkload(num_mesh=args.pool, tmin=1000, tmax=1_000_000, img=512, num_ray=16384, seed=SEED)
+    gen_s = time.perf_counter() - t0
+    n = args.requests
+    out = {"metric": "served requests: p50/p99 latency and rays/s against the plain serial path", "unit": "ms",
+           "config": {"pool": args.pool, "total_tri": int(sum(t.shape[0] for t, _ in wl.meshes)),
+                      "max_tri": wl.max_tri, "mix": "20% build+cast 512^2, 60% refit+re-cast, 20% cast 16k rays",
+                      "budget_gb": args.budget_gb, "slots": args.slots, "requests_per_trace": n,
+                      "generation_s": gen_s}, "data": "synthetic (seeded jittered icospheres / tori)",
+           "loads": []}
+    with Server(budget_bytes=int(args.budget_gb * (1 << 30)), num_slots=args.slots, max_tri=wl.max_tri,
+                max_out=wl.max_out) as srv:
+        wl.register_all(srv)
+        # capacities: a closed burst (all arrivals at t=0) through each path
+        reqs, _ = wl.stream(min(n, 300), 1.0)
+        plain_burst = latency_stats(srv.run_plain(reqs, [0.0] * len(reqs)))
+        plain_cap = len(reqs) / plain_burst["span_s"]
+        reqs, _ = wl.stream(len(wl.meshes), 1.0)  # touch the pool so trees are resident
+        srv.run_trace(reqs, [0.0] * len(reqs))
+        reqs, _ = wl.stream(n, 1.0)
+        served_burst = latency_stats(srv.run_trace(reqs, [0.0] * n))
+        served_cap = n / served_burst["span_s"]
+        out["plain_capacity_rps"] = plain_cap
+        out["served_capacity_rps"] = served_cap
+        for frac in args.loads:
+            rate = frac * plain_cap
+            reqs, arr = wl.stream(n, rate)
+            rays = sum(r.num_ray if r.kind == 2 else r.img_w * r.img_h for r in reqs)
+            s = latency_stats(srv.run_trace(reqs, arr))
+            entry = {"offered_rps": rate, "fraction_of_plain_capacity": frac, "served": s,
+                     "served_rays_per_s": rays / s["span_s"]}
+            if frac <= 0.9:
+                reqs_p, arr_p = wl.stream(min(n, 600), rate)
+                rays_p = sum(r.num_ray if r.kind == 2 else r.img_w * r.img_h for r in reqs_p)
+                p = latency_stats(srv.run_plain(reqs_p, arr_p))
+                entry["plain"] = p
+                entry["plain_rays_per_s"] = rays_p / p["span_s"]
+                entry["served_p99_below_plain_p50"] = s["p99_ms"] < p["p50_ms"]
+            out["loads"].append(entry)
+        out["server_stats"] = srv.stats()
+    from del_msh_gb300 import _native as N
+    out["device_status"] = N.device_status(clear=True)
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def read_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from the committed ncu summary
     (profiles/ncu_config2.md lines `traffic <kernel> <bytes>`), else None."""
@@ -470,13 +529,21 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--workload", choices=["single", "batched"], default="single")
+    ap.add_argument("--workload", choices=["single", "batched", "served"], default="single")
     ap.add_argument("--num-mesh", type=int, default=4096, help="meshes of the batched workload")
+    ap.add_argument("--pool", type=int, default=512, help="meshes of the served pool")
+    ap.add_argument("--requests", type=int, default=1000, help="requests per served trace")
+    ap.add_argument("--slots", type=int, default=8, help="concurrent request slots of the server")
+    ap.add_argument("--budget-gb", type=float, default=120.0, help="HBM budget of the server")
+    ap.add_argument("--loads", type=float, nargs="*", default=[0.5, 0.8, 2.0, 4.0],
+                    help="offered loads as fractions of the plain path's capacity")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "served":
+        return run_served(args)
     return run_ours(args)
 
 

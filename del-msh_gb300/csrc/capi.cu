@@ -163,7 +163,7 @@ void sort4(cudaStream_t s, uint32_t n, const uint32_t* k0, uint32_t* ak, uint32_
 int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz,
                uint32_t* bvhnodes, float* aabb, float* transform_out, uint32_t* tri2morton_out, uint32_t* idx2tri_out,
                uint32_t* idx2morton_out, uint32_t* height_out, void* scratch, size_t scratch_bytes,
-               cudaEvent_t* ev = nullptr) {
+               cudaEvent_t* ev = nullptr, uint32_t* other_end_out = nullptr) {
   if (int e = check_mesh(T, tri2vtx, num_vtx, vtx2xyz)) return e;
   DM_REQUIRE(bvhnodes && aabb, "bvhnodes / bvhnode2aabb must not be NULL");
   cudaStream_t s = as_stream(stream_ptr);
@@ -198,7 +198,7 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   if (ev) DM_CUDA(cudaEventRecord(ev[1], s));
   sort4(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
   if (ev) DM_CUDA(cudaEventRecord(ev[2], s));
-  uint32_t* other_end = ak;  // the sort's A buffers are dead after pass 3
+  uint32_t* other_end = other_end_out ? other_end_out : ak;  // the sort's A buffers are dead after pass 3
   dm::launch_topology(s, T, ok, ov, bvhnodes, other_end);
   if (ev) DM_CUDA(cudaEventRecord(ev[3], s));
   dm::launch_refit_windowed(s, T, dm::Segments{1, nullptr, nullptr}, num_vtx, bvhnodes, other_end, tri2vtx, vtx2xyz,
@@ -261,6 +261,14 @@ int set_error(int code, const char* fmt, ...) {
 }
 
 uint32_t* device_status_word() { return status_ptr(); }
+
+int build_keep_ranges(cudaStream_t s, uint32_t T, const uint32_t* tri2vtx, uint32_t V, const float* vtx2xyz,
+                      uint32_t* bvhnodes, float* aabb, uint32_t* other_end_out, void* scratch, size_t scratch_bytes) {
+  return build_impl(reinterpret_cast<uint64_t>(s), T, tri2vtx, V, vtx2xyz, bvhnodes, aabb, nullptr, nullptr, nullptr,
+                    nullptr, nullptr, scratch, scratch_bytes, nullptr, other_end_out);
+}
+
+size_t build_scratch_bytes(uint32_t T) { return build_layout(T).total; }
 
 }  // namespace dm
 

@@ -12,6 +12,11 @@ namespace dm {
 int set_error(int code, const char* fmt, ...);
 // Device address of the library's status word on the current device (or nullptr).
 uint32_t* device_status_word();
+// The single-mesh build with each branch's range end kept in other_end_out
+// (u32[T-1]), so later refits of the tree can use launch_refit_windowed.
+int build_keep_ranges(cudaStream_t s, uint32_t T, const uint32_t* tri2vtx, uint32_t V, const float* vtx2xyz,
+                      uint32_t* bvhnodes, float* aabb, uint32_t* other_end_out, void* scratch, size_t scratch_bytes);
+size_t build_scratch_bytes(uint32_t T);
 
 // ---------------------------------------------------------------- build.cu
 constexpr int kAabbBlocks = 1024;  // upper bound on centroid-AABB reduction blocks

@@ -39,6 +39,11 @@ _SIGNATURES = {
     "dm_batch_cast_scratch_bytes": (sz, [u32, u32]),
 }
 
+# request-server entry points; their ctypes signatures (with the request /
+# result structures) are set by del_msh_gb300.serve
+SERVER_FUNCS = ("dm_server_create", "dm_server_register_mesh", "dm_server_submit", "dm_server_wait",
+                "dm_server_run_trace", "dm_plain_run_trace", "dm_server_stats_get", "dm_server_destroy")
+
 # entry points that return a status code
 STATUS_FUNCS = {k for k, (r, _) in _SIGNATURES.items() if r is i32 and k != "dm_device_status"}
 
@@ -78,7 +83,7 @@ def load(build_if_missing: bool = False):
 
 
 def exported_symbols():
-    return sorted(_SIGNATURES)
+    return sorted(set(_SIGNATURES) | set(SERVER_FUNCS))
 
 
 def call(name: str, *args):

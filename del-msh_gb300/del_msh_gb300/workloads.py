@@ -216,7 +216,8 @@ def ragged_batch(num_mesh: int = 4096, tmin: int = 64, tmax: int = 65536, jitter
     for i in range(num_mesh):
         t = float(target[i])
         if kinds[i] == 0:
-            level = int(np.clip(round(math.log(max(t, 20) / 20.0, 4)), 1, 6))
+            top = max(1, int(math.floor(math.log(tmax / 20.0, 4))))  # keep 20*4^level <= tmax
+            level = int(np.clip(round(math.log(max(t, 20) / 20.0, 4)), 1, top))
             if level not in ico_cache:
                 ico_cache[level] = icosphere(level)
             tri, vtx = ico_cache[level]

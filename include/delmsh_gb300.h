@@ -202,6 +202,72 @@ int dm_batch_pix2tri_by_raycast(uint64_t stream_ptr, uint32_t num_mesh, const ui
                                 size_t scratch_bytes);
 size_t dm_batch_cast_scratch_bytes(uint32_t num_ray, uint32_t max_tri_per_mesh);
 
+/* ---- serving: a request server keeping built trees resident in HBM ----
+ * No reference counterpart (del-msh has no serving loop).  A dispatcher thread
+ * admits each submitted request when one of num_slots slots (a CUDA stream
+ * with preallocated scratch) is free and the request's mesh is resident,
+ * evicting least-recently-used idle meshes to stay under budget_bytes;
+ * admitted requests run concurrently.  A mesh's tree topology is always built
+ * from its rest pose and `frame` selects the vertex state (0 = rest, f > 0 =
+ * rest + deform_amplitude*sin(phase_v + f + axis), phase_v a hash of the
+ * mesh's deform_seed and v), so every result is a pure function of its
+ * request: the same bits alone or in any mix.  Host arrays of a request must
+ * stay valid until it completes (pinned memory keeps the copies
+ * asynchronous). */
+#define DM_REQ_BUILD_CAST 0u /* full build from the rest pose, state -> frame, pixel cast */
+#define DM_REQ_REFIT_CAST 1u /* state -> frame by refitting the resident tree, pixel cast */
+#define DM_REQ_CAST_RAYS 2u  /* state -> frame if needed, cast of explicit rays */
+
+typedef struct dm_request {
+  uint32_t kind;
+  uint32_t mesh_id;
+  uint32_t frame;
+  float deform_amplitude;
+  uint32_t img_w, img_h;              /* pixel casts */
+  uint32_t num_ray;                   /* DM_REQ_CAST_RAYS */
+  uint32_t reserved;
+  const float* transform_ndc2world;   /* host, 16 floats column-major (pixel casts) */
+  const float* ray_org;               /* host, num_ray*3 (DM_REQ_CAST_RAYS) */
+  const float* ray_dir;               /* host, num_ray*3 */
+  uint32_t* out_tri;                  /* host, one hit id per pixel / ray (u32::MAX = miss) */
+  float* out_t;                       /* host, hit t per pixel / ray (+inf = miss), may be NULL */
+} dm_request;
+
+typedef struct dm_result {
+  int32_t status;
+  uint32_t resident_hit;              /* 1 if the mesh's tree was resident and built at admission */
+  uint64_t t_submit_ns, t_admit_ns, t_done_ns;  /* steady clock */
+} dm_result;
+
+typedef struct dm_server_stats {
+  uint64_t submitted, completed, resident_hits, builds, refits, evictions;
+  uint64_t bytes_resident, bytes_budget, bytes_slots;
+  uint32_t meshes_resident, reserved;
+} dm_server_stats;
+
+typedef struct dm_server dm_server;
+
+/* max_tri: largest mesh to be registered; max_out: most pixels / rays of one request. */
+int dm_server_create(int device, size_t budget_bytes, int num_slots, uint32_t max_tri, uint32_t max_out,
+                     dm_server** out);
+/* Copies the mesh into server-owned pinned host memory. */
+int dm_server_register_mesh(dm_server* server, uint32_t mesh_id, const uint32_t* tri2vtx, uint32_t num_tri,
+                            const float* vtx2xyz, uint32_t num_vtx, uint32_t deform_seed);
+int dm_server_submit(dm_server* server, const dm_request* req, uint64_t* ticket);
+/* Blocks until the request completes; returns its status. */
+int dm_server_wait(dm_server* server, uint64_t ticket, dm_result* out);
+/* Submits reqs[i] at arrival_s[i] seconds after the start (an open-loop
+ * arrival trace), waits for all; latencies count from the scheduled arrival. */
+int dm_server_run_trace(dm_server* server, uint32_t n, const dm_request* reqs, const double* arrival_s,
+                        dm_result* results);
+/* The same trace the straightforward way: one request at a time, each
+ * uploading its mesh, building, refitting to its frame, casting and
+ * downloading, synchronizing before the next; nothing stays resident. */
+int dm_plain_run_trace(dm_server* server, uint32_t n, const dm_request* reqs, const double* arrival_s,
+                       dm_result* results);
+int dm_server_stats_get(dm_server* server, dm_server_stats* out);
+int dm_server_destroy(dm_server* server);
+
 #ifdef __cplusplus
 }
 #endif
