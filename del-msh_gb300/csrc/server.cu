@@ -358,9 +358,9 @@ void dispatch_loop(dm_server* S) {
       j->res.status = DM_OK;
       if (cudaLaunchHostFunc(st, on_done, j) != cudaSuccess) rc = DM_ERR_CUDA;
     }
+    if (rc != DM_OK) cudaStreamSynchronize(st);  // never with the lock held: callbacks take it
     lk.lock();
     if (rc != DM_OK) {
-      cudaStreamSynchronize(st);
       fill_error(&j->res, rc);
       j->res.t_done_ns = now_ns();
       j->done = true;
