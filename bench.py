@@ -509,6 +509,94 @@ def run_served(args):
     return 0
 
 
+def run_soup(args):
+    """Adversarial Morton distribution: 4,194,304-triangle soup whose centroids
+    come from 32 Gaussian clusters (sigma 1e-3 in the unit cube), so many
+    30-bit codes repeat and duplicate runs become long chains in the tree.
+    One step = full LBVH build + cast of 1,048,576 rays from uniformly random
+    points of the cube boundary in uniformly random inward directions."""
+    import torch
+    from del_msh_gb300 import _native
+    from del_msh_gb300 import workloads as W
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    L = _native.load(build_if_missing=True)
+    tri, vtx = W.clustered_soup(4_194_304, seed=SEED)
+    org, d = W.cube_boundary_rays(1_048_576, seed=SEED)
+    T, V, R = tri.shape[0], vtx.shape[0], org.shape[0]
+    d_tri = torch.from_numpy(tri.view(np.int32)).to(dev)
+    d_vtx = torch.from_numpy(vtx).to(dev)
+    d_org, d_dir = torch.from_numpy(org).to(dev), torch.from_numpy(d).to(dev)
+    bvh = torch.empty((2 * T - 1, 3), dtype=torch.int32, device=dev)
+    aabb = torch.empty((2 * T - 1, 6), dtype=torch.float32, device=dev)
+    hit = torch.empty((R,), dtype=torch.int32, device=dev)
+    ht = torch.empty((R,), dtype=torch.float32, device=dev)
+    height = torch.zeros((1,), dtype=torch.int32, device=dev)
+    bs, cs = L.dm_trimesh3_build_scratch_bytes(T), L.dm_cast_scratch_bytes(R, T)
+    b_scr = torch.empty((bs,), dtype=torch.uint8, device=dev)
+    c_scr = torch.empty((cs,), dtype=torch.uint8, device=dev)
+    flush = torch.empty((L2_FLUSH_BYTES,), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+
+    def build():
+        _native.call("dm_trimesh3_build_ex", sp, T, d_tri.data_ptr(), V, d_vtx.data_ptr(), bvh.data_ptr(),
+                     aabb.data_ptr(), None, None, None, None, height.data_ptr(), b_scr.data_ptr(), bs)
+
+    def cast():
+        _native.call("dm_search_bvh3_first_intersection_ray", sp, R, d_org.data_ptr(), d_dir.data_ptr(),
+                     hit.data_ptr(), ht.data_ptr(), None, T, d_tri.data_ptr(), V, d_vtx.data_ptr(), bvh.data_ptr(),
+                     aabb.data_ptr(), c_scr.data_ptr(), cs)
+
+    for _ in range(max(args.warmup, 3)):
+        build()
+        cast()
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
+    for k in range(args.steps):
+        flush.zero_()
+        ev[k][0].record(stream)
+        build()
+        ev[k][1].record(stream)
+        cast()
+        ev[k][2].record(stream)
+    torch.cuda.synchronize()
+    b_ms = statistics.mean(e[0].elapsed_time(e[1]) for e in ev)
+    c_ms = statistics.mean(e[1].elapsed_time(e[2]) for e in ev)
+    stage = (ctypes.c_float * 4)()
+    runs = []
+    for _ in range(5):
+        _native.call("dm_trimesh3_build_profiled", sp, T, d_tri.data_ptr(), V, d_vtx.data_ptr(), bvh.data_ptr(),
+                     aabb.data_ptr(), b_scr.data_ptr(), bs, ctypes.cast(stage, ctypes.c_void_p))
+        runs.append(list(stage))
+    peak, _ = peaks()
+    nb = algorithmic_bytes(T, V, R)
+    line = {"metric": "rays/s (adversarial soup: build + cast per step)", "unit": UNIT,
+            "value": R / ((b_ms + c_ms) * 1e-3), "ms_per_step": b_ms + c_ms, "steps": args.steps,
+            "config": {"workload": "4,194,304-triangle soup in 32 Gaussian clusters (sigma 1e-3), 1,048,576 "
+                                   "cube-boundary rays", "num_tri": T, "num_vtx": V, "rays": R,
+                       "tree_height": int(height.item()), "l2": "flushed between timed steps"},
+            "build_ms": b_ms, "cast_ms": c_ms, "build_tris_per_s": T / (b_ms * 1e-3),
+            "cast_rays_per_s": R / (c_ms * 1e-3),
+            "stage_ms": {k: statistics.mean(r[i] for r in runs)
+                         for i, k in enumerate(("morton", "sort", "topology", "refit"))},
+            "build_roofline_frac": nb["build"] / (b_ms * 1e-3) / 1e9 / peak,
+            "hits": int((hit != -1).sum().item()), "device_status": _native.device_status(clear=True)}
+    if not args.no_cpu:
+        from oracle import build as obuild
+        from oracle import oracle as O
+        obuild.build_oracle()
+        t0 = time.perf_counter()
+        r = O.build(tri, vtx)
+        t1 = time.perf_counter()
+        O.cast_rays(org, d, tri, vtx, r["bvhnodes"], r["bvhnode2aabb"])
+        t2 = time.perf_counter()
+        line["cpu_baseline"] = {"build_s": t1 - t0, "cast_s": t2 - t1, "cores": O.default_threads(), "kind": "port",
+                                "value": R / (t2 - t0), "unit": UNIT}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def read_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from the committed ncu summary
     (profiles/ncu_config2.md lines `traffic <kernel> <bytes>`), else None."""
@@ -529,7 +617,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--workload", choices=["single", "batched", "served"], default="single")
+    ap.add_argument("--workload", choices=["single", "batched", "served", "soup"], default="single")
     ap.add_argument("--num-mesh", type=int, default=4096, help="meshes of the batched workload")
     ap.add_argument("--pool", type=int, default=512, help="meshes of the served pool")
     ap.add_argument("--requests", type=int, default=1000, help="requests per served trace")
@@ -544,6 +632,8 @@ def main():
         return run_batched(args)
     if args.workload == "served":
         return run_served(args)
+    if args.workload == "soup":
+        return run_soup(args)
     return run_ours(args)
 
 
