@@ -324,14 +324,23 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
   if (height_out) *height_out = h;
 }
 
-// Windowed refit.  Block b owns the kWinLeaves sorted leaves starting at
-// b*kWinLeaves (global leaf order, across the meshes of a batch).  A branch
-// whose whole leaf range lies in the window (known from other_end: a branch
-// index is one end of its range) gets both arrivals from this block, so its
-// arrival counter and both child boxes live in shared memory and need only
-// block-scope ordering; only branches whose range crosses a window edge (about
-// 2 per window per tree level above the window) use the global acquire-release
-// arrival of k_refit.  Values and merge order are those of k_refit.
+// Windowed refit, in two kernels.
+//
+// k_leaf_boxes writes the box of every leaf.  k_refit_win then gives block b
+// the kWinLeaves sorted leaves starting at b*kWinLeaves (global leaf order,
+// across the meshes of a batch) and climbs from them.  A branch whose whole
+// leaf range lies in the window (known from other_end: a branch index is one
+// end of its range) gets both arrivals from this block, so its arrival
+// counter and both child boxes live in shared memory and need only
+// block-scope ordering; only branches whose range crosses a window edge use
+// the global acquire-release arrival of k_refit.
+//
+// Link chains (branch j with left child leaf j and right child branch j+1; a
+// run of equal Morton codes is one long chain) are not climbed level by
+// level: the leaf of a link does not climb, and the thread that completes the
+// branch below the chain walks the whole chain upward alone, box(j) =
+// from_two(leaf j, box(j+1)), with no arrival counter, prefetching the next
+// link's record and leaf box.  Values and merge order are those of k_refit.
 constexpr int kWinLeaves = 512;
 constexpr int kWinThreads = 256;
 
@@ -355,13 +364,58 @@ __device__ __forceinline__ uint32_t mesh_of_leaf(const Segments& seg, uint32_t i
   return lo;
 }
 
+// Offsets of the mesh owning global leaf i (single mesh: everything zero).
+struct LeafMesh {
+  uint32_t m, t0, T, v0, V;
+  bool ok;
+};
+
+template <bool kBatch>
+__device__ __forceinline__ LeafMesh leaf_mesh(const Segments& seg, uint32_t total_tri, uint32_t num_vtx_single,
+                                              uint32_t i) {
+  LeafMesh r{0, 0, total_tri, 0, num_vtx_single, true};
+  if (kBatch) {
+    r.m = mesh_of_leaf(seg, i);
+    r.t0 = __ldg(seg.tri_off + r.m);
+    r.T = __ldg(seg.tri_off + r.m + 1) - r.t0;
+    r.v0 = __ldg(seg.vtx_off + r.m);
+    r.V = __ldg(seg.vtx_off + r.m + 1) - r.v0;
+  }
+  r.ok = !(i < r.t0 || i - r.t0 >= r.T || r.T > 0x7FFFFFFFu);  // false only with invalid offsets
+  return r;
+}
+
+template <bool kBatch>
+__global__ void __launch_bounds__(kThreads) k_leaf_boxes(uint32_t total_tri, Segments seg, uint32_t num_vtx_single,
+                                                        const uint32_t* __restrict__ bvhnodes_all,
+                                                        const uint32_t* __restrict__ tri2vtx_all,
+                                                        const float* __restrict__ vtx0_all,
+                                                        const float* __restrict__ vtx1_all, float* aabb_all,
+                                                        uint32_t* status) {
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  if (i >= total_tri) return;
+  const LeafMesh lm = leaf_mesh<kBatch>(seg, total_tri, num_vtx_single, i);
+  if (!lm.ok) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  const size_t node_off = 2ull * lm.t0 - lm.m;
+  const uint32_t leaf = lm.T - 1 + (i - lm.t0);
+  const uint32_t it = __ldg(bvhnodes_all + 3 * (node_off + leaf) + 1);
+  if (it >= lm.T) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  const uint32_t* t2v = tri2vtx_all + 3ull * lm.t0;
+  Box b = leaf_box(t2v, lm.V, vtx0_all + 3ull * lm.v0, it, status);
+  if (vtx1_all) b = box_union(b, leaf_box(t2v, lm.V, vtx1_all + 3ull * lm.v0, it, status));
+  box_store(aabb_all + 6 * (node_off + leaf), b);
+}
+
 template <bool kBatch>
 __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, Segments seg, uint32_t num_vtx_single,
                                                           const uint32_t* __restrict__ bvhnodes_all,
-                                                          const uint32_t* __restrict__ other_all,
-                                                          const uint32_t* __restrict__ tri2vtx_all,
-                                                          const float* __restrict__ vtx0_all,
-                                                          const float* __restrict__ vtx1_all, float* aabb_all,
+                                                          const uint32_t* __restrict__ other_all, float* aabb_all,
                                                           uint32_t* gflags_all, uint32_t* height_out,
                                                           uint32_t* status) {
   extern __shared__ __align__(16) unsigned char win_raw[];
@@ -371,16 +425,14 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, S
     S.flag[k] = 0u;
     const uint32_t g = wA + k;  // position in the global leaf order
     if (g >= total_tri) continue;
-    uint32_t m = 0, t0 = 0, T = total_tri;
-    if (kBatch) {
-      m = mesh_of_leaf(seg, g);
-      t0 = __ldg(seg.tri_off + m);
-      T = __ldg(seg.tri_off + m + 1) - t0;
-    }
-    if (g < t0 || T > 0x7FFFFFFFu) continue;  // only with invalid offsets
-    const uint32_t n = g - t0;  // branch n of mesh m, if it exists
-    if (n + 1 >= T) continue;
-    const size_t node_off = 2ull * t0 - m, int_off = static_cast<size_t>(t0) - m;
+    const LeafMesh lm = leaf_mesh<kBatch>(seg, total_tri, num_vtx_single, g);
+    if (!lm.ok) continue;
+    const size_t node_off = 2ull * lm.t0 - lm.m, int_off = static_cast<size_t>(lm.t0) - lm.m;
+    const uint32_t n = g - lm.t0;  // leaf n and (if it exists) branch n of mesh m
+    const float2* lb = reinterpret_cast<const float2*>(aabb_all + 6 * (node_off + lm.T - 1 + n));
+    const float2 a = __ldcg(lb), bb = __ldcg(lb + 1), c = __ldcg(lb + 2);
+    S.leaf[k] = Box{{a.x, a.y, bb.x}, {bb.y, c.x, c.y}};
+    if (n + 1 >= lm.T) continue;
     const uint32_t* r = bvhnodes_all + 3 * (node_off + n);
     S.rec[k][0] = __ldg(r);
     S.rec[k][1] = __ldg(r + 1);
@@ -391,57 +443,82 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, S
   for (uint32_t k = threadIdx.x; k < static_cast<uint32_t>(kWinLeaves); k += kWinThreads) {
     const uint32_t i = wA + k;
     if (i >= total_tri) break;
-    uint32_t m = 0, t0 = 0, T = total_tri, v0 = 0, V = num_vtx_single;
-    if (kBatch) {
-      m = mesh_of_leaf(seg, i);
-      t0 = __ldg(seg.tri_off + m);
-      T = __ldg(seg.tri_off + m + 1) - t0;
-      v0 = __ldg(seg.vtx_off + m);
-      V = __ldg(seg.vtx_off + m + 1) - v0;
-    }
-    if (i < t0 || i - t0 >= T || T > 0x7FFFFFFFu) {  // only with invalid offsets
-      raise_status(status, kStatusBadIndex);
-      continue;
-    }
-    const size_t node_off = 2ull * t0 - m, int_off = static_cast<size_t>(t0) - m;
+    const LeafMesh lm = leaf_mesh<kBatch>(seg, total_tri, num_vtx_single, i);
+    if (!lm.ok) continue;
+    const uint32_t t0 = lm.t0, T = lm.T;
+    const size_t node_off = 2ull * t0 - lm.m, int_off = static_cast<size_t>(t0) - lm.m;
     const uint32_t* bn = bvhnodes_all + 3 * node_off;
     const uint32_t* oe = other_all + int_off;
     float* aabb = aabb_all + 6 * node_off;
     uint32_t* gflags = gflags_all + int_off;
-    const uint32_t* t2v = tri2vtx_all + 3ull * t0;
-    const float* x0 = vtx0_all + 3ull * v0;
-    const float* x1 = vtx1_all ? vtx1_all + 3ull * v0 : nullptr;
     const uint32_t num_node = 2 * T - 1;
-    const uint32_t leaf = T - 1 + (i - t0);
-    const uint32_t it = __ldg(bn + static_cast<size_t>(leaf) * 3 + 1);
-    if (it >= T) {
-      raise_status(status, kStatusBadIndex);
-      continue;
-    }
-    Box b = leaf_box(t2v, V, x0, it, status);
-    if (x1) b = box_union(b, leaf_box(t2v, V, x1, it, status));
-    box_store(aabb + static_cast<size_t>(leaf) * 6, b);
-    S.leaf[k] = b;
-    uint32_t h = 1, prev = leaf, guard = 0;
+    const uint32_t n = i - t0;
+    const uint32_t leaf = T - 1 + n;
     uint32_t node = __ldg(bn + static_cast<size_t>(leaf) * 3);
+    // the left leaf of a link is folded in by the chain walk, not climbed
+    if (node == n && n + 1 < T - 1 && S.rec[k][1] == leaf && S.rec[k][2] == n + 1) continue;
+    Box b = S.leaf[k];
+    uint32_t h = 1, prev = leaf, guard = 0;
+    auto in_win = [&](uint32_t x) { return t0 + x >= wA && t0 + x < wA + kWinLeaves; };
+    auto record = [&](uint32_t x, uint32_t& parent, uint32_t& c0, uint32_t& c1, uint32_t& other) {
+      if (in_win(x)) {
+        const uint32_t* r = S.rec[t0 + x - wA];
+        parent = r[0];
+        c0 = r[1];
+        c1 = r[2];
+        other = r[3];
+      } else {
+        parent = __ldg(bn + static_cast<size_t>(x) * 3);
+        c0 = __ldg(bn + static_cast<size_t>(x) * 3 + 1);
+        c1 = __ldg(bn + static_cast<size_t>(x) * 3 + 2);
+        other = __ldg(oe + x);
+      }
+    };
+    auto leafbox = [&](uint32_t j) -> Box {
+      if (in_win(j)) return S.leaf[t0 + j - wA];
+      const float2* p2 = reinterpret_cast<const float2*>(aabb + static_cast<size_t>(T - 1 + j) * 6);
+      const float2 a = __ldcg(p2), bb = __ldcg(p2 + 1), c = __ldcg(p2 + 2);
+      return Box{{a.x, a.y, bb.x}, {bb.y, c.x, c.y}};
+    };
     while (node != kUMax) {
       if (node >= T - 1 || ++guard > num_node) {
         raise_status(status, kStatusBadIndex);
         break;
       }
       uint32_t parent, c0, c1, other;
-      const bool in_win = (t0 + node >= wA) && (t0 + node < wA + kWinLeaves);
-      if (in_win) {
-        const uint32_t* r = S.rec[t0 + node - wA];
-        parent = r[0];
-        c0 = r[1];
-        c1 = r[2];
-        other = r[3];
-      } else {
-        parent = __ldg(bn + static_cast<size_t>(node) * 3);
-        c0 = __ldg(bn + static_cast<size_t>(node) * 3 + 1);
-        c1 = __ldg(bn + static_cast<size_t>(node) * 3 + 2);
-        other = __ldg(oe + node);
+      record(node, parent, c0, c1, other);
+      if (c0 == T - 1 + node && c1 == node + 1 && prev == c1) {
+        // chain walk: node is a link reached from its right child
+        uint32_t j = node, pj = parent;
+        Box lb = leafbox(j);
+        for (;;) {
+          uint32_t pp = kUMax, pl = 0, pr = 0, po = 0;
+          Box lbn{};
+          const bool may = (pj != kUMax && pj + 1 == j && pj < T - 1);
+          if (may) {  // prefetch the next link
+            record(pj, pp, pl, pr, po);
+            lbn = leafbox(pj);
+          }
+          b = box_union(lb, b);
+          box_store(aabb + static_cast<size_t>(j) * 6, b);
+          if (in_win(j)) S.node[t0 + j - wA] = b;
+          h += 1;
+          prev = j;
+          if (++guard > num_node) {
+            raise_status(status, kStatusBadIndex);
+            pj = kUMax;
+            break;
+          }
+          if (may && pl == T - 1 + pj && pr == j) {
+            j = pj;
+            pj = pp;
+            lb = lbn;
+            continue;
+          }
+          break;
+        }
+        node = pj;
+        continue;
       }
       const uint32_t lo = node < other ? node : other, hi = node < other ? other : node;
       const bool local = (t0 + lo >= wA) && (t0 + hi < wA + kWinLeaves);
@@ -465,15 +542,24 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, S
       const bool mine_first = (c0 == prev);
       const uint32_t sib = mine_first ? c1 : c0;
       Box sb;
-      if (local) sb = (sib >= T - 1) ? S.leaf[t0 + (sib - (T - 1)) - wA] : S.node[t0 + sib - wA];
-      else sb = box_load_cg(aabb + static_cast<size_t>(sib) * 6);
+      if (local) {
+        // a valid tree keeps the sibling inside the window; check it anyway
+        const uint32_t slot = (sib >= T - 1) ? t0 + (sib - (T - 1)) - wA : t0 + sib - wA;
+        if (slot >= static_cast<uint32_t>(kWinLeaves)) {
+          raise_status(status, kStatusBadIndex);
+          break;
+        }
+        sb = (sib >= T - 1) ? S.leaf[slot] : S.node[slot];
+      } else {
+        sb = box_load_cg(aabb + static_cast<size_t>(sib) * 6);
+      }
       b = mine_first ? box_union(b, sb) : box_union(sb, b);
       box_store(aabb + static_cast<size_t>(node) * 6, b);
       if (local) S.node[t0 + node - wA] = b;
       prev = node;
       node = parent;
     }
-    if (node == kUMax && height_out) height_out[m] = h;
+    if (node == kUMax && height_out) height_out[lm.m] = h;
   }
 }
 
@@ -523,6 +609,7 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   if (total_tri == 0) return;
   const int smem = static_cast<int>(sizeof(WinSmem));
   const uint32_t grid = (total_tri + kWinLeaves - 1) / kWinLeaves;
+  const uint32_t leaf_grid = (total_tri + kThreads - 1) / kThreads;
   // the attribute is per device; set it once so that later calls (possibly
   // under stream capture) make no further runtime configuration calls
   static bool configured[64] = {false};
@@ -534,11 +621,15 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
     configured[dev] = true;
   }
   if (seg.tri_off) {
-    k_refit_win<true><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
-                                                      vtx2xyz0, vtx2xyz1, aabb, flags, height_out, status);
+    k_leaf_boxes<true><<<leaf_grid, kThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, tri2vtx, vtx2xyz0,
+                                                      vtx2xyz1, aabb, status);
+    k_refit_win<true><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, aabb, flags,
+                                                      height_out, status);
   } else {
-    k_refit_win<false><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
-                                                       vtx2xyz0, vtx2xyz1, aabb, flags, height_out, status);
+    k_leaf_boxes<false><<<leaf_grid, kThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, tri2vtx, vtx2xyz0,
+                                                       vtx2xyz1, aabb, status);
+    k_refit_win<false><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, aabb,
+                                                       flags, height_out, status);
   }
 }
 

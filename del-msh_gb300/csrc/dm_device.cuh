@@ -120,17 +120,19 @@ __device__ __forceinline__ bool tri_ray(float3 p0, float3 p1, float3 p2, float3 
   return true;
 }
 
-// Slab test (Kay & Kajiya 1986; Williams et al. 2005) with precomputed 1/dir:
-// a zero direction component hits iff the origin lies inside that slab.
-// True iff t_enter <= t_exit and t_exit >= 0.
+// Slab test (Kay & Kajiya 1986; Williams et al. 2005) with precomputed 1/dir;
+// entry / exit per axis and their running max / min use IEEE minNum / maxNum
+// (fminf / fmaxf: a NaN operand yields the other), as the CPU restatement
+// does with libm's fminf / fmaxf.  A zero direction component hits iff the
+// origin lies inside that slab.  True iff t_enter <= t_exit and t_exit >= 0.
+// The sign of a zero result may differ from the CPU's; every use of these
+// values is a comparison, for which -0 == +0.
 __device__ __forceinline__ bool slab_axis(float lo, float hi, float o, float inv, float d, float& tmin, float& tmax) {
   if (d != 0.0f) {
     const float t0 = __fmul_rn(__fsub_rn(lo, o), inv);
     const float t1 = __fmul_rn(__fsub_rn(hi, o), inv);
-    const float tn = (t1 < t0) ? t1 : t0;
-    const float tf = (t1 < t0) ? t0 : t1;
-    if (tn > tmin) tmin = tn;
-    if (tf < tmax) tmax = tf;
+    tmin = fmaxf(tmin, fminf(t0, t1));
+    tmax = fminf(tmax, fmaxf(t0, t1));
     return true;
   }
   return !(o < lo || o > hi);

@@ -21,6 +21,16 @@
 // is resolved inline; a far child that must be searched continues in the
 // enclosing level after folding R(near) into "saved".
 //
+// Link chains.  A "link" branch i has the leaf i (node T-1+i) as left child
+// and branch i+1 as right child; a run of k equal Morton codes is a chain of
+// k-1 links.  When a link's near child is branch i+1 and both boxes are hit,
+// its frame is (far = leaf i, enter, saved); along a descent through
+// consecutive links every frame after the first has saved = none, so the
+// whole run is kept as one chain frame (first link s, last link t, saved of
+// s) and unwound leaf by leaf (t, t-1, ..., s), recomputing each far leaf's
+// slab entry.  The stack then grows with the number of runs, not their
+// length, and the decisions are exactly those of the uncompressed frames.
+//
 // Execution.  The traversal is a step function (one node entry plus the
 // ascent that follows it) run by persistent warps: a lane whose ray is
 // finished takes the next ray index from a global counter (one atomic per
@@ -98,12 +108,15 @@ struct GlobalStack {
   __device__ __forceinline__ uint4 load(uint32_t i) const { return __ldcg(p + i); }
 };
 
+constexpr uint32_t kChainBit = 0x80000000u;  // frame.x flag of a chain frame (node ids are < 2^31)
+
 // Per-ray traversal state between steps.
 struct Trav {
   uint32_t node;         // node to enter next
   uint32_t left, right;  // its record (bvhnodes[node*3+1], [node*3+2]), fetched ahead
   uint32_t sp;           // frames in use
   uint32_t steps;        // node entries so far (bounded by the node count)
+  uint32_t chain_next;   // the link that would extend the top chain frame, or kUMax
   Hit best;              // accumulator of the current level
 };
 
@@ -120,6 +133,7 @@ __device__ __forceinline__ bool trav_begin(const MeshView& m, const Ray& r, Trav
   s.node = 0;
   s.sp = 0;
   s.steps = 0;
+  s.chain_next = kUMax;
   s.best = Hit{INFINITY, kUMax};
   load_record(m.bvhnodes, 0, s.left, s.right);
   float te, tx;
@@ -146,7 +160,7 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
     if (leaf_hit(m, r, s.left, t, u, v, bad)) s.best = pick(s.best, Hit{t, s.left});
     ascend = true;
   } else {
-    const uint32_t left = s.left, right = s.right;
+    const uint32_t node = s.node, left = s.left, right = s.right;
     if (left >= num_node || right >= num_node) {
       bad = true;
       return kStepDone;
@@ -183,8 +197,19 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
         s.left = n_l;
         s.right = n_r;
       } else {
-        if (s.sp >= cap) return kStepOverflow;
-        stack.store(s.sp++, make_uint4(nf, __float_as_uint(far_enter), __float_as_uint(s.best.t), s.best.id));
+        const bool link = !near_left && left == m.num_tri - 1 + node && right == node + 1;
+        if (link && node == s.chain_next && s.best.id == kUMax) {
+          // extend the chain frame on top: its last link becomes `node`
+          const uint4 f = stack.load(s.sp - 1);
+          stack.store(s.sp - 1, make_uint4(f.x, node, f.z, f.w));
+        } else {
+          if (s.sp >= cap) return kStepOverflow;
+          if (link)
+            stack.store(s.sp++, make_uint4(kChainBit | node, node, __float_as_uint(s.best.t), s.best.id));
+          else
+            stack.store(s.sp++, make_uint4(nf, __float_as_uint(far_enter), __float_as_uint(s.best.t), s.best.id));
+        }
+        s.chain_next = link ? node + 1 : kUMax;
         s.best = Hit{INFINITY, kUMax};
         s.node = nn;
         s.left = n_l;
@@ -193,13 +218,39 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
     }
   }
   if (!ascend) return kStepContinue;
+  s.chain_next = kUMax;
   while (s.sp > 0) {
-    const uint4 f = stack.load(--s.sp);
+    const uint4 f = stack.load(s.sp - 1);
     const Hit saved{__uint_as_float(f.z), f.w};
-    const bool skip = (s.best.id != kUMax) && __uint_as_float(f.y) > s.best.t;
-    s.best = pick(saved, s.best);
+    uint32_t far;
+    float far_enter;
+    if (f.x & kChainBit) {
+      // level j = f.y of a chain frame: far child = leaf j, saved = none
+      // unless j is the chain's first link
+      const uint32_t first = f.x & ~kChainBit, j = f.y;
+      far = m.num_tri - 1 + j;
+      if (far >= num_node) {
+        bad = true;
+        return kStepDone;
+      }
+      float te = 0.f, tx = 0.f;
+      node_slab(m, r, far, te, tx);  // hit when the frame was pushed; same value again
+      far_enter = te;
+      if (j == first) {
+        --s.sp;
+        s.best = pick(saved, s.best);
+      } else {
+        stack.store(s.sp - 1, make_uint4(f.x, j - 1, f.z, f.w));
+      }
+    } else {
+      --s.sp;
+      far = f.x;
+      far_enter = __uint_as_float(f.y);
+      s.best = pick(saved, s.best);
+    }
+    const bool skip = (s.best.id != kUMax) && far_enter > s.best.t;
     if (!skip) {
-      s.node = f.x;
+      s.node = far;
       if (s.node >= num_node) {
         bad = true;
         return kStepDone;

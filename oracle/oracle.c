@@ -435,9 +435,12 @@ int or_tri3_ray_f64(const float p0[3], const float p1[3], const float p2[3], con
 }
 
 /* Slab test (Kay & Kajiya 1986; Williams et al., "An Efficient and Robust
- * Ray-Box Intersection Algorithm", 2005) with precomputed 1/dir.  An axis with
+ * Ray-Box Intersection Algorithm", 2005) with precomputed 1/dir, the per-axis
+ * entry / exit and their running max / min taken with IEEE 754 minNum /
+ * maxNum (fminf / fmaxf: a NaN operand yields the other one).  An axis with
  * dir == 0 is a hit iff the origin lies inside the slab.  Returns 1 and
- * (t_enter, t_exit) iff t_enter <= t_exit and t_exit >= 0. */
+ * (t_enter, t_exit) iff t_enter <= t_exit and t_exit >= 0.  (The sign of a
+ * zero result is unspecified; no decision depends on it.) */
 int or_aabb3_ray(const float aabb[6], const float org[3], const float inv_dir[3], const float dir[3], float* t_enter,
                  float* t_exit) {
   float tmin = -INFINITY, tmax = INFINITY;
@@ -445,10 +448,8 @@ int or_aabb3_ray(const float aabb[6], const float org[3], const float inv_dir[3]
     if (dir[d] != 0.0f) {
       const float t0 = (aabb[d] - org[d]) * inv_dir[d];
       const float t1 = (aabb[d + 3] - org[d]) * inv_dir[d];
-      const float tn = (t1 < t0) ? t1 : t0;
-      const float tf = (t1 < t0) ? t0 : t1;
-      if (tn > tmin) tmin = tn;
-      if (tf < tmax) tmax = tf;
+      tmin = fmaxf(tmin, fminf(t0, t1));
+      tmax = fminf(tmax, fmaxf(t0, t1));
     } else if (org[d] < aabb[d] || org[d] > aabb[d + 3]) {
       return 0;
     }
