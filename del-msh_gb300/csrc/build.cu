@@ -1,6 +1,7 @@
 // build.cu — LBVH build kernels: centroid AABB + fit transform, Morton codes
 // (with the radix sort's digit histogram fused in), Karras topology and the
 // bottom-up AABB refit.  All of them are HBM-bound integer / min-max work.
+#include <algorithm>
 #include <cfloat>
 #include <cuda/atomic>
 
@@ -127,6 +128,7 @@ __global__ void __launch_bounds__(kThreads) k_centroid_aabb(uint32_t num_tri, co
     }
     __threadfence();
     s_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+    __threadfence();  // acquire: the other blocks' partials
   }
   __syncthreads();
   if (!s_last) return;
@@ -326,32 +328,41 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
 
 // Windowed refit, in two kernels.
 //
-// k_leaf_boxes writes the box of every leaf.  k_refit_win then gives block b
-// the kWinLeaves sorted leaves starting at b*kWinLeaves (global leaf order,
-// across the meshes of a batch) and climbs from them.  A branch whose whole
-// leaf range lies in the window (known from other_end: a branch index is one
-// end of its range) gets both arrivals from this block, so its arrival
-// counter and both child boxes live in shared memory and need only
-// block-scope ordering; only branches whose range crosses a window edge use
-// the global acquire-release arrival of k_refit.
+// k_refit_win gives block b the kRefitWindow sorted leaves starting at
+// b*kRefitWindow (global leaf order, across the meshes of a batch).  It
+// writes their leaf boxes and climbs from them through every branch whose
+// whole leaf range lies in the window ("local": known from other_end, since
+// a branch index is one end of its range).  Both arrivals at a local branch
+// come from this block, so its arrival counter and child boxes live in
+// shared memory and the whole local climb reads no global memory.
+//
+// A climb that reaches a branch whose range crosses the window edge stops
+// there.  At a crossing branch it makes the global acquire-release arrival
+// of k_refit; the first arriver is done, the second merges the branch and
+// hands its parent to k_refit_top through a small queue.  Only the LCA of a
+// window boundary can get both arrivals here, and only the link just below a
+// window can be reached from a local right child, so the queue holds at most
+// two entries per window.  k_refit_top climbs the remaining top of the tree
+// from the queue entries with global arrivals.
 //
 // Link chains (branch j with left child leaf j and right child branch j+1; a
-// run of equal Morton codes is one long chain) are not climbed level by
-// level: the leaf of a link does not climb, and the thread that completes the
-// branch below the chain walks the whole chain upward alone, box(j) =
-// from_two(leaf j, box(j+1)), with no arrival counter, prefetching the next
-// link's record and leaf box.  Values and merge order are those of k_refit.
-constexpr int kWinLeaves = 512;
+// run of equal Morton codes is one long chain) need no arrival counter: the
+// leaf of a link never climbs, and the climb that completes branch j+1 folds
+// the chain upward, box(j) = from_two(leaf j, box(j+1)).  In k_refit_top the
+// fold prefetches eight links at a time (their records and leaf boxes sit at
+// consecutive addresses).  Values and merge order are those of k_refit.
 constexpr int kWinThreads = 256;
+constexpr int kWinPerThread = kRefitWindow / kWinThreads;
+constexpr int kFoldDepth = 8;
+static_assert(kWinPerThread * kWinThreads == kRefitWindow, "window");
 
-// Every branch whose range lies in the window has its index in the window,
-// so the records and other ends of branches wA..wA+kWinLeaves-1 are loaded
-// into shared memory once (coalesced) and the in-window climb reads no L2.
+// The records and other ends of branches wA..wA+kRefitWindow-1 (every local
+// branch has its index in the window) are loaded into shared memory once.
 struct WinSmem {
-  uint32_t flag[kWinLeaves];
-  uint32_t rec[kWinLeaves][4];  // parent, left, right, other end
-  Box leaf[kWinLeaves];
-  Box node[kWinLeaves];
+  uint32_t flag[kRefitWindow];
+  uint32_t rec[kRefitWindow][4];  // parent, left, right, other end
+  Box leaf[kRefitWindow];
+  Box node[kRefitWindow];
 };
 
 __device__ __forceinline__ uint32_t mesh_of_leaf(const Segments& seg, uint32_t i) {
@@ -385,183 +396,621 @@ __device__ __forceinline__ LeafMesh leaf_mesh(const Segments& seg, uint32_t tota
   return r;
 }
 
-template <bool kBatch>
-__global__ void __launch_bounds__(kThreads) k_leaf_boxes(uint32_t total_tri, Segments seg, uint32_t num_vtx_single,
-                                                        const uint32_t* __restrict__ bvhnodes_all,
-                                                        const uint32_t* __restrict__ tri2vtx_all,
-                                                        const float* __restrict__ vtx0_all,
-                                                        const float* __restrict__ vtx1_all, float* aabb_all,
-                                                        uint32_t* status) {
-  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
-  if (i >= total_tri) return;
-  const LeafMesh lm = leaf_mesh<kBatch>(seg, total_tri, num_vtx_single, i);
-  if (!lm.ok) {
+// Hand-over queue: word 0 counts entries; entries {branch, child, height,
+// global leaf} start at word kRefitQueueHdr.
+__device__ __forceinline__ void queue_push(uint32_t* queue, uint32_t capacity, uint32_t node, uint32_t prev,
+                                           uint32_t h, uint32_t leaf, uint32_t* status) {
+  const uint32_t slot = atomicAdd(queue, 1u);
+  if (slot >= capacity) {
     raise_status(status, kStatusBadIndex);
     return;
   }
-  const size_t node_off = 2ull * lm.t0 - lm.m;
-  const uint32_t leaf = lm.T - 1 + (i - lm.t0);
-  const uint32_t it = __ldg(bvhnodes_all + 3 * (node_off + leaf) + 1);
-  if (it >= lm.T) {
-    raise_status(status, kStatusBadIndex);
-    return;
-  }
-  const uint32_t* t2v = tri2vtx_all + 3ull * lm.t0;
-  Box b = leaf_box(t2v, lm.V, vtx0_all + 3ull * lm.v0, it, status);
-  if (vtx1_all) b = box_union(b, leaf_box(t2v, lm.V, vtx1_all + 3ull * lm.v0, it, status));
-  box_store(aabb_all + 6 * (node_off + leaf), b);
+  reinterpret_cast<uint4*>(queue + kRefitQueueHdr)[slot] = make_uint4(node, prev, h, leaf);
 }
 
 template <bool kBatch>
 __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, Segments seg, uint32_t num_vtx_single,
                                                           const uint32_t* __restrict__ bvhnodes_all,
-                                                          const uint32_t* __restrict__ other_all, float* aabb_all,
-                                                          uint32_t* gflags_all, uint32_t* height_out,
-                                                          uint32_t* status) {
+                                                          const uint32_t* __restrict__ other_all,
+                                                          const uint32_t* __restrict__ tri2vtx_all,
+                                                          const float* __restrict__ vtx0_all,
+                                                          const float* __restrict__ vtx1_all, float* aabb_all,
+                                                          uint32_t* gflags_all, uint32_t* queue, uint32_t capacity,
+                                                          uint32_t* height_out, uint32_t* status) {
+  // runs only when the range-query refit handed over (NaN) or heights are wanted
+  if (*reinterpret_cast<volatile uint32_t*>(queue + 1) == 0u) return;
   extern __shared__ __align__(16) unsigned char win_raw[];
   WinSmem& S = *reinterpret_cast<WinSmem*>(win_raw);
-  const uint32_t wA = blockIdx.x * kWinLeaves;
-  for (int k = threadIdx.x; k < kWinLeaves; k += kWinThreads) {
-    S.flag[k] = 0u;
-    const uint32_t g = wA + k;  // position in the global leaf order
-    if (g >= total_tri) continue;
-    const LeafMesh lm = leaf_mesh<kBatch>(seg, total_tri, num_vtx_single, g);
-    if (!lm.ok) continue;
-    const size_t node_off = 2ull * lm.t0 - lm.m, int_off = static_cast<size_t>(lm.t0) - lm.m;
-    const uint32_t n = g - lm.t0;  // leaf n and (if it exists) branch n of mesh m
-    const float2* lb = reinterpret_cast<const float2*>(aabb_all + 6 * (node_off + lm.T - 1 + n));
-    const float2 a = __ldcg(lb), bb = __ldcg(lb + 1), c = __ldcg(lb + 2);
-    S.leaf[k] = Box{{a.x, a.y, bb.x}, {bb.y, c.x, c.y}};
-    if (n + 1 >= lm.T) continue;
-    const uint32_t* r = bvhnodes_all + 3 * (node_off + n);
-    S.rec[k][0] = __ldg(r);
-    S.rec[k][1] = __ldg(r + 1);
-    S.rec[k][2] = __ldg(r + 2);
-    S.rec[k][3] = __ldg(other_all + int_off + n);
-  }
-  __syncthreads();
-  for (uint32_t k = threadIdx.x; k < static_cast<uint32_t>(kWinLeaves); k += kWinThreads) {
-    const uint32_t i = wA + k;
-    if (i >= total_tri) break;
-    const LeafMesh lm = leaf_mesh<kBatch>(seg, total_tri, num_vtx_single, i);
-    if (!lm.ok) continue;
-    const uint32_t t0 = lm.t0, T = lm.T;
-    const size_t node_off = 2ull * t0 - lm.m, int_off = static_cast<size_t>(t0) - lm.m;
-    const uint32_t* bn = bvhnodes_all + 3 * node_off;
-    const uint32_t* oe = other_all + int_off;
-    float* aabb = aabb_all + 6 * node_off;
-    uint32_t* gflags = gflags_all + int_off;
-    const uint32_t num_node = 2 * T - 1;
-    const uint32_t n = i - t0;
-    const uint32_t leaf = T - 1 + n;
-    uint32_t node = __ldg(bn + static_cast<size_t>(leaf) * 3);
-    // the left leaf of a link is folded in by the chain walk, not climbed
-    if (node == n && n + 1 < T - 1 && S.rec[k][1] == leaf && S.rec[k][2] == n + 1) continue;
-    Box b = S.leaf[k];
-    uint32_t h = 1, prev = leaf, guard = 0;
-    auto in_win = [&](uint32_t x) { return t0 + x >= wA && t0 + x < wA + kWinLeaves; };
-    auto record = [&](uint32_t x, uint32_t& parent, uint32_t& c0, uint32_t& c1, uint32_t& other) {
-      if (in_win(x)) {
-        const uint32_t* r = S.rec[t0 + x - wA];
-        parent = r[0];
-        c0 = r[1];
-        c1 = r[2];
-        other = r[3];
-      } else {
-        parent = __ldg(bn + static_cast<size_t>(x) * 3);
-        c0 = __ldg(bn + static_cast<size_t>(x) * 3 + 1);
-        c1 = __ldg(bn + static_cast<size_t>(x) * 3 + 2);
-        other = __ldg(oe + x);
+  // persistent over the windows: when the range queries did the work, the
+  // early exit above costs one wave instead of one block per window
+  const uint32_t num_win = (total_tri + kRefitWindow - 1) / kRefitWindow;
+  for (uint32_t win = blockIdx.x; win < num_win; win += gridDim.x) {
+    const uint32_t wA = win * kRefitWindow;
+
+    // Phase 0: leaf boxes, branch records and other ends of the window.  The
+    // dependent loads (leaf record -> triangle -> vertices) of both leaves of a
+    // thread are issued together.
+    LeafMesh lm[kWinPerThread];
+    uint32_t par[kWinPerThread];
+#pragma unroll
+    for (int r = 0; r < kWinPerThread; ++r) {
+      const uint32_t k = threadIdx.x + r * kWinThreads, g = wA + k;
+      S.flag[k] = 0u;
+      lm[r] = leaf_mesh<kBatch>(seg, total_tri, num_vtx_single, g < total_tri ? g : 0u);
+      if (g >= total_tri) lm[r].ok = false;
+      par[r] = kUMax;
+    }
+    uint32_t tri[kWinPerThread];
+#pragma unroll
+    for (int r = 0; r < kWinPerThread; ++r) {
+      const uint32_t k = threadIdx.x + r * kWinThreads;
+      tri[r] = kUMax;
+      if (!lm[r].ok) continue;
+      const size_t node_off = 2ull * lm[r].t0 - lm[r].m;
+      const uint32_t n = wA + k - lm[r].t0;
+      const uint32_t* lr = bvhnodes_all + 3 * (node_off + lm[r].T - 1 + n);
+      par[r] = __ldg(lr);
+      tri[r] = __ldg(lr + 1);
+      if (n + 1 < lm[r].T) {
+        const uint32_t* br = bvhnodes_all + 3 * (node_off + n);
+        S.rec[k][0] = __ldg(br);
+        S.rec[k][1] = __ldg(br + 1);
+        S.rec[k][2] = __ldg(br + 2);
+        S.rec[k][3] = __ldg(other_all + (static_cast<size_t>(lm[r].t0) - lm[r].m) + n);
       }
-    };
-    auto leafbox = [&](uint32_t j) -> Box {
-      if (in_win(j)) return S.leaf[t0 + j - wA];
-      const float2* p2 = reinterpret_cast<const float2*>(aabb + static_cast<size_t>(T - 1 + j) * 6);
-      const float2 a = __ldcg(p2), bb = __ldcg(p2 + 1), c = __ldcg(p2 + 2);
-      return Box{{a.x, a.y, bb.x}, {bb.y, c.x, c.y}};
-    };
-    while (node != kUMax) {
-      if (node >= T - 1 || ++guard > num_node) {
+    }
+#pragma unroll
+    for (int r = 0; r < kWinPerThread; ++r) {
+      const uint32_t k = threadIdx.x + r * kWinThreads;
+      if (!lm[r].ok) continue;
+      if (tri[r] >= lm[r].T) {
         raise_status(status, kStatusBadIndex);
-        break;
+        tri[r] = 0u;
       }
-      uint32_t parent, c0, c1, other;
-      record(node, parent, c0, c1, other);
-      if (c0 == T - 1 + node && c1 == node + 1 && prev == c1) {
-        // chain walk: node is a link reached from its right child
-        uint32_t j = node, pj = parent;
-        Box lb = leafbox(j);
-        for (;;) {
-          uint32_t pp = kUMax, pl = 0, pr = 0, po = 0;
-          Box lbn{};
-          const bool may = (pj != kUMax && pj + 1 == j && pj < T - 1);
-          if (may) {  // prefetch the next link
-            record(pj, pp, pl, pr, po);
-            lbn = leafbox(pj);
-          }
-          b = box_union(lb, b);
-          box_store(aabb + static_cast<size_t>(j) * 6, b);
-          if (in_win(j)) S.node[t0 + j - wA] = b;
-          h += 1;
-          prev = j;
-          if (++guard > num_node) {
-            raise_status(status, kStatusBadIndex);
-            pj = kUMax;
-            break;
-          }
-          if (may && pl == T - 1 + pj && pr == j) {
-            j = pj;
-            pj = pp;
-            lb = lbn;
-            continue;
-          }
-          break;
-        }
-        node = pj;
-        continue;
-      }
-      const uint32_t lo = node < other ? node : other, hi = node < other ? other : node;
-      const bool local = (t0 + lo >= wA) && (t0 + hi < wA + kWinLeaves);
-      uint32_t old;
-      if (local) {
-        __threadfence_block();  // this thread's shared box is visible before the arrival
-        old = atomicAdd(&S.flag[t0 + node - wA], h);
-        if (old == 0u) break;
-        __threadfence_block();
-      } else {
-        cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrival(gflags[node]);
-        old = arrival.fetch_add(h, cuda::memory_order_acq_rel);
-        if (old == 0u) break;
-        gflags[node] = 0u;
-      }
-      h = (old > h ? old : h) + 1;
-      if (c0 >= num_node || c1 >= num_node || (c0 != prev && c1 != prev)) {
-        raise_status(status, kStatusBadIndex);
-        break;
-      }
-      const bool mine_first = (c0 == prev);
-      const uint32_t sib = mine_first ? c1 : c0;
-      Box sb;
-      if (local) {
-        // a valid tree keeps the sibling inside the window; check it anyway
-        const uint32_t slot = (sib >= T - 1) ? t0 + (sib - (T - 1)) - wA : t0 + sib - wA;
-        if (slot >= static_cast<uint32_t>(kWinLeaves)) {
+      const uint32_t* t2v = tri2vtx_all + 3ull * lm[r].t0;
+      const float* v0 = vtx0_all + 3ull * lm[r].v0;
+      Box bx = leaf_box(t2v, lm[r].V, v0, tri[r], status);
+      if (vtx1_all) bx = box_union(bx, leaf_box(t2v, lm[r].V, vtx1_all + 3ull * lm[r].v0, tri[r], status));
+      S.leaf[k] = bx;
+      const size_t node_off = 2ull * lm[r].t0 - lm[r].m;
+      box_store(aabb_all + 6 * (node_off + lm[r].T - 1 + (wA + k - lm[r].t0)), bx);
+    }
+    __syncthreads();
+
+    // Phase 1: climb the local branches.
+#pragma unroll
+    for (int r = 0; r < kWinPerThread; ++r) {
+      if (!lm[r].ok) continue;
+      const uint32_t k = threadIdx.x + r * kWinThreads;
+      const uint32_t t0 = lm[r].t0, T = lm[r].T;
+      const size_t node_off = 2ull * t0 - lm[r].m, int_off = static_cast<size_t>(t0) - lm[r].m;
+      const uint32_t* bn = bvhnodes_all + 3 * node_off;
+      float* aabb = aabb_all + 6 * node_off;
+      const uint32_t num_node = 2 * T - 1;
+      const uint32_t n = wA + k - t0;
+      const uint32_t leaf = T - 1 + n;
+      uint32_t node = par[r];
+      // the left leaf of a link is folded in by the climb through the chain
+      if (node == n && n + 1 < T - 1 && S.rec[k][1] == leaf && S.rec[k][2] == n + 1) continue;
+      Box b = S.leaf[k];
+      uint32_t h = 1, prev = leaf, guard = 0;
+      while (node != kUMax) {
+        if (node >= T - 1 || ++guard > num_node) {
           raise_status(status, kStatusBadIndex);
           break;
         }
-        sb = (sib >= T - 1) ? S.leaf[slot] : S.node[slot];
-      } else {
-        sb = box_load_cg(aabb + static_cast<size_t>(sib) * 6);
+        const uint32_t slot = t0 + node - wA;  // wraps to a large value below the window
+        bool local = slot < static_cast<uint32_t>(kRefitWindow);
+        uint32_t parent = 0, c0 = 0, c1 = 0;
+        if (local) {
+          parent = S.rec[slot][0];
+          c0 = S.rec[slot][1];
+          c1 = S.rec[slot][2];
+          const uint32_t other = S.rec[slot][3];
+          const uint32_t lo = node < other ? node : other, hi = node < other ? other : node;
+          local = (t0 + lo >= wA) && (t0 + hi < wA + kRefitWindow);
+        }
+        if (!local) {
+          // crossing branch: one global step, then stop
+          parent = __ldg(bn + static_cast<size_t>(node) * 3);
+          c0 = __ldg(bn + static_cast<size_t>(node) * 3 + 1);
+          c1 = __ldg(bn + static_cast<size_t>(node) * 3 + 2);
+          if (c0 == T - 1 + node && c1 == node + 1 && prev == c1) {
+            queue_push(queue, capacity, node, prev, h, wA + k, status);
+            break;
+          }
+          cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrival(gflags_all[int_off + node]);
+          const uint32_t old = arrival.fetch_add(h, cuda::memory_order_acq_rel);
+          if (old == 0u) break;
+          gflags_all[int_off + node] = 0u;
+          h = (old > h ? old : h) + 1;
+          if (c0 >= num_node || c1 >= num_node || (c0 != prev && c1 != prev)) {
+            raise_status(status, kStatusBadIndex);
+            break;
+          }
+          const bool mine_first = (c0 == prev);
+          const Box sb = box_load_cg(aabb + static_cast<size_t>(mine_first ? c1 : c0) * 6);
+          b = mine_first ? box_union(b, sb) : box_union(sb, b);
+          box_store(aabb + static_cast<size_t>(node) * 6, b);
+          if (parent != kUMax) queue_push(queue, capacity, parent, node, h, wA + k, status);
+          else if (height_out) height_out[lm[r].m] = h;
+          break;
+        }
+        if (c0 == T - 1 + node && c1 == node + 1 && prev == c1) {
+          // link reached from its right child: no arrival, its leaf is in the window
+          b = box_union(S.leaf[slot], b);
+          box_store(aabb + static_cast<size_t>(node) * 6, b);
+          S.node[slot] = b;
+          h += 1;
+          prev = node;
+          node = parent;
+          continue;
+        }
+        __threadfence_block();  // this thread's shared box is visible before the arrival
+        const uint32_t old = atomicAdd(&S.flag[slot], h);
+        if (old == 0u) break;
+        __threadfence_block();
+        h = (old > h ? old : h) + 1;
+        if (c0 >= num_node || c1 >= num_node || (c0 != prev && c1 != prev)) {
+          raise_status(status, kStatusBadIndex);
+          break;
+        }
+        const bool mine_first = (c0 == prev);
+        const uint32_t sib = mine_first ? c1 : c0;
+        // a valid tree keeps the sibling inside the window; check it anyway
+        const uint32_t sslot = (sib >= T - 1) ? t0 + (sib - (T - 1)) - wA : t0 + sib - wA;
+        if (sslot >= static_cast<uint32_t>(kRefitWindow)) {
+          raise_status(status, kStatusBadIndex);
+          break;
+        }
+        const Box sb = (sib >= T - 1) ? S.leaf[sslot] : S.node[sslot];
+        b = mine_first ? box_union(b, sb) : box_union(sb, b);
+        box_store(aabb + static_cast<size_t>(node) * 6, b);
+        S.node[slot] = b;
+        prev = node;
+        node = parent;
       }
-      b = mine_first ? box_union(b, sb) : box_union(sb, b);
-      box_store(aabb + static_cast<size_t>(node) * 6, b);
-      if (local) S.node[t0 + node - wA] = b;
-      prev = node;
-      node = parent;
+      if (node == kUMax && height_out) height_out[lm[r].m] = h;
     }
-    if (node == kUMax && height_out) height_out[lm.m] = h;
+    __syncthreads();  // the next window reuses the shared arrays
   }
 }
+
+// The top of the tree: one thread per queue entry, global arrivals as in
+// k_refit, link chains folded kFoldDepth links per round trip.
+template <bool kBatch>
+__global__ void __launch_bounds__(128) k_refit_top(uint32_t total_tri, Segments seg,
+                                                   const uint32_t* __restrict__ bvhnodes_all, float* aabb_all,
+                                                   uint32_t* gflags_all, const uint32_t* queue, uint32_t capacity,
+                                                   uint32_t* height_out, uint32_t* status) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t count = __ldcg(queue);
+  if (e >= count || e >= capacity) return;
+  const uint4 q = __ldcg(reinterpret_cast<const uint4*>(queue + kRefitQueueHdr) + e);
+  const LeafMesh lm = leaf_mesh<kBatch>(seg, total_tri, 0u, q.w < total_tri ? q.w : 0u);
+  if (!lm.ok || q.w >= total_tri) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  const uint32_t T = lm.T, num_node = 2 * T - 1;
+  const size_t node_off = 2ull * lm.t0 - lm.m;
+  const uint32_t* bn = bvhnodes_all + 3 * node_off;
+  float* aabb = aabb_all + 6 * node_off;
+  uint32_t* gflags = gflags_all + (static_cast<size_t>(lm.t0) - lm.m);
+  uint32_t node = q.x, prev = q.y, h = q.z, guard = 0;
+  if (prev >= num_node) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  Box b = box_load_cg(aabb + static_cast<size_t>(prev) * 6);
+  while (node != kUMax) {
+    if (node >= T - 1 || ++guard > num_node) {
+      raise_status(status, kStatusBadIndex);
+      return;
+    }
+    const uint32_t parent = __ldg(bn + static_cast<size_t>(node) * 3);
+    const uint32_t c0 = __ldg(bn + static_cast<size_t>(node) * 3 + 1);
+    const uint32_t c1 = __ldg(bn + static_cast<size_t>(node) * 3 + 2);
+    if (c0 == T - 1 + node && c1 == node + 1 && prev == c1) {
+      // fold the chain from link j = node upward, kFoldDepth links per round
+      uint32_t j = node, pj = parent;
+      for (;;) {
+        Box lb[kFoldDepth];
+        uint32_t rp[kFoldDepth], rl[kFoldDepth], rr[kFoldDepth];  // records of j-1-d
+#pragma unroll
+        for (int d = 0; d < kFoldDepth; ++d) {
+          if (j >= static_cast<uint32_t>(d)) lb[d] = box_load_cg(aabb + static_cast<size_t>(T - 1 + j - d) * 6);
+          if (j >= static_cast<uint32_t>(d) + 1) {
+            const uint32_t* r = bn + static_cast<size_t>(j - 1 - d) * 3;
+            rp[d] = __ldg(r);
+            rl[d] = __ldg(r + 1);
+            rr[d] = __ldg(r + 2);
+          } else {
+            rp[d] = rl[d] = rr[d] = kUMax;
+          }
+        }
+        bool more = true;
+#pragma unroll
+        for (int d = 0; d < kFoldDepth; ++d) {
+          if (!more) continue;
+          const uint32_t jj = j - d;  // a link whose right child is complete
+          b = box_union(lb[d], b);
+          box_store(aabb + static_cast<size_t>(jj) * 6, b);
+          h += 1;
+          prev = jj;
+          if (++guard > num_node) {
+            raise_status(status, kStatusBadIndex);
+            return;
+          }
+          const uint32_t up = (d == 0) ? pj : rp[d - 1];  // parent of jj
+          node = up;
+          more = jj >= 1 && up == jj - 1 && rl[d] == T - 1 + up && rr[d] == jj;
+        }
+        if (!more) break;
+        j -= kFoldDepth;
+        pj = rp[kFoldDepth - 1];
+      }
+      continue;
+    }
+    cuda::atomic_ref<uint32_t, cuda::thread_scope_device> arrival(gflags[node]);
+    const uint32_t old = arrival.fetch_add(h, cuda::memory_order_acq_rel);
+    if (old == 0u) return;
+    gflags[node] = 0u;
+    h = (old > h ? old : h) + 1;
+    if (c0 >= num_node || c1 >= num_node || (c0 != prev && c1 != prev)) {
+      raise_status(status, kStatusBadIndex);
+      return;
+    }
+    const bool mine_first = (c0 == prev);
+    const Box sb = box_load_cg(aabb + static_cast<size_t>(mine_first ? c1 : c0) * 6);
+    b = mine_first ? box_union(b, sb) : box_union(sb, b);
+    box_store(aabb + static_cast<size_t>(node) * 6, b);
+    prev = node;
+    node = parent;
+  }
+  if (height_out) height_out[lm.m] = h;
+}
+
+// ------------------------------------------------------- range-query refit
+//
+// Without NaN, box_union(a, b) keeps a unless b is strictly smaller (lo) /
+// larger (hi), an associative operation whose fold over any tree is the
+// leftmost extreme of the leaves below.  So branch i's box equals the fold of
+// the leaf boxes over its leaf range [min(i, other_end[i]), max(...)], which a
+// segment tree over the sorted leaf boxes answers with no climb at all.
+// The tree is a perfect binary heap per 512-leaf window (nodes of 8..512
+// leaves kept), per 64-window superblock and over the superblocks; only nodes
+// lying wholly inside [0, total_tri) are ever built or read.  Identity boxes
+// are (+inf, -inf), which box_union returns unchanged bit for bit.
+struct SegView {
+  const float* wseg;  // [window][128] boxes, heap index 1..127
+  const float* sseg;  // [superblock][64] boxes, heap index 1..63
+  const float* tseg;  // [2 << top_log] boxes, heap index 1..
+  uint32_t top_log;
+};
+
+__device__ __forceinline__ const float* seg_node(const SegView& v, uint32_t lvl, uint32_t j) {
+  if (lvl <= kRefitWindowLog) {
+    const uint32_t sh = kRefitWindowLog - lvl;
+    return v.wseg + 6 * (static_cast<size_t>(j >> sh) * 128 + (1u << sh) + (j & ((1u << sh) - 1)));
+  }
+  if (lvl <= kRefitSuperLog) {
+    const uint32_t sh = kRefitSuperLog - lvl;
+    return v.sseg + 6 * (static_cast<size_t>(j >> sh) * 64 + (1u << sh) + (j & ((1u << sh) - 1)));
+  }
+  const uint32_t sh = kRefitSuperLog + v.top_log - lvl;
+  return v.tseg + 6 * ((static_cast<size_t>(1) << sh) + j);
+}
+
+__device__ __forceinline__ Box box_identity() {
+  return Box{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}};
+}
+
+__device__ __forceinline__ bool box_has_nan(const Box& b) {
+  bool n = false;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) n = n || (b.lo[d] != b.lo[d]) || (b.hi[d] != b.hi[d]);
+  return n;
+}
+
+// heap node h (1-based) of a heap whose leaves sit at level leaf_lvl: its
+// level and index within that level
+__device__ __forceinline__ void heap_node(uint32_t h, uint32_t top_lvl, uint32_t& lvl, uint32_t& j) {
+  const uint32_t lg = 31u - __clz(h);
+  lvl = top_lvl - lg;
+  j = h - (1u << lg);
+}
+
+__device__ __forceinline__ bool node_inside(uint64_t start_leaf, uint32_t lvl, uint32_t j, uint32_t total) {
+  return start_leaf + ((static_cast<uint64_t>(j) + 1) << lvl) <= total;
+}
+
+// Mesh of global leaf g, walking forward from a block-wide starting mesh.
+__device__ __forceinline__ uint32_t mesh_from(const Segments& seg, uint32_t m0, uint32_t g) {
+  uint32_t m = m0;
+  while (m + 1 < seg.num_mesh && __ldg(seg.tri_off + m + 1) <= g) ++m;
+  return m;
+}
+
+// Window kernel: leaf boxes, the window heap, and every branch whose range
+// lies inside the window.
+template <bool kBatch>
+__global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tri, Segments seg,
+                                                              uint32_t num_vtx_single,
+                                                              const uint32_t* __restrict__ bvhnodes_all,
+                                                              const uint32_t* __restrict__ other_all,
+                                                              const uint32_t* __restrict__ tri2vtx_all,
+                                                              const float* __restrict__ vtx0_all,
+                                                              const float* __restrict__ vtx1_all, float* aabb_all,
+                                                              uint32_t* hdr, uint32_t* cross_list, float* wseg,
+                                                              uint32_t* status) {
+  __shared__ Box tree[2 * kRefitWindow];
+  __shared__ uint32_t s_mesh, s_flag;
+  const uint32_t wA = blockIdx.x * kRefitWindow;
+  if (threadIdx.x == 0) {
+    // another block may raise the flag meanwhile: read it once for the block
+    s_flag = *reinterpret_cast<volatile uint32_t*>(hdr + 1);
+    if (kBatch) s_mesh = mesh_of_leaf(seg, wA);
+  }
+  __syncthreads();
+  if (s_flag != 0u) return;  // the climb does this call
+  LeafMesh lm[kWinPerThread];
+  uint32_t tri[kWinPerThread], oth[kWinPerThread];
+#pragma unroll
+  for (int r = 0; r < kWinPerThread; ++r) {
+    const uint32_t k = threadIdx.x + r * kWinThreads, g = wA + k;
+    lm[r] = LeafMesh{0, 0, total_tri, 0, num_vtx_single, g < total_tri};
+    if (kBatch && g < total_tri) {
+      const uint32_t m = mesh_from(seg, s_mesh, g);
+      lm[r].m = m;
+      lm[r].t0 = __ldg(seg.tri_off + m);
+      lm[r].T = __ldg(seg.tri_off + m + 1) - lm[r].t0;
+      lm[r].v0 = __ldg(seg.vtx_off + m);
+      lm[r].V = __ldg(seg.vtx_off + m + 1) - lm[r].v0;
+      lm[r].ok = !(g < lm[r].t0 || g - lm[r].t0 >= lm[r].T || lm[r].T > 0x7FFFFFFFu);
+    }
+    tri[r] = 0u;
+    oth[r] = kUMax;
+    if (!lm[r].ok) continue;
+    const uint32_t n = g - lm[r].t0;
+    tri[r] = __ldg(bvhnodes_all + 3 * (2ull * lm[r].t0 - lm[r].m + lm[r].T - 1 + n) + 1);
+    if (n + 1 < lm[r].T) oth[r] = __ldg(other_all + (static_cast<size_t>(lm[r].t0) - lm[r].m) + n);
+  }
+  bool nan = false;
+#pragma unroll
+  for (int r = 0; r < kWinPerThread; ++r) {
+    const uint32_t k = threadIdx.x + r * kWinThreads;
+    Box bx = box_identity();
+    if (lm[r].ok) {
+      if (tri[r] >= lm[r].T) {
+        raise_status(status, kStatusBadIndex);
+        tri[r] = 0u;
+      }
+      const uint32_t* t2v = tri2vtx_all + 3ull * lm[r].t0;
+      bx = leaf_box(t2v, lm[r].V, vtx0_all + 3ull * lm[r].v0, tri[r], status);
+      if (vtx1_all) bx = box_union(bx, leaf_box(t2v, lm[r].V, vtx1_all + 3ull * lm[r].v0, tri[r], status));
+      box_store(aabb_all + 6 * (2ull * lm[r].t0 - lm[r].m + lm[r].T - 1 + (wA + k - lm[r].t0)), bx);
+      nan = nan || box_has_nan(bx);
+    }
+    tree[kRefitWindow + k] = bx;
+  }
+  if (__syncthreads_or(nan)) {
+    if (threadIdx.x == 0) atomicOr(hdr + 1, 1u);  // hand the whole call to the climb
+    return;
+  }
+#pragma unroll 1
+  for (uint32_t half = kRefitWindow / 2; half >= 1; half >>= 1) {
+    for (uint32_t h = half + threadIdx.x; h < 2 * half; h += kWinThreads) tree[h] = box_union(tree[2 * h], tree[2 * h + 1]);
+    __syncthreads();
+  }
+  // heap nodes of 8..512 leaves for the crossing queries
+  if (threadIdx.x >= 1 && threadIdx.x < 128) {
+    uint32_t lvl, j;
+    heap_node(threadIdx.x, kRefitWindowLog, lvl, j);
+    if (node_inside(wA, lvl, j, total_tri)) box_store(wseg + 6 * (static_cast<size_t>(blockIdx.x) * 128 + threadIdx.x), tree[threadIdx.x]);
+  }
+#pragma unroll
+  for (int r = 0; r < kWinPerThread; ++r) {
+    if (oth[r] == kUMax) continue;
+    const uint32_t g = wA + threadIdx.x + r * kWinThreads, n = g - lm[r].t0;
+    const uint32_t lo = n < oth[r] ? n : oth[r], hi = n < oth[r] ? oth[r] : n;
+    if (hi >= lm[r].T) {
+      raise_status(status, kStatusBadIndex);
+      continue;
+    }
+    const uint32_t a = lm[r].t0 + lo, b = lm[r].t0 + hi;
+    if ((a >> kRefitWindowLog) != (b >> kRefitWindowLog)) {
+      // crossing: listed for k_refit_seg_cross in the (zero) arrival
+      // counters, which that kernel clears again as it reads them
+      const uint32_t slot = atomicAdd(hdr + 3, 1u);
+      if (slot < total_tri) cross_list[slot] = g + 1;  // + 1: a listed entry is never zero
+      else raise_status(status, kStatusBadIndex);      // more than total_tri - 1 branches: not a tree
+      continue;
+    }
+    uint32_t l = a - wA + kRefitWindow, rr = b - wA + kRefitWindow + 1;
+    Box L = box_identity(), R = box_identity();
+    while (l < rr) {
+      if (l & 1u) L = box_union(L, tree[l++]);
+      if (rr & 1u) R = box_union(tree[--rr], R);
+      l >>= 1;
+      rr >>= 1;
+    }
+    box_store(aabb_all + 6 * (2ull * lm[r].t0 - lm[r].m + n), box_union(L, R));
+  }
+}
+
+// Superblock heaps from the window totals; the last block builds the top heap.
+constexpr uint32_t kTopSmem = 256;
+__global__ void __launch_bounds__(256) k_refit_seg_super(uint32_t total_tri, uint32_t* hdr, const float* wseg,
+                                                         float* sseg, float* tseg, uint32_t top_log) {
+  __shared__ Box t[2 * kRefitSuper];
+  __shared__ Box ttop[2 * kTopSmem];  // the top heap, when it fits
+  __shared__ bool s_last;
+  if (*reinterpret_cast<volatile uint32_t*>(hdr + 1) != 0u) return;
+  const uint32_t sb = blockIdx.x;
+  const uint64_t sb_start = static_cast<uint64_t>(sb) << kRefitSuperLog;
+  if (threadIdx.x < kRefitSuper) {
+    const uint32_t w = sb * kRefitSuper + threadIdx.x;
+    t[kRefitSuper + threadIdx.x] = (static_cast<uint64_t>(w + 1) << kRefitWindowLog) <= total_tri
+                                       ? box_load_cg(wseg + 6 * (static_cast<size_t>(w) * 128 + 1))
+                                       : box_identity();
+  }
+  __syncthreads();
+#pragma unroll 1
+  for (uint32_t half = kRefitSuper / 2; half >= 1; half >>= 1) {
+    if (threadIdx.x < half) {
+      const uint32_t h = half + threadIdx.x;
+      t[h] = box_union(t[2 * h], t[2 * h + 1]);
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x >= 1 && threadIdx.x < kRefitSuper) {
+    uint32_t lvl, j;
+    heap_node(threadIdx.x, kRefitSuperLog, lvl, j);
+    if (node_inside(sb_start, lvl, j, total_tri)) box_store(sseg + 6 * (static_cast<size_t>(sb) * 64 + threadIdx.x), t[threadIdx.x]);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();  // release: the block's heap nodes (seen through the barrier) before the ticket
+    s_last = atomicAdd(hdr + 2, 1u) == gridDim.x - 1;
+    __threadfence();  // acquire: the other blocks' heap nodes
+  }
+  __syncthreads();
+  if (!s_last) return;
+  const uint32_t leaves = 1u << top_log, top_lvl = kRefitSuperLog + top_log;
+  if (leaves <= kTopSmem) {
+    for (uint32_t s = threadIdx.x; s < leaves; s += blockDim.x)
+      ttop[leaves + s] = (static_cast<uint64_t>(s + 1) << kRefitSuperLog) <= total_tri
+                             ? box_load_cg(sseg + 6 * (static_cast<size_t>(s) * 64 + 1))
+                             : box_identity();
+    __syncthreads();
+#pragma unroll 1
+    for (uint32_t half = leaves / 2; half >= 1; half >>= 1) {
+      for (uint32_t h = half + threadIdx.x; h < 2 * half; h += blockDim.x) ttop[h] = box_union(ttop[2 * h], ttop[2 * h + 1]);
+      __syncthreads();
+    }
+    for (uint32_t h = 1 + threadIdx.x; h < 2 * leaves; h += blockDim.x) {
+      uint32_t lvl, j;
+      heap_node(h, top_lvl, lvl, j);
+      if (node_inside(0, lvl, j, total_tri)) box_store(tseg + 6 * static_cast<size_t>(h), ttop[h]);
+    }
+    return;
+  }
+  for (uint32_t s = threadIdx.x; s < leaves; s += blockDim.x)
+    if ((static_cast<uint64_t>(s + 1) << kRefitSuperLog) <= total_tri)
+      box_store(tseg + 6 * (static_cast<size_t>(leaves) + s), box_load_cg(sseg + 6 * (static_cast<size_t>(s) * 64 + 1)));
+  __syncthreads();
+#pragma unroll 1
+  for (uint32_t half = leaves / 2; half >= 1; half >>= 1) {
+    for (uint32_t h = half + threadIdx.x; h < 2 * half; h += blockDim.x) {
+      uint32_t lvl, j;
+      heap_node(h, top_lvl, lvl, j);
+      if (node_inside(0, lvl, j, total_tri))
+        box_store(tseg + 6 * static_cast<size_t>(h),
+                  box_union(box_load_cg(tseg + 12 * static_cast<size_t>(h)), box_load_cg(tseg + 12 * static_cast<size_t>(h) + 6)));
+    }
+    __syncthreads();
+  }
+}
+
+// One crossing branch (global position g of its index): the segment-tree
+// query over its leaf range.
+template <bool kBatch>
+__device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, const Segments& seg,
+                                                const uint32_t* __restrict__ other_all, float* aabb_all,
+                                                const SegView& v, uint32_t* status) {
+  uint32_t m = 0, t0 = 0, T = total_tri;
+  if (kBatch) {
+    m = mesh_of_leaf(seg, g);
+    t0 = __ldg(seg.tri_off + m);
+    T = __ldg(seg.tri_off + m + 1) - t0;
+  }
+  const uint32_t n = g - t0;
+  if (g < t0 || n + 1 >= T) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  const uint32_t oth = __ldg(other_all + (static_cast<size_t>(t0) - m) + n);
+  const uint32_t lo = n < oth ? n : oth, hi = n < oth ? oth : n;
+  if (hi >= T) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  uint32_t l = t0 + lo, r = t0 + hi + 1;
+  const float* leaf0 = aabb_all + 6 * (2ull * t0 - m + T - 1) - 6ull * t0;  // + 6*p: leaf of global position p
+  const float* dummy = leaf0 + 6ull * l;
+  Box L = box_identity(), R = box_identity();
+  {  // ragged ends: up to 7 leaves on each side
+    const uint32_t nl = (8u - (l & 7u)) & 7u, nr = r & 7u;
+    Box bl[7], br[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+      bl[q] = box_load_cg(static_cast<uint32_t>(q) < nl ? leaf0 + 6ull * (l + q) : dummy);
+      br[q] = box_load_cg(static_cast<uint32_t>(q) < nr ? leaf0 + 6ull * (r - 1 - q) : dummy);
+    }
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+      if (static_cast<uint32_t>(q) < nl) L = box_union(L, bl[q]);
+      if (static_cast<uint32_t>(q) < nr) R = box_union(br[q], R);
+    }
+    l = (l + nl) >> 3;
+    r = (r - nr) >> 3;
+  }
+  uint32_t lvl = 3;
+  while (l < r) {
+    const float* pl[4];
+    const float* pr[4];
+    bool tl[4], tr[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      tl[q] = (l < r) && (l & 1u);
+      pl[q] = tl[q] ? seg_node(v, lvl, l) : dummy;
+      if (tl[q]) ++l;
+      tr[q] = (l < r) && (r & 1u);
+      if (tr[q]) --r;
+      pr[q] = tr[q] ? seg_node(v, lvl, r) : dummy;
+      l >>= 1;
+      r >>= 1;
+      ++lvl;
+    }
+    Box bl[4], br[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      bl[q] = box_load_cg(pl[q]);
+      br[q] = box_load_cg(pr[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (tl[q]) L = box_union(L, bl[q]);
+      if (tr[q]) R = box_union(br[q], R);
+    }
+  }
+  box_store(aabb_all + 6 * (2ull * t0 - m + n), box_union(L, R));
+}
+
+// Branches whose range crosses a window edge, from the list the window kernel
+// appended: a global segment-tree query, its loads issued four levels at a
+// time.  Every list entry read is cleared, also when the climb took over.
+template <bool kBatch>
+__global__ void __launch_bounds__(256) k_refit_seg_cross(uint32_t total_tri, Segments seg,
+                                                         const uint32_t* __restrict__ other_all, float* aabb_all,
+                                                         const uint32_t* hdr, uint32_t* cross_list, SegView v,
+                                                         uint32_t* status) {
+  const bool climb = *reinterpret_cast<const volatile uint32_t*>(hdr + 1) != 0u;
+  uint32_t count = *reinterpret_cast<const volatile uint32_t*>(hdr + 3);
+  if (count > total_tri) count = total_tri;
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+    const uint32_t entry = cross_list[e];
+    cross_list[e] = 0u;
+    if (climb) continue;
+    if (entry == 0u || entry > total_tri) {
+      raise_status(status, kStatusBadIndex);
+      continue;
+    }
+    refit_cross_one<kBatch>(entry - 1, total_tri, seg, other_all, aabb_all, v, status);
+  }
+}
+
 
 }  // namespace
 
@@ -608,28 +1057,56 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
                            uint32_t* height_out, uint32_t* status) {
   if (total_tri == 0) return;
   const int smem = static_cast<int>(sizeof(WinSmem));
-  const uint32_t grid = (total_tri + kWinLeaves - 1) / kWinLeaves;
-  const uint32_t leaf_grid = (total_tri + kThreads - 1) / kThreads;
+  const uint32_t windows = refit_num_windows(total_tri), supers = refit_num_super(total_tri);
+  const uint32_t top_log = refit_top_log(total_tri);
+  const uint32_t capacity = refit_queue_capacity(total_tri);
+  uint32_t* queue = flags + refit_queue_offset(total_tri);  // also the header: count, climb flag, ticket
+  float* segbase = reinterpret_cast<float*>(flags + refit_seg_offset(total_tri));
+  SegView v{segbase, segbase + 6 * size_t{128} * windows, segbase + 6 * (size_t{128} * windows + size_t{64} * supers),
+            top_log};
   // the attribute is per device; set it once so that later calls (possibly
   // under stream capture) make no further runtime configuration calls
   static bool configured[64] = {false};
+  static int sm_count[64] = {0};
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && !configured[dev]) {
     cudaFuncSetAttribute(k_refit_win<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_refit_win<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
     configured[dev] = true;
   }
+  const uint32_t sms = (dev >= 0 && dev < 64 && sm_count[dev] > 0) ? static_cast<uint32_t>(sm_count[dev]) : 152u;
+  cudaMemsetAsync(queue, 0, kRefitQueueHdr * sizeof(uint32_t), s);
+  if (height_out) cudaMemsetAsync(queue + 1, 1, sizeof(uint32_t), s);  // heights come from the climb
+  const uint32_t top_grid = (capacity + 127) / 128;
+  // persistent grids: the crossing list is short, and the climb usually exits at once
+  const uint32_t cross_grid = std::min<uint32_t>((total_tri + 255) / 256, sms * 2);
+  const uint32_t climb_grid = std::min<uint32_t>(windows, sms * 6);
+  float* wseg = const_cast<float*>(v.wseg);
+  float* sseg = const_cast<float*>(v.sseg);
+  float* tseg = const_cast<float*>(v.tseg);
   if (seg.tri_off) {
-    k_leaf_boxes<true><<<leaf_grid, kThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, tri2vtx, vtx2xyz0,
-                                                      vtx2xyz1, aabb, status);
-    k_refit_win<true><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, aabb, flags,
-                                                      height_out, status);
+    k_refit_seg_win<true><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
+                                                          vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg, status);
+    k_refit_seg_super<<<supers, 256, 0, s>>>(total_tri, queue, wseg, sseg, tseg, top_log);
+    k_refit_seg_cross<true><<<cross_grid, 256, 0, s>>>(total_tri, seg, other_end, aabb, queue, flags, v, status);
+    k_refit_win<true><<<climb_grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
+                                                         vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out,
+                                                         status);
+    k_refit_top<true><<<top_grid, 128, 0, s>>>(total_tri, seg, bvhnodes, aabb, flags, queue, capacity, height_out,
+                                               status);
   } else {
-    k_leaf_boxes<false><<<leaf_grid, kThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, tri2vtx, vtx2xyz0,
-                                                       vtx2xyz1, aabb, status);
-    k_refit_win<false><<<grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, aabb,
-                                                       flags, height_out, status);
+    k_refit_seg_win<false><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end,
+                                                           tri2vtx, vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg,
+                                                           status);
+    k_refit_seg_super<<<supers, 256, 0, s>>>(total_tri, queue, wseg, sseg, tseg, top_log);
+    k_refit_seg_cross<false><<<cross_grid, 256, 0, s>>>(total_tri, seg, other_end, aabb, queue, flags, v, status);
+    k_refit_win<false><<<climb_grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
+                                                          vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out,
+                                                          status);
+    k_refit_top<false><<<top_grid, 128, 0, s>>>(total_tri, seg, bvhnodes, aabb, flags, queue, capacity, height_out,
+                                                status);
   }
 }
 

@@ -131,7 +131,7 @@ BuildLayout build_layout(uint32_t T) {
   L.avals = L.akeys + align256(static_cast<size_t>(T) * 4);
   L.bvals = L.avals + align256(static_cast<size_t>(T) * 4);
   L.flags = L.bvals + align256(static_cast<size_t>(T) * 4);
-  L.total = L.flags + align256(static_cast<size_t>(T) * 4);
+  L.total = L.flags + align256(dm::refit_flags_words(T) * 4);
   return L;
 }
 
@@ -201,8 +201,9 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   uint32_t* other_end = other_end_out ? other_end_out : ak;  // the sort's A buffers are dead after pass 3
   dm::launch_topology(s, T, ok, ov, bvhnodes, other_end);
   if (ev) DM_CUDA(cudaEventRecord(ev[3], s));
+  // the height is only computed on request: it needs the tree-order climb
   dm::launch_refit_windowed(s, T, dm::Segments{1, nullptr, nullptr}, num_vtx, bvhnodes, other_end, tri2vtx, vtx2xyz,
-                            nullptr, aabb, flags, height, status);
+                            nullptr, aabb, flags, height_out ? height : nullptr, status);
   if (ev) DM_CUDA(cudaEventRecord(ev[4], s));
   if (transform_out) DM_CUDA(cudaMemcpyAsync(transform_out, transform, 64, cudaMemcpyDeviceToDevice, s));
   if (height_out) DM_CUDA(cudaMemcpyAsync(height_out, height, 4, cudaMemcpyDeviceToDevice, s));
@@ -231,7 +232,7 @@ BatchLayout batch_layout(uint32_t num_mesh, uint32_t total_tri) {
   L.vals_b = L.keys_b + align256(size_t{8} * total_tri);
   L.other = L.vals_b + align256(size_t{4} * total_tri);
   L.flags = L.other + align256(size_t{4} * total_tri);
-  L.total = L.flags + align256(size_t{4} * total_tri);
+  L.total = L.flags + align256(dm::refit_flags_words(total_tri) * 4);
   return L;
 }
 

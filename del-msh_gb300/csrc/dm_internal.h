@@ -64,8 +64,40 @@ struct Segments {
 };
 
 // Refit of trees built by launch_topology with other_end: the same boxes as
-// launch_refit, with most merges done in shared memory (see k_refit_win).
-// height_out (optional) receives one height per mesh.
+// launch_refit.  Without NaN in the leaf boxes, the first-wins merge of
+// from_two_aabbs makes every branch box the leftmost minimum / maximum over
+// its leaf range, so the boxes come from range queries on a segment tree of
+// the leaf boxes (k_refit_seg_*).  With NaN, or when heights are asked for,
+// the tree-order climb runs instead (k_refit_win + k_refit_top).
+// flags: u32[refit_flags_words(total_tri)]; its first total_tri words are
+// arrival counters, zero on entry and left zero; the rest (queue, segment
+// tree) needs no initialisation.  height_out (optional) receives one height
+// per mesh.
+constexpr uint32_t kRefitWindow = 512;      // leaves per window (a power of two)
+constexpr uint32_t kRefitWindowLog = 9;
+constexpr uint32_t kRefitSuper = 64;        // windows per superblock
+constexpr uint32_t kRefitSuperLog = 15;     // log2(kRefitWindow * kRefitSuper)
+constexpr uint32_t kRefitQueueHdr = 4;      // queue count, climb flag, ticket, spare
+inline uint32_t refit_num_windows(uint32_t total_tri) { return (total_tri + kRefitWindow - 1) / kRefitWindow; }
+inline uint32_t refit_num_super(uint32_t total_tri) {
+  return (refit_num_windows(total_tri) + kRefitSuper - 1) / kRefitSuper;
+}
+inline uint32_t refit_top_log(uint32_t total_tri) {
+  uint32_t lg = 0;
+  while ((1ull << lg) < refit_num_super(total_tri)) ++lg;
+  return lg;
+}
+inline uint32_t refit_queue_capacity(uint32_t total_tri) { return 2 * refit_num_windows(total_tri) + 2; }
+inline size_t refit_queue_offset(uint32_t total_tri) { return (static_cast<size_t>(total_tri) + 3) & ~size_t{3}; }
+inline size_t refit_seg_offset(uint32_t total_tri) {
+  return refit_queue_offset(total_tri) + kRefitQueueHdr + 4 * static_cast<size_t>(refit_queue_capacity(total_tri));
+}
+// window heaps (128 boxes each), superblock heaps (64 each), top heap (2 * 2^top_log)
+inline size_t refit_seg_words(uint32_t total_tri) {
+  return 6 * (size_t{128} * refit_num_windows(total_tri) + size_t{64} * refit_num_super(total_tri) +
+              (size_t{2} << refit_top_log(total_tri)));
+}
+inline size_t refit_flags_words(uint32_t total_tri) { return refit_seg_offset(total_tri) + refit_seg_words(total_tri); }
 void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
                            const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
                            const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,

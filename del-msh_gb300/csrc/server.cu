@@ -102,7 +102,7 @@ struct DevMesh {
 
 size_t mesh_bytes(uint32_t T, uint32_t V) {
   return a256(12ull * T) + 2 * a256(12ull * V) + a256(12ull * (2 * T - 1)) + a256(24ull * (2 * T - 1)) +
-         2 * a256(4ull * T);
+         a256(4ull * T) + a256(4 * refit_flags_words(T));
 }
 
 void carve(DevMesh& m, uint32_t T, uint32_t V) {

@@ -39,10 +39,12 @@ def make_bvhnodes_bvhnode2aabb(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor):
     return bvhnodes, bvhnode2aabb
 
 
-def make_bvhnodes_bvhnode2aabb_ex(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor):
+def make_bvhnodes_bvhnode2aabb_ex(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor, want_height: bool = True):
     """The same build, also returning its intermediate values: a dict with
     bvhnodes, bvhnode2aabb, transform (4x4 row-major float32), tri2morton,
-    idx2tri, idx2morton (uint32) and height (int)."""
+    idx2tri, idx2morton (uint32) and height (int, or None without
+    want_height).  Asking for the height makes the refit climb the tree in
+    tree order instead of answering range queries; the boxes are the same."""
     vtx2xyz = vtx2xyz.detach().contiguous()
     num_vtx, num_tri = vtx2xyz.shape[0], tri2vtx.shape[0]
     device = tri2vtx.device
@@ -55,12 +57,13 @@ def make_bvhnodes_bvhnode2aabb_ex(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor):
                tri2morton=torch.empty((num_tri,), dtype=torch.uint32, device=device),
                idx2tri=torch.empty((num_tri,), dtype=torch.uint32, device=device),
                idx2morton=torch.empty((num_tri,), dtype=torch.uint32, device=device),
-               height=torch.zeros((1,), dtype=torch.int32, device=device))
+               height=torch.zeros((1,), dtype=torch.int32, device=device) if want_height else None)
     _native.call("dm_trimesh3_build_ex", stream_ptr(device), num_tri, ptr(tri2vtx.contiguous()), num_vtx,
                  ptr(vtx2xyz), ptr(out["bvhnodes"]), ptr(out["bvhnode2aabb"]), ptr(out["transform"]),
-                 ptr(out["tri2morton"]), ptr(out["idx2tri"]), ptr(out["idx2morton"]), ptr(out["height"]), None, 0)
+                 ptr(out["tri2morton"]), ptr(out["idx2tri"]), ptr(out["idx2morton"]),
+                 ptr(out["height"]) if want_height else None, None, 0)
     out["transform"] = out["transform"].view(4, 4).T.contiguous()
-    out["height"] = int(out["height"].item())
+    out["height"] = int(out["height"].item()) if want_height else None
     return out
 
 

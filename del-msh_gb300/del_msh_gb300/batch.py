@@ -27,7 +27,7 @@ class MeshBatch:
     """Meshes (a list of (tri2vtx u32[T,3], vtx2xyz f32[V,3]) numpy arrays)
     concatenated on ``device`` with their trees, scratch and casting buffers."""
 
-    def __init__(self, meshes, device="cuda:0"):
+    def __init__(self, meshes, device="cuda:0", want_heights: bool = False):
         self.device = torch.device(device)
         self.num_mesh = len(meshes)
         assert self.num_mesh >= 1
@@ -49,7 +49,9 @@ class MeshBatch:
         num_node = 2 * self.total_tri - self.num_mesh
         self.bvhnodes = torch.empty((num_node, 3), dtype=torch.uint32, device=dev)
         self.bvhnode2aabb = torch.empty((num_node, 6), dtype=torch.float32, device=dev)
-        self.heights = torch.zeros((self.num_mesh,), dtype=torch.int32, device=dev)
+        # per-mesh tree heights, only on request: they come from the tree-order
+        # climb, which is slower than the range-query refit
+        self.heights = torch.zeros((self.num_mesh,), dtype=torch.int32, device=dev) if want_heights else None
         L = _native.load()
         self._build_bytes = L.dm_batch_build_scratch_bytes(self.num_mesh, self.total_tri)
         self._build_scratch = torch.empty((self._build_bytes,), dtype=torch.uint8, device=dev)
@@ -65,7 +67,8 @@ class MeshBatch:
         _native.call("dm_batch_trimesh3_build", self._stream(), self.num_mesh, self.d_tri_off.data_ptr(),
                      self.d_vtx_off.data_ptr(), self.total_tri, self.total_vtx, self.tri2vtx.data_ptr(),
                      self.vtx2xyz.data_ptr(), self.bvhnodes.data_ptr(), self.bvhnode2aabb.data_ptr(),
-                     self.heights.data_ptr(), self._build_scratch.data_ptr(), self._build_bytes)
+                     self.heights.data_ptr() if self.heights is not None else None, self._build_scratch.data_ptr(),
+                     self._build_bytes)
 
     def alloc_cast(self, img_w: int, img_h: int, want_t: bool = True):
         """Output images (num_mesh, img_h, img_w) and cast scratch for img_w x img_h per mesh."""

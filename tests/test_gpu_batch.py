@@ -20,11 +20,12 @@ def _meshes():
     return ms
 
 
-def test_batch_build_and_cast_match_single_and_oracle(cuda, oracle):
+@pytest.mark.parametrize("want_heights", [False, True])
+def test_batch_build_and_cast_match_single_and_oracle(cuda, oracle, want_heights):
     torch = cuda
     from del_msh_gb300.batch import MeshBatch, PlainPath, ortho_transforms
     meshes = _meshes()
-    b = MeshBatch(meshes)
+    b = MeshBatch(meshes, want_heights=want_heights)
     b.build()
     tf = torch.from_numpy(ortho_transforms(meshes)).to("cuda:0")
     b.alloc_cast(24, 20)
@@ -35,14 +36,16 @@ def test_batch_build_and_cast_match_single_and_oracle(cuda, oracle):
     q2t, qt = plain.cast_pixels(tf)
     torch.cuda.synchronize()
     p2t, tt, q2t, qt = to_np(p2t, torch), to_np(tt, torch), to_np(q2t, torch), to_np(qt, torch)
-    heights = to_np(b.heights, torch)
+    heights = to_np(b.heights, torch) if want_heights else None
     for m, (tri, vtx) in enumerate(meshes):
         bvh, aabb = b.mesh_tree(m)
         ref = oracle.build(tri, vtx)
         assert np.array_equal(to_np(bvh, torch), ref["bvhnodes"]), m
         assert np.array_equal(bits(to_np(aabb, torch)), bits(ref["bvhnode2aabb"])), m
         assert np.array_equal(to_np(plain.trees[m][0], torch), ref["bvhnodes"]), m
-        assert heights[m] == oracle.tree_height(ref["bvhnodes"], tri.shape[0]), m
+        assert np.array_equal(bits(to_np(plain.trees[m][1], torch)), bits(ref["bvhnode2aabb"])), m
+        if want_heights:
+            assert heights[m] == oracle.tree_height(ref["bvhnodes"], tri.shape[0]), m
         r_p2t, r_tt = oracle.pix2tri(tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"], ortho_transforms([meshes[m]])[0],
                                      24, 20)
         assert np.array_equal(p2t[m], r_p2t), m

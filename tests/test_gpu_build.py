@@ -84,9 +84,9 @@ def test_topology_single_object(cuda):
     assert to_np(got, torch).tolist() == [[0xFFFFFFFF, 5, 0xFFFFFFFF]]
 
 
-def _build_ex(torch, tri, vtx):
+def _build_ex(torch, tri, vtx, want_height=True):
     from del_msh_gb300.TriMesh3 import torch as TriMesh3
-    r = TriMesh3.make_bvhnodes_bvhnode2aabb_ex(to_dev(tri, torch), to_dev(vtx, torch))
+    r = TriMesh3.make_bvhnodes_bvhnode2aabb_ex(to_dev(tri, torch), to_dev(vtx, torch), want_height=want_height)
     out = {k: (to_np(v, torch) if hasattr(v, "device") else v) for k, v in r.items()}
     out["transform"] = np.ascontiguousarray(out["transform"].T).reshape(-1)  # back to column-major
     return out
@@ -105,8 +105,12 @@ def test_build_cfg1_matches_golden(cuda, golden_dir):
     assert _status_clear() == 0
 
 
-@pytest.mark.parametrize("case", ["torus", "soup", "ico", "tiny2", "tiny3", "same_tris", "flat"])
-def test_build_matches_oracle(cuda, oracle, case):
+@pytest.mark.parametrize("want_height", [True, False])
+@pytest.mark.parametrize("case", ["torus", "soup", "ico", "tiny2", "tiny3", "same_tris", "flat", "nan_vertex",
+                                  "big_window_span"])
+def test_build_matches_oracle(cuda, oracle, case, want_height):
+    """Both refits: the tree-order climb (asked for the height) and the range
+    queries (no height; NaN in a leaf box hands the call to the climb)."""
     torch = cuda
     if case == "torus":
         tri, vtx = W.displaced_torus(256, seed=3)
@@ -123,14 +127,22 @@ def test_build_matches_oracle(cuda, oracle, case):
     elif case == "same_tris":
         tri = np.tile(np.array([[0, 1, 2]], np.uint32), (5000, 1))
         vtx = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    elif case == "nan_vertex":
+        tri, vtx = W.displaced_torus(64, seed=6)
+        vtx = vtx.copy()
+        vtx[[5, 700, 2047]] = np.nan
+    elif case == "big_window_span":  # > 2^15 leaves: superblock and top heaps, ragged last window
+        tri, vtx = W.displaced_torus(190, seed=7)
+        tri = tri[:-37]
     else:  # all vertices on the plane z = 0
         rng = np.random.default_rng(8)
         vtx = np.concatenate([rng.random((3000, 2)), np.zeros((3000, 1))], 1).astype(np.float32)
         tri = rng.integers(0, 3000, (4000, 3)).astype(np.uint32)
     ref = oracle.build(tri, vtx)
-    got = _build_ex(torch, tri, vtx)
+    got = _build_ex(torch, tri, vtx, want_height)
     _compare_build(got, ref, tri.shape[0])
-    assert got["height"] == oracle.tree_height(ref["bvhnodes"], tri.shape[0])
+    if want_height:
+        assert got["height"] == oracle.tree_height(ref["bvhnodes"], tri.shape[0])
     assert _status_clear() == 0
 
 
