@@ -43,6 +43,11 @@ import numpy as np  # noqa: E402
 METRIC = "rays/s (LBVH build + cast per step)"
 UNIT = "rays/s"
 IMG_W, IMG_H = 1920, 1080
+# kernels of this repo launched per single-mesh step: build = centroid AABB,
+# Morton, 4 sort passes, topology, 5 refit kernels (window, superblock,
+# crossing, and the tree-order climb's two, which exit at once without NaN);
+# cast = persistent traversal + 2 overflow tiers (exit at once when empty)
+KERNELS_PER_STEP = 15
 NDIV = 1024
 SEED = 0
 L2_FLUSH_BYTES = 256 << 20
@@ -357,7 +362,7 @@ def run_ours(args):
         "e2e": {"value": world * R / (e2e_ms * 1e-3), "unit": UNIT,
                 "h2d_bytes_per_step": int(tri.nbytes + vtx.nbytes), "d2h_bytes_per_step": int(8 * R),
                 "ms_per_step": e2e_ms, "api": "TriMesh3.torch + Pix2Tri.torch", "matches_device_run": ok},
-        "gpu_launches": args.steps * 11,
+        "gpu_launches": args.steps * KERNELS_PER_STEP,
         "clocks": clocks,
         "device_status": status,
         "wall_s": wall,

@@ -155,10 +155,14 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
     return kStepDone;
   }
   bool ascend = false;
+  // At most one triangle test per step, issued from one place so that lanes
+  // testing a root / far leaf and lanes testing a near leaf share it.
+  uint32_t leaf_tri = kUMax;
+  bool leaf_near = false, has_far = false;
+  uint32_t nf = 0, f_l = 0, f_r = 0;
+  float far_enter = 0.f;
   if (s.right == kUMax) {  // a leaf reached as the root or as a far child
-    float t, u, v;
-    if (leaf_hit(m, r, s.left, t, u, v, bad)) s.best = pick(s.best, Hit{t, s.left});
-    ascend = true;
+    leaf_tri = s.left;
   } else {
     const uint32_t node = s.node, left = s.left, right = s.right;
     if (left >= num_node || right >= num_node) {
@@ -176,22 +180,15 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
     } else {
       const bool near_left = (hl && hr) ? tuple_lt(l0, l1, r0, r1) : hl;
       const uint32_t nn = near_left ? left : right;
-      const uint32_t nf = near_left ? right : left;
+      nf = near_left ? right : left;
       const uint32_t n_l = near_left ? ll : rl, n_r = near_left ? lr : rr;
-      const uint32_t f_l = near_left ? rl : ll, f_r = near_left ? rr : lr;
-      const bool has_far = hl && hr;
-      const float far_enter = near_left ? r0 : l0;
+      f_l = near_left ? rl : ll;
+      f_r = near_left ? rr : lr;
+      has_far = hl && hr;
+      far_enter = near_left ? r0 : l0;
       if (n_r == kUMax) {  // near child is a leaf holding triangle n_l
-        float t, u, v;
-        const bool h = leaf_hit(m, r, n_l, t, u, v, bad);
-        if (h) s.best = pick(s.best, Hit{t, n_l});
-        if (!has_far || (h && far_enter > t)) {
-          ascend = true;
-        } else {
-          s.node = nf;
-          s.left = f_l;
-          s.right = f_r;
-        }
+        leaf_tri = n_l;
+        leaf_near = true;
       } else if (!has_far) {
         s.node = nn;  // R(node) == R(near): no pending decision, no frame
         s.left = n_l;
@@ -215,6 +212,18 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
         s.left = n_l;
         s.right = n_r;
       }
+    }
+  }
+  if (leaf_tri != kUMax) {
+    float t, u, v;
+    const bool h = leaf_hit(m, r, leaf_tri, t, u, v, bad);
+    if (h) s.best = pick(s.best, Hit{t, leaf_tri});
+    if (!leaf_near || !has_far || (h && far_enter > t)) {
+      ascend = true;
+    } else {  // the far child of a near leaf
+      s.node = nf;
+      s.left = f_l;
+      s.right = f_r;
     }
   }
   if (!ascend) return kStepContinue;
@@ -287,7 +296,7 @@ constexpr int kCastThreads = 128;
 // Persistent warps with per-lane ray refill.  Rays overflowing the on-chip
 // stack go to ovf_list (their work index).
 template <typename Job>
-__global__ void __launch_bounds__(kCastThreads) k_cast_persistent(Job job, uint32_t* work_counter, uint32_t* ovf_list,
+__global__ void __launch_bounds__(kCastThreads, 8) k_cast_persistent(Job job, uint32_t* work_counter, uint32_t* ovf_list,
                                                                  uint32_t* ovf_count, uint32_t* status) {
   __shared__ float smem[64];
   job.prepare(smem);
