@@ -33,6 +33,20 @@ __device__ __forceinline__ uint32_t digit_of(KeyT k, uint32_t shift) {
   return static_cast<uint32_t>(k >> shift) & (kRadix - 1);
 }
 
+// Lanes of the warp holding the same 8-bit digit, among the valid lanes: one
+// ballot per digit bit.  Measured on GB300, this is several times faster than
+// __match_any_sync, which made ranking the longest phase of a pass.
+__device__ __forceinline__ uint32_t warp_peers(uint32_t d, bool valid) {
+  uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+  for (int b = 0; b < 8; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const uint32_t bb = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? bb : ~bb;
+  }
+  return peers;
+}
+
 // Exclusive scan of one value per thread over the 256-thread block.
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp /* kWarps */) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -90,20 +104,14 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
   const uint32_t tile_base = tile * kSortTile;
   const uint32_t wbase = tile_base + static_cast<uint32_t>(warp) * 32u * kKpt;
 
-  // Load (warp-striped: key j of this lane is at wbase + 32*j + lane).
+  // Load the keys (warp-striped: key j of this lane is at wbase + 32*j + lane);
+  // the values are loaded after ranking, to keep them out of its registers.
   KeyT keys[kKpt];
-  uint32_t vals[kKpt];
   uint32_t ranks[kKpt];
 #pragma unroll
   for (int j = 0; j < kKpt; ++j) {
     const uint32_t idx = wbase + 32u * j + lane;
-    if (idx < n) {
-      keys[j] = keys_in[idx];
-      vals[j] = kIota ? idx : vals_in[idx];
-    } else {
-      keys[j] = 0;
-      vals[j] = 0;
-    }
+    keys[j] = idx < n ? keys_in[idx] : KeyT{0};
   }
 
   // Rank inside the warp in (j, lane) order, i.e. input order.
@@ -113,13 +121,19 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
   for (int j = 0; j < kKpt; ++j) {
     const uint32_t idx = wbase + 32u * j + lane;
     const bool valid = idx < n;
-    const uint32_t d = valid ? digit_of(keys[j], shift) : static_cast<uint32_t>(kRadix);
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t d = digit_of(keys[j], shift);
+    const uint32_t peers = warp_peers(d, valid);
     const uint32_t before = valid ? my_hist[d] : 0u;
     __syncwarp();
     if (valid && lane == __ffs(peers) - 1) my_hist[d] = before + __popc(peers);
     __syncwarp();
     ranks[j] = before + __popc(peers & lt_mask);
+  }
+  uint32_t vals[kKpt];  // in flight while the counts are combined and scanned
+#pragma unroll
+  for (int j = 0; j < kKpt; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    vals[j] = kIota ? idx : (idx < n ? vals_in[idx] : 0u);
   }
   __syncthreads();
 
@@ -132,17 +146,37 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
     S.whist[w][d] = cnt;
     cnt += c;
   }
-
-  // Decoupled look-back for digit d.
+  // Publish this tile's count at once, so that successors looking back find it.
   volatile uint32_t* lb = lookback;
+  if (tile == 0) lb[d] = kFlagInc | cnt;
+  else lb[static_cast<size_t>(tile) * kRadix + d] = kFlagAgg | cnt;
+
+  // The tile-local layout needs no global information: scatter the tile into
+  // shared memory in (digit, input order) before looking back, so that the
+  // keys, values and ranks no longer hold registers during the look-back.
+  const uint32_t ts = block_exclusive_scan(cnt, S.scan);  // has __syncthreads
+  S.tstart[d] = ts;
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kKpt; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    if (idx < n) {
+      const uint32_t dg = digit_of(keys[j], shift);
+      const uint32_t pos = S.tstart[dg] + S.whist[warp][dg] + ranks[j];
+      S.keys[pos] = keys[j];
+      S.vals[pos] = vals[j];
+    }
+  }
+
+  // Decoupled look-back for digit d: walk back over the predecessors kWindow
+  // at a time (independent loads in flight together), consuming them in
+  // order until an inclusive prefix.  Every tile publishes its count right
+  // after ranking.  A window of 4 measured fastest on GB300 for 2M keys
+  // (105 us for four passes against 107 / 111 / 115 / 132 us with 8 / 12 /
+  // 16 / 32): the inclusive prefix is usually a few tiles back.
   uint32_t excl = 0;
-  if (tile == 0) {
-    lb[d] = kFlagInc | cnt;
-  } else {
-    lb[static_cast<size_t>(tile) * kRadix + d] = kFlagAgg | cnt;
-    // Walk back over the predecessors kWindow at a time (independent loads in
-    // flight together), consuming them in order until an inclusive prefix.
-    constexpr int kWindow = 8;
+  if (tile != 0) {
+    constexpr int kWindow = 4;
     int64_t k = static_cast<int64_t>(tile) - 1;
     uint32_t spins = 0;
     bool done = false;
@@ -177,21 +211,6 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
     lb[static_cast<size_t>(tile) * kRadix + d] = kFlagInc | ((excl + cnt) & kValueMask);
   }
   S.excl[d] = excl;
-  const uint32_t ts = block_exclusive_scan(cnt, S.scan);  // has __syncthreads
-  S.tstart[d] = ts;
-  __syncthreads();
-
-  // Scatter into shared memory in (digit, input order).
-#pragma unroll
-  for (int j = 0; j < kKpt; ++j) {
-    const uint32_t idx = wbase + 32u * j + lane;
-    if (idx < n) {
-      const uint32_t dg = digit_of(keys[j], shift);
-      const uint32_t pos = S.tstart[dg] + S.whist[warp][dg] + ranks[j];
-      S.keys[pos] = keys[j];
-      S.vals[pos] = vals[j];
-    }
-  }
   __syncthreads();
 
   // Write out: consecutive shared slots of one digit go to consecutive addresses.
