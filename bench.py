@@ -363,6 +363,7 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(tri.nbytes + vtx.nbytes), "d2h_bytes_per_step": int(8 * R),
                 "ms_per_step": e2e_ms, "api": "TriMesh3.torch + Pix2Tri.torch", "matches_device_run": ok},
         "gpu_launches": args.steps * KERNELS_PER_STEP,
+        "tuning": _native.get_tuning(),
         "clocks": clocks,
         "device_status": status,
         "wall_s": wall,

@@ -18,7 +18,7 @@
 //   k_batch_topology per branch of every mesh (binary search of its mesh)
 //   k_refit_win      windowed refit over the global leaf order
 // and of a batch cast: the persistent traversal of dm_traverse.cuh over the
-// 8x4 pixel tiles of every mesh's image, each lane loading its own mesh.
+// 32-pixel tiles (8x4 by default) of every mesh's image, each lane loading its own mesh.
 #include <cfloat>
 
 #include "dm_lbvh.cuh"
@@ -205,7 +205,6 @@ __global__ void __launch_bounds__(kThreads) k_batch_topology(uint32_t total_bran
 
 // ------------------------------------------------------------ batch cast
 
-constexpr uint32_t kTileW = 8, kTileH = 4;
 
 struct BatchJob {
   uint32_t num_work;
@@ -214,7 +213,7 @@ struct BatchJob {
   const float* vtx2xyz;
   const uint32_t* bvhnodes;
   const float* aabb;
-  uint32_t img_w, img_h, tiles_x, work_per_mesh;
+  uint32_t img_w, img_h, tiles_x, tile_w, tile_h, work_per_mesh;
   const float* transforms;  // num_mesh x 16, column-major ndc -> world
   CastOut o;
 
@@ -223,8 +222,8 @@ struct BatchJob {
   __device__ __forceinline__ bool fetch(uint32_t w, const float*, MeshView& mv, Ray& r, uint32_t& out) const {
     const uint32_t m = w / work_per_mesh, lw = w - m * work_per_mesh;
     const uint32_t tile = lw >> 5, j = lw & 31u;
-    const uint32_t px = (tile % tiles_x) * kTileW + (j % kTileW);
-    const uint32_t py = (tile / tiles_x) * kTileH + (j / kTileW);
+    const uint32_t px = (tile % tiles_x) * tile_w + (j % tile_w);
+    const uint32_t py = (tile / tiles_x) * tile_h + (j / tile_w);
     if (px >= img_w || py >= img_h) return false;
     const uint32_t t0 = __ldg(seg.tri_off + m), T = __ldg(seg.tri_off + m + 1) - t0;
     const uint32_t v0 = __ldg(seg.vtx_off + m), V = __ldg(seg.vtx_off + m + 1) - v0;
@@ -305,8 +304,11 @@ void launch_batch_cast_pixels(cudaStream_t s, const Segments& seg, uint32_t max_
   job.aabb = aabb;
   job.img_w = img_w;
   job.img_h = img_h;
-  job.tiles_x = (img_w + kTileW - 1) / kTileW;
-  job.work_per_mesh = job.tiles_x * ((img_h + kTileH - 1) / kTileH) * 32u;
+  const Tuning t = get_tuning();
+  job.tile_w = t.tile_w;
+  job.tile_h = 32u / t.tile_w;
+  job.tiles_x = (img_w + job.tile_w - 1) / job.tile_w;
+  job.work_per_mesh = job.tiles_x * ((img_h + job.tile_h - 1) / job.tile_h) * 32u;
   job.num_work = job.work_per_mesh * seg.num_mesh;
   job.transforms = transforms;
   job.o = o;

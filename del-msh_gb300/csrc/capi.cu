@@ -271,6 +271,27 @@ int build_keep_ranges(cudaStream_t s, uint32_t T, const uint32_t* tri2vtx, uint3
 
 size_t build_scratch_bytes(uint32_t T) { return build_layout(T).total; }
 
+namespace {
+std::mutex g_tuning_mutex;
+Tuning g_tuning;
+}  // namespace
+
+Tuning get_tuning() {
+  std::lock_guard<std::mutex> lk(g_tuning_mutex);
+  return g_tuning;
+}
+
+bool set_tuning(const Tuning& t) {
+  bool cast_ok = false;
+  for (const auto& v : kCastVariants) cast_ok = cast_ok || (v[0] == t.cast_threads && v[1] == t.cast_stack);
+  const bool tile_ok = t.tile_w == 2 || t.tile_w == 4 || t.tile_w == 8 || t.tile_w == 16 || t.tile_w == 32;
+  const bool sort_ok = t.sort_window == 4 || t.sort_window == 8;
+  if (!cast_ok || !tile_ok || !sort_ok) return false;
+  std::lock_guard<std::mutex> lk(g_tuning_mutex);
+  g_tuning = t;
+  return true;
+}
+
 }  // namespace dm
 
 extern "C" {
@@ -287,6 +308,25 @@ int dm_device_status(uint32_t* bits, int clear) {
   DM_CUDA(cudaMemcpy(&v, p, 4, cudaMemcpyDeviceToHost));
   if (clear) DM_CUDA(cudaMemset(p, 0, 4));
   if (bits) *bits = v;
+  return DM_OK;
+}
+
+int dm_tuning_get(dm_tuning* out) {
+  DM_REQUIRE(out, "NULL argument");
+  const dm::Tuning t = dm::get_tuning();
+  *out = dm_tuning{t.cast_threads, t.cast_stack, t.tile_w, t.sort_window, {0, 0, 0, 0}};
+  return DM_OK;
+}
+
+int dm_tuning_set(const dm_tuning* in) {
+  DM_REQUIRE(in, "NULL argument");
+  dm::Tuning t;
+  t.cast_threads = in->cast_threads;
+  t.cast_stack = in->cast_stack;
+  t.tile_w = in->tile_w;
+  t.sort_window = in->sort_window;
+  DM_REQUIRE(dm::set_tuning(t), "unsupported tuning (cast %u threads x %u frames, tile_w %u, sort window %u)",
+             in->cast_threads, in->cast_stack, in->tile_w, in->sort_window);
   return DM_OK;
 }
 

@@ -2,19 +2,18 @@
 // as pix2tri.rs:3-48 / pix2tri.cu:13-76) or an array of explicit rays
 // (search_bvh3.rs:103-221 per ray), with the traversal of dm_traverse.cuh.
 //
-// Pixels are handed out in 8x4 tiles (32 consecutive work indices = one tile)
-// so that the rays of a warp start close together and walk similar nodes.
+// Pixels are handed out in tiles of 32 (8x4 by default, a tuning choice; 32
+// consecutive work indices = one tile) so that the rays of a warp start close
+// together and walk similar nodes.
 #include "dm_traverse.cuh"
 
 namespace dm {
 namespace {
 
-constexpr uint32_t kTileW = 8, kTileH = 4;
-
 struct SingleJob {
   uint32_t num_work;
   MeshView m;
-  uint32_t img_w, img_h, tiles_x;  // pixel mode
+  uint32_t img_w, img_h, tiles_x, tile_w, tile_h;  // pixel mode
   const float* t_ndc2world;
   const float* ray_org;  // ray mode when non-null
   const float* ray_dir;
@@ -35,8 +34,8 @@ struct SingleJob {
       return true;
     }
     const uint32_t tile = w >> 5, j = w & 31u;
-    const uint32_t px = (tile % tiles_x) * kTileW + (j % kTileW);
-    const uint32_t py = (tile / tiles_x) * kTileH + (j / kTileW);
+    const uint32_t px = (tile % tiles_x) * tile_w + (j % tile_w);
+    const uint32_t py = (tile / tiles_x) * tile_h + (j / tile_w);
     if (px >= img_w || py >= img_h) return false;
     out = py * img_w + px;
     float3 o3, d3;
@@ -89,8 +88,11 @@ void launch_cast_pixels(cudaStream_t s, uint32_t img_w, uint32_t img_h, const fl
   job.m = m;
   job.img_w = img_w;
   job.img_h = img_h;
-  job.tiles_x = (img_w + kTileW - 1) / kTileW;
-  const uint32_t tiles_y = (img_h + kTileH - 1) / kTileH;
+  const Tuning t = get_tuning();
+  job.tile_w = t.tile_w;
+  job.tile_h = 32u / t.tile_w;
+  job.tiles_x = (img_w + job.tile_w - 1) / job.tile_w;
+  const uint32_t tiles_y = (img_h + job.tile_h - 1) / job.tile_h;
   job.num_work = job.tiles_x * tiles_y * 32u;
   job.t_ndc2world = t_ndc2world;
   job.o = o;

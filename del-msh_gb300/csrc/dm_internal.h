@@ -138,7 +138,21 @@ void launch_batch_topology(cudaStream_t s, uint32_t total_tri, const Segments& s
                            const uint32_t* vals, uint32_t* bvhnodes, uint32_t* other_end);
 
 // ----------------------------------------------------------------- cast.cu
-constexpr int kCastStack = 64;  // frames of the on-chip (local) traversal stack
+constexpr int kCastStack = 64;  // default frames of the on-chip (local) traversal stack
+
+// Launch parameters picked by the autotuner (del_msh_gb300/autotune.py) and
+// set through dm_tuning_set.  Every choice gives the same results; only the
+// speed differs.  Read at each launch.
+struct Tuning {
+  uint32_t cast_threads = 128;  // threads per block of the persistent cast
+  uint32_t cast_stack = 64;     // on-chip frames per ray
+  uint32_t tile_w = 8;          // pixel tile of one warp: tile_w x (32 / tile_w)
+  uint32_t sort_window = 4;     // predecessors read per look-back round of the sort
+};
+// (threads, stack) pairs compiled for the persistent cast
+constexpr uint32_t kCastVariants[][2] = {{128, 64}, {64, 64}, {256, 64}, {128, 32}, {128, 96}};
+Tuning get_tuning();
+bool set_tuning(const Tuning& t);  // false (and nothing changed) for an unsupported choice
 constexpr size_t kFrameBytes = 16;
 
 struct MeshView {

@@ -294,16 +294,20 @@ constexpr int kCastThreads = 128;
 //   __device__ void write(uint32_t out, const MeshView& m, const Ray& r, const Hit& h) const;
 
 // Persistent warps with per-lane ray refill.  Rays overflowing the on-chip
-// stack go to ovf_list (their work index).
-template <typename Job>
-__global__ void __launch_bounds__(kCastThreads, 8) k_cast_persistent(Job job, uint32_t* work_counter, uint32_t* ovf_list,
-                                                                 uint32_t* ovf_count, uint32_t* status) {
+// stack go to ovf_list (their work index).  kThreads threads per block and
+// kStack on-chip frames per ray are tuning choices (Tuning); the register
+// bound (64 registers) keeps 2048 resident threads per SM.
+template <typename Job, int kThreads, int kStack>
+__global__ void __launch_bounds__(kThreads, 65536 / (64 * kThreads)) k_cast_persistent(Job job, uint32_t* work_counter,
+                                                                                 uint32_t* ovf_list,
+                                                                                 uint32_t* ovf_count,
+                                                                                 uint32_t* status) {
   __shared__ float smem[64];
   job.prepare(smem);
   __syncthreads();
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
-  uint4 frames[kCastStack];
+  uint4 frames[kStack];
   LocalStack stack{frames};
   MeshView m{};
   Ray r{};
@@ -332,7 +336,7 @@ __global__ void __launch_bounds__(kCastThreads, 8) k_cast_persistent(Job job, ui
       continue;
     }
     if (active) {
-      const int rc = trav_step(m, r, stack, kCastStack, s, bad);
+      const int rc = trav_step(m, r, stack, kStack, s, bad);
       if (rc == kStepDone) {
         job.write(out, m, r, s.best);
         active = false;
@@ -397,8 +401,9 @@ __global__ void __launch_bounds__(kCastThreads) k_cast_deep(Job job, const uint3
   if (bad) raise_status(status, kStatusBadIndex);
 }
 
-// Number of resident blocks of the persistent kernel on the current device.
-template <typename Job>
+// Number of resident blocks of a persistent kernel instantiation on the
+// current device.
+template <typename Job, int kThreads, int kStack>
 inline int persistent_grid() {
   static int cached[64] = {0};
   int dev = 0;
@@ -407,22 +412,34 @@ inline int persistent_grid() {
   if (cached[dev] == 0) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cast_persistent<Job>, kCastThreads, 0);
-    cached[dev] = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 4);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cast_persistent<Job, kThreads, kStack>, kThreads, 0);
+    cached[dev] = (sms > 0 ? sms : 152) * (per_sm > 0 ? per_sm : 1);
   }
   return cached[dev];
 }
 
+template <typename Job, int kThreads, int kStack>
+inline void launch_persistent(cudaStream_t s, const Job& job, const CastScratch& sc, uint32_t* status) {
+  int grid = persistent_grid<Job, kThreads, kStack>();
+  const uint32_t needed = (job.num_work + kThreads - 1) / kThreads;
+  if (static_cast<uint32_t>(grid) > needed) grid = static_cast<int>(needed);
+  k_cast_persistent<Job, kThreads, kStack><<<grid, kThreads, 0, s>>>(job, sc.counters, sc.list1, sc.counters + 1,
+                                                                     status);
+}
+
 // The three-tier cast of every work index of `job`.  sc.counters (4 words)
 // must be zero on entry: [0] work counter, [1] tier-1 overflow count, [2]
-// tier-2 overflow count.
+// tier-2 overflow count.  The first tier's block size and on-chip stack
+// depth come from the current Tuning (kCastVariants lists the choices).
 template <typename Job>
 inline void cast_job(cudaStream_t s, const Job& job, const CastScratch& sc, uint32_t max_tri, uint32_t* status) {
   if (job.num_work == 0) return;
-  int grid = persistent_grid<Job>();
-  const uint32_t needed = (job.num_work + kCastThreads - 1) / kCastThreads;
-  if (static_cast<uint32_t>(grid) > needed) grid = static_cast<int>(needed);
-  k_cast_persistent<Job><<<grid, kCastThreads, 0, s>>>(job, sc.counters, sc.list1, sc.counters + 1, status);
+  const Tuning t = get_tuning();
+  if (t.cast_threads == 64 && t.cast_stack == 64) launch_persistent<Job, 64, 64>(s, job, sc, status);
+  else if (t.cast_threads == 256 && t.cast_stack == 64) launch_persistent<Job, 256, 64>(s, job, sc, status);
+  else if (t.cast_threads == 128 && t.cast_stack == 32) launch_persistent<Job, 128, 32>(s, job, sc, status);
+  else if (t.cast_threads == 128 && t.cast_stack == 96) launch_persistent<Job, 128, 96>(s, job, sc, status);
+  else launch_persistent<Job, 128, 64>(s, job, sc, status);
   const uint64_t pool_frames = sc.pool_bytes / kFrameBytes;
   uint4* pool = static_cast<uint4*>(sc.pool);
   const uint32_t deep_grid = 152 * 4;

@@ -86,7 +86,7 @@ struct SortSmem {
   uint32_t vals[kSortTile];
 };
 
-template <typename KeyT, bool kIota>
+template <typename KeyT, bool kIota, int kWindow>
 __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_onesweep(const KeyT* __restrict__ keys_in,
                                                       const uint32_t* __restrict__ vals_in, KeyT* __restrict__ keys_out,
                                                       uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift,
@@ -171,12 +171,12 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
   // Decoupled look-back for digit d: walk back over the predecessors kWindow
   // at a time (independent loads in flight together), consuming them in
   // order until an inclusive prefix.  Every tile publishes its count right
-  // after ranking.  A window of 4 measured fastest on GB300 for 2M keys
-  // (105 us for four passes against 107 / 111 / 115 / 132 us with 8 / 12 /
-  // 16 / 32): the inclusive prefix is usually a few tiles back.
+  // after ranking.  kWindow is a tuning choice (4 or 8); 4 measured fastest
+  // on GB300 for 2M keys (105 us for four passes against 107 / 111 / 115 /
+  // 132 us with 8 / 12 / 16 / 32): the inclusive prefix is usually a few
+  // tiles back.
   uint32_t excl = 0;
   if (tile != 0) {
-    constexpr int kWindow = 4;
     int64_t k = static_cast<int64_t>(tile) - 1;
     uint32_t spins = 0;
     bool done = false;
@@ -241,27 +241,39 @@ __global__ void __launch_bounds__(kThreads) k_digit_hist(uint32_t n, const KeyT*
     if (sh[i]) atomicAdd(hist + i, sh[i]);
 }
 
-template <typename KeyT>
-void onesweep(cudaStream_t s, uint32_t n, uint32_t shift, const KeyT* keys_in, const uint32_t* vals_in,
-              KeyT* keys_out, uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback, uint32_t* tile_counter,
-              uint32_t* status) {
-  if (n == 0) return;
+template <typename KeyT, int kWindow>
+void onesweep_w(cudaStream_t s, uint32_t n, uint32_t shift, const KeyT* keys_in, const uint32_t* vals_in,
+                KeyT* keys_out, uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback, uint32_t* tile_counter,
+                uint32_t* status) {
   const size_t smem = sizeof(SortSmem<KeyT>);
   static bool configured[64] = {false};  // the attribute is per device and function
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev >= 0 && dev < 64 && !configured[dev]) {
-    cudaFuncSetAttribute(k_onesweep<KeyT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-    cudaFuncSetAttribute(k_onesweep<KeyT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    cudaFuncSetAttribute(k_onesweep<KeyT, true, kWindow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
+    cudaFuncSetAttribute(k_onesweep<KeyT, false, kWindow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
     configured[dev] = true;
   }
   const uint32_t grid = sort_num_tiles(n);
   if (vals_in == nullptr)
-    k_onesweep<KeyT, true><<<grid, kThreads, smem, s>>>(keys_in, nullptr, keys_out, vals_out, n, shift, hist, lookback,
-                                                         tile_counter, status);
+    k_onesweep<KeyT, true, kWindow><<<grid, kThreads, smem, s>>>(keys_in, nullptr, keys_out, vals_out, n, shift, hist,
+                                                                 lookback, tile_counter, status);
   else
-    k_onesweep<KeyT, false><<<grid, kThreads, smem, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, hist,
-                                                          lookback, tile_counter, status);
+    k_onesweep<KeyT, false, kWindow><<<grid, kThreads, smem, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
+                                                                  hist, lookback, tile_counter, status);
+}
+
+template <typename KeyT>
+void onesweep(cudaStream_t s, uint32_t n, uint32_t shift, const KeyT* keys_in, const uint32_t* vals_in,
+              KeyT* keys_out, uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback, uint32_t* tile_counter,
+              uint32_t* status) {
+  if (n == 0) return;
+  if (get_tuning().sort_window == 8)
+    onesweep_w<KeyT, 8>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
+  else
+    onesweep_w<KeyT, 4>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
 }
 
 }  // namespace

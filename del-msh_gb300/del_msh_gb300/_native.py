@@ -19,6 +19,8 @@ _SIGNATURES = {
     "dm_version": (C.c_char_p, []),
     "dm_last_error": (C.c_char_p, []),
     "dm_device_status": (i32, [C.POINTER(C.c_uint32), i32]),
+    "dm_tuning_get": (i32, [vp]),
+    "dm_tuning_set": (i32, [vp]),
     "dm_mortons_vtx2morton_from_vtx2co": (i32, [u64, u32, u32, vp, vp, vp]),
     "dm_array1d_argsort": (i32, [u64, u32, vp, vp, vp, sz]),
     "dm_array1d_argsort_scratch_bytes": (sz, [u32]),
@@ -46,6 +48,26 @@ SERVER_FUNCS = ("dm_server_create", "dm_server_register_mesh", "dm_server_submit
 
 # entry points that return a status code
 STATUS_FUNCS = {k for k, (r, _) in _SIGNATURES.items() if r is i32 and k != "dm_device_status"}
+
+
+class Tuning(C.Structure):
+    """dm_tuning of include/delmsh_gb300.h."""
+    _fields_ = [("cast_threads", C.c_uint32), ("cast_stack", C.c_uint32), ("tile_w", C.c_uint32),
+                ("sort_window", C.c_uint32), ("reserved", C.c_uint32 * 4)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k in ("cast_threads", "cast_stack", "tile_w", "sort_window")}
+
+
+def get_tuning() -> dict:
+    t = Tuning()
+    call("dm_tuning_get", C.addressof(t))
+    return t.as_dict()
+
+
+def set_tuning(cast_threads: int, cast_stack: int, tile_w: int, sort_window: int) -> None:
+    t = Tuning(cast_threads, cast_stack, tile_w, sort_window)
+    call("dm_tuning_set", C.addressof(t))
 
 
 class DelMshError(RuntimeError):
@@ -79,7 +101,13 @@ def load(build_if_missing: bool = False):
             fn.restype = res
             fn.argtypes = args
         _lib = L
-        return L
+    # the autotuned launch parameters for this device model, if a table was made
+    try:
+        from . import autotune
+        autotune.apply()
+    except Exception:  # a malformed or foreign table leaves the defaults
+        pass
+    return L
 
 
 def exported_symbols():

@@ -1,0 +1,189 @@
+"""Autotuner for the launch parameters of ``dm_tuning`` (include/delmsh_gb300.h).
+
+The choices it sweeps are compiled into the library:
+
+- the persistent cast's block size and on-chip stack depth (frames per ray
+  before the overflow tiers), as (threads, frames) pairs;
+- the pixel tile of one warp (tile_w x 32/tile_w);
+- the radix sort's look-back window (predecessor tiles read per round).
+
+Every choice gives the same results, and the sweep checks that: each
+candidate's output must equal the default's bit for bit, or the candidate is
+rejected.  Timing uses CUDA events on the launching stream, with the L2
+flushed (a 256 MiB write) outside the timed region between repetitions.
+
+``tune()`` writes the fastest choice, with the whole sweep, to a JSON table;
+``apply()`` sets it when the table was measured on a device of the same name.
+``del_msh_gb300._native.load()`` calls ``apply()`` on the table shipped next to
+this file, if there is one.
+
+The radix width stays at 8 bits.  With 256 digits a 2M-key pass is one wave
+of 547 tiles, four 41 KB tiles per SM.  10-bit digits need 32 KB of per-warp
+digit counters (74 KB per tile, three tiles per SM) and 11-bit ones 64 KB (one
+or two per SM), so a pass would take two waves or more, which costs more than
+the one pass (of four) it saves over 30-bit codes.
+"""
+from __future__ import annotations
+
+import json
+import pathlib
+import statistics
+import time
+
+from . import _native
+
+DEFAULT_TABLE = pathlib.Path(__file__).resolve().parent / "tuning.json"
+CAST_CHOICES = [(128, 64), (64, 64), (256, 64), (128, 32), (128, 96)]
+TILE_CHOICES = [4, 8, 16, 32]
+SORT_WINDOWS = [4, 8]
+DEFAULT = dict(cast_threads=128, cast_stack=64, tile_w=8, sort_window=4)
+
+
+def _device_name(device) -> str | None:
+    try:
+        import torch
+        if not torch.cuda.is_available():
+            return None
+        return torch.cuda.get_device_name(torch.device(device))
+    except Exception:  # no torch / no driver: nothing to match against
+        return None
+
+
+def apply(path=DEFAULT_TABLE, device="cuda:0") -> dict | None:
+    """Sets the table's best choice if it was measured on this device model;
+    returns it (or None when nothing was applied)."""
+    p = pathlib.Path(path)
+    if not p.exists():
+        return None
+    table = json.loads(p.read_text())
+    name = _device_name(device)
+    if name is None or table.get("device") != name:
+        return None
+    best = table["best"]
+    _native.set_tuning(best["cast_threads"], best["cast_stack"], best["tile_w"], best["sort_window"])
+    return best
+
+
+def _events_ms(torch, stream, fn, flush, reps: int) -> float:
+    times = []
+    for _ in range(reps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return statistics.median(times)
+
+
+def tune(device="cuda:0", out=DEFAULT_TABLE, reps: int = 15, ndiv: int = 1024, img=(1920, 1080),
+         seed: int = 0) -> dict:
+    """Sweeps every compiled choice on the single-mesh workload (a displaced
+    torus on an ndiv x ndiv grid, a pinhole image of img pixels), writes the
+    table to `out` (unless None) and applies its best choice."""
+    import numpy as np
+    import torch
+
+    from . import workloads as W
+
+    dev = torch.device(device)
+    L = _native.load()
+    tri, vtx = W.displaced_torus(ndiv, seed=seed)
+    eye = W.random_viewpoint(3.0, seed=seed)
+    m = W.pinhole_ndc2world(eye, aspect=img[0] / img[1])  # column-major, as the C ABI reads it
+    T, V = tri.shape[0], vtx.shape[0]
+    d_tri = torch.from_numpy(tri.view(np.int32)).to(dev).view(torch.uint32)
+    d_vtx = torch.from_numpy(vtx).to(dev)
+    d_m = torch.from_numpy(m).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    flush = torch.empty((256 << 20,), dtype=torch.uint8, device=dev)
+    bvh = torch.empty((2 * T - 1, 3), dtype=torch.int32, device=dev)
+    aabb = torch.empty((2 * T - 1, 6), dtype=torch.float32, device=dev)
+    p2t = torch.empty((img[1], img[0]), dtype=torch.int32, device=dev)
+    tt = torch.empty((img[1], img[0]), dtype=torch.float32, device=dev)
+    bs, cs = L.dm_trimesh3_build_scratch_bytes(T), L.dm_cast_scratch_bytes(img[0] * img[1], T)
+    b_scr = torch.empty((bs,), dtype=torch.uint8, device=dev)
+    c_scr = torch.empty((cs,), dtype=torch.uint8, device=dev)
+
+    def build():
+        _native.call("dm_trimesh3_make_bvhnodes_bvhnode2aabb", sp, T, d_tri.data_ptr(), V, d_vtx.data_ptr(),
+                     bvh.data_ptr(), aabb.data_ptr(), b_scr.data_ptr(), bs)
+
+    def cast():
+        _native.call("dm_pix2tri_by_raycast", sp, img[0], img[1], p2t.data_ptr(), tt.data_ptr(), T,
+                     d_tri.data_ptr(), V, d_vtx.data_ptr(), bvh.data_ptr(), aabb.data_ptr(), d_m.data_ptr(),
+                     c_scr.data_ptr(), cs)
+
+    start = time.time()
+    _native.set_tuning(**DEFAULT)
+    build()
+    cast()
+    torch.cuda.synchronize(dev)
+    ref_tree = (bvh.clone(), aabb.clone())
+    ref_img = (p2t.clone(), tt.clone().view(torch.int32))
+
+    def same_tree():
+        return bool(torch.equal(bvh, ref_tree[0]) and torch.equal(aabb.view(torch.int32), ref_tree[1].view(torch.int32)))
+
+    def same_img():
+        return bool(torch.equal(p2t, ref_img[0]) and torch.equal(tt.view(torch.int32), ref_img[1]))
+
+    sweep = {"cast": [], "sort": []}
+    for threads, frames in CAST_CHOICES:
+        for tile_w in TILE_CHOICES:
+            _native.set_tuning(threads, frames, tile_w, DEFAULT["sort_window"])
+            for _ in range(3):
+                cast()
+            ms = _events_ms(torch, stream, cast, flush, reps)
+            sweep["cast"].append(dict(cast_threads=threads, cast_stack=frames, tile_w=tile_w, ms=ms,
+                                      identical=same_img()))
+    for window in SORT_WINDOWS:
+        _native.set_tuning(DEFAULT["cast_threads"], DEFAULT["cast_stack"], DEFAULT["tile_w"], window)
+        for _ in range(3):
+            build()
+        ms = _events_ms(torch, stream, build, flush, reps)
+        sweep["sort"].append(dict(sort_window=window, build_ms=ms, identical=same_tree()))
+    status = _native.device_status(clear=True)
+
+    ok_cast = [c for c in sweep["cast"] if c["identical"]]
+    ok_sort = [c for c in sweep["sort"] if c["identical"]]
+    bc = min(ok_cast, key=lambda c: c["ms"])
+    bsrt = min(ok_sort, key=lambda c: c["build_ms"])
+    best = dict(cast_threads=bc["cast_threads"], cast_stack=bc["cast_stack"], tile_w=bc["tile_w"],
+                sort_window=bsrt["sort_window"])
+    table = {
+        "device": torch.cuda.get_device_name(dev),
+        "sm_count": torch.cuda.get_device_properties(dev).multi_processor_count,
+        "torch": torch.__version__,
+        "cuda": torch.version.cuda,
+        "library": L.dm_version().decode(),
+        "workload": f"displaced torus {ndiv}x{ndiv} grid ({T} tris), {img[0]}x{img[1]} pinhole cast, seed {seed}",
+        "timing": f"median of {reps} CUDA-event timings per choice, L2 flushed between them",
+        "default": DEFAULT,
+        "best": best,
+        "speedup_cast_vs_default": next(c["ms"] for c in sweep["cast"]
+                                        if c["cast_threads"] == DEFAULT["cast_threads"]
+                                        and c["cast_stack"] == DEFAULT["cast_stack"]
+                                        and c["tile_w"] == DEFAULT["tile_w"]) / bc["ms"],
+        "rejected": [c for c in sweep["cast"] + sweep["sort"] if not c["identical"]],
+        "device_status": status,
+        "sweep": sweep,
+        "sweep_s": time.time() - start,
+    }
+    _native.set_tuning(**best)
+    if out is not None:
+        pathlib.Path(out).write_text(json.dumps(table, indent=1) + "\n")
+    return table
+
+
+if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--device", default="cuda:0")
+    ap.add_argument("--out", default=str(DEFAULT_TABLE))
+    ap.add_argument("--reps", type=int, default=15)
+    args = ap.parse_args()
+    t = tune(args.device, args.out, args.reps)
+    print(json.dumps({k: t[k] for k in ("device", "best", "speedup_cast_vs_default", "sweep_s")}))

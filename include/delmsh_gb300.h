@@ -60,6 +60,26 @@ const char* dm_last_error(void);
  * bvhnode2aabb.cu:21-48), which this library replaces by this word. */
 int dm_device_status(uint32_t* bits, int clear);
 
+/* Launch parameters chosen by the autotuner (del_msh_gb300/autotune.py).
+ * Every choice computes the same results; only speed differs.  They are read
+ * at each launch (a CUDA graph keeps those of its capture).  Process-wide.
+ * No reference counterpart: the reference hard-codes its launch shapes. */
+typedef struct dm_tuning {
+  uint32_t cast_threads; /* threads per block of the persistent cast: 64, 128 or 256 (with cast_stack 64),
+                            or 128 with cast_stack 32 / 96 */
+  uint32_t cast_stack;   /* on-chip traversal frames per ray before the overflow tiers */
+  uint32_t tile_w;       /* pixel tile of one warp is tile_w x (32 / tile_w): 2, 4, 8, 16 or 32 */
+  uint32_t sort_window;  /* predecessor tiles read per look-back round of the radix sort: 4 or 8 */
+  uint32_t reserved[4];  /* zero */
+} dm_tuning;
+
+/* The current launch parameters. */
+int dm_tuning_get(dm_tuning* out);
+
+/* Sets the launch parameters; DM_ERR_INVALID_ARGUMENT (nothing changed) for
+ * a combination that is not compiled. */
+int dm_tuning_set(const dm_tuning* in);
+
 /* Morton codes of points after a homogeneous transform (num_dim 2: 3x3, 3: 4x4
  * column-major), clamped to the unit cube as del-msh-cpu does.
  * Replaces: del-msh-dlpack/src/mortons.rs:18-77 mortons_vtx2morton_from_vtx2co

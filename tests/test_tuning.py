@@ -1,0 +1,95 @@
+"""Launch-parameter tuning: the host-side table (CPU) and result identity of
+every compiled choice against the oracle (GPU)."""
+import numpy as np
+import pytest
+
+from helpers import bits, to_dev, to_np
+
+from del_msh_gb300 import workloads as W
+
+
+def test_tuning_roundtrip_and_validation():
+    from del_msh_gb300 import _native
+    from del_msh_gb300.autotune import CAST_CHOICES, DEFAULT, SORT_WINDOWS, TILE_CHOICES
+    before = _native.get_tuning()
+    try:
+        for threads, frames in CAST_CHOICES:
+            for tile_w in TILE_CHOICES:
+                for window in SORT_WINDOWS:
+                    _native.set_tuning(threads, frames, tile_w, window)
+                    assert _native.get_tuning() == dict(cast_threads=threads, cast_stack=frames, tile_w=tile_w,
+                                                        sort_window=window)
+        _native.set_tuning(**DEFAULT)
+        for bad in [(96, 64, 8, 4), (128, 48, 8, 4), (128, 64, 3, 4), (128, 64, 64, 4), (128, 64, 8, 5)]:
+            with pytest.raises(_native.DelMshError):
+                _native.set_tuning(*bad)
+            assert _native.get_tuning() == DEFAULT  # a rejected choice changes nothing
+    finally:
+        _native.set_tuning(**before)
+
+
+def test_apply_ignores_foreign_table(tmp_path):
+    import json
+    from del_msh_gb300 import _native, autotune
+    before = _native.get_tuning()
+    p = tmp_path / "t.json"
+    p.write_text(json.dumps({"device": "not this GPU", "best": dict(cast_threads=64, cast_stack=64, tile_w=4,
+                                                                        sort_window=8)}))
+    assert autotune.apply(p) is None
+    assert _native.get_tuning() == before
+
+
+@pytest.mark.gpu
+def test_every_tuning_choice_matches_oracle(cuda, oracle):
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.autotune import CAST_CHOICES, SORT_WINDOWS, TILE_CHOICES
+    from del_msh_gb300.Pix2Tri import torch as Pix2Tri
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    tri, vtx = W.displaced_torus(96, seed=11)
+    ref = oracle.build(tri, vtx)
+    m = W.pinhole_ndc2world(W.random_viewpoint(3.0, seed=2), aspect=200 / 150)
+    r_p2t, r_tt = oracle.pix2tri(tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"], m, 200, 150)
+    d_tri, d_vtx = to_dev(tri, torch), to_dev(vtx, torch)
+    m_row = torch.from_numpy(np.ascontiguousarray(m.reshape(4, 4).T)).to("cuda:0")
+    before = _native.get_tuning()
+    try:
+        for window in SORT_WINDOWS:
+            _native.set_tuning(before["cast_threads"], before["cast_stack"], before["tile_w"], window)
+            bvh, aabb = TriMesh3.make_bvhnodes_bvhnode2aabb(d_tri, d_vtx)
+            assert np.array_equal(to_np(bvh, torch), ref["bvhnodes"]), window
+            assert np.array_equal(bits(to_np(aabb, torch)), bits(ref["bvhnode2aabb"])), window
+        for threads, frames in CAST_CHOICES:
+            for tile_w in TILE_CHOICES:
+                _native.set_tuning(threads, frames, tile_w, before["sort_window"])
+                p2t, tt = Pix2Tri.by_raycasting(d_tri, d_vtx, bvh, aabb, m_row, (200, 150), return_depth=True)
+                assert np.array_equal(to_np(p2t, torch), r_p2t), (threads, frames, tile_w)
+                assert np.array_equal(bits(to_np(tt, torch)), bits(r_tt)), (threads, frames, tile_w)
+    finally:
+        _native.set_tuning(**before)
+    assert _native.device_status(clear=True) == 0
+
+
+@pytest.mark.gpu
+def test_shallow_stack_overflows_to_deeper_tiers(cuda, oracle):
+    """The 32-frame on-chip stack on the duplicate-heavy soup: rays that need
+    more go through the overflow tiers and still give the oracle's hits."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.SearchBvh3 import torch as SearchBvh3
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    tri, vtx = W.clustered_soup(60_000, seed=9)
+    org, d = W.cube_boundary_rays(20_000, seed=9)
+    ref = oracle.build(tri, vtx)
+    r_hit, r_t = oracle.cast_rays(org, d, tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"])
+    before = _native.get_tuning()
+    try:
+        _native.set_tuning(128, 32, before["tile_w"], before["sort_window"])
+        d_tri, d_vtx = to_dev(tri, torch), to_dev(vtx, torch)
+        bvh, aabb = TriMesh3.make_bvhnodes_bvhnode2aabb(d_tri, d_vtx)
+        hit, t = SearchBvh3.first_intersection_ray(to_dev(org, torch), to_dev(d, torch), d_tri, d_vtx, bvh, aabb)
+        assert np.array_equal(to_np(hit, torch), r_hit)
+        assert np.array_equal(bits(to_np(t, torch)), bits(r_t))
+    finally:
+        _native.set_tuning(**before)
+    assert _native.device_status(clear=True) == 0
