@@ -176,6 +176,23 @@ def dist_env():
     return rank, world, local
 
 
+def reduce_max_over_ranks(pg, values, device=None):
+    """Each value's maximum over the ranks: the slowest replica sets the job's
+    time.  pg is torch.distributed (or None for one process)."""
+    if pg is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return [float(x) for x in t.tolist()]
+
+
+def job_throughput(world: int, units_per_rank: float, ms: float) -> float:
+    """Whole-job units/s of `world` replicas that each process units_per_rank
+    in ms (the max over ranks)."""
+    return world * units_per_rank / (ms * 1e-3)
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -330,10 +347,7 @@ def run_ours(args):
     e2e_ms = statistics.mean(a.elapsed_time(b) for a, b in e_ev)
     ok = bool(np.array_equal(h_p2t.numpy(), pix2tri.cpu().numpy()))
 
-    if pg is not None:
-        t = torch.tensor([step_ms, e2e_ms, build_mean, cast_mean], device=dev)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        step_ms, e2e_ms, build_mean, cast_mean = (float(x) for x in t.tolist())
+    step_ms, e2e_ms, build_mean, cast_mean = reduce_max_over_ranks(pg, [step_ms, e2e_ms, build_mean, cast_mean], dev)
     if rank != 0:
         if pg is not None:
             pg.destroy_process_group()
@@ -348,7 +362,7 @@ def run_ours(args):
     achieved = nbytes[dom] / (dom_ms * 1e-3) / 1e9
     build_gbs = nbytes["build"] / (build_mean * 1e-3) / 1e9
     line = {
-        "metric": METRIC, "value": world * R / (step_ms * 1e-3), "unit": UNIT, "n_gpus": world,
+        "metric": METRIC, "value": job_throughput(world, R, step_ms), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32/u32", "data": "synthetic (seeded displaced torus)",
         "config": config_dict(tri, vtx),
@@ -359,7 +373,7 @@ def run_ours(args):
                      "algorithmic_bytes": nbytes[dom]},
         "build_roofline": {"achieved": build_gbs, "peak": peak, "unit": "GB/s", "frac": build_gbs / peak,
                            "algorithmic_bytes": nbytes["build"]},
-        "e2e": {"value": world * R / (e2e_ms * 1e-3), "unit": UNIT,
+        "e2e": {"value": job_throughput(world, R, e2e_ms), "unit": UNIT,
                 "h2d_bytes_per_step": int(tri.nbytes + vtx.nbytes), "d2h_bytes_per_step": int(8 * R),
                 "ms_per_step": e2e_ms, "api": "TriMesh3.torch + Pix2Tri.torch", "matches_device_run": ok},
         "gpu_launches": args.steps * KERNELS_PER_STEP,

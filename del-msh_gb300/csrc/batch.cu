@@ -16,7 +16,8 @@
 //                    covering 30 + log2(num_mesh) bits); values = global
 //                    triangle index, so ties keep ascending triangle order
 //   k_batch_topology per branch of every mesh (binary search of its mesh)
-//   k_refit_win      windowed refit over the global leaf order
+//   refit            launch_refit_windowed over the global leaf order (segment-
+//                    tree range queries; the tree-order climb for NaN / heights)
 // and of a batch cast: the persistent traversal of dm_traverse.cuh over the
 // 32-pixel tiles (8x4 by default) of every mesh's image, each lane loading its own mesh.
 #include <cfloat>

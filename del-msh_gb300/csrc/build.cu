@@ -326,10 +326,13 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
   if (height_out) *height_out = h;
 }
 
-// Windowed refit, in two kernels.
+// Tree-order refit, in two kernels: the path taken when a leaf box holds NaN
+// (where the merge order matters) or when tree heights are asked for; the
+// range-query refit further below handles every other call, and these two
+// kernels then exit at once.
 //
-// k_refit_win gives block b the kRefitWindow sorted leaves starting at
-// b*kRefitWindow (global leaf order, across the meshes of a batch).  It
+// k_refit_win takes the windows of kRefitWindow sorted leaves (global leaf
+// order, across the meshes of a batch; each block loops over windows).  It
 // writes their leaf boxes and climbs from them through every branch whose
 // whole leaf range lies in the window ("local": known from other_end, since
 // a branch index is one end of its range).  Both arrivals at a local branch
