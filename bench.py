@@ -529,6 +529,89 @@ def run_served(args):
     return 0
 
 
+def run_render(args):
+    """The consumers of the config-2 pix2tri image (1920x1080 over the
+    2,097,152-triangle torus): depth and 3-channel interpolation, forward and
+    backward, each timed alone with CUDA events (L2 flushed between
+    repetitions), with the oracle on the host cores beside them."""
+    import torch
+    from del_msh_gb300 import _native
+    from del_msh_gb300.Pix2Depth import torch as Pix2Depth
+    from del_msh_gb300.Pix2Tri import torch as Pix2Tri
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    dev = torch.device("cuda", 0)
+    _native.load(build_if_missing=True)
+    tri, vtx, m = workload()
+    T, V, R = tri.shape[0], vtx.shape[0], IMG_W * IMG_H
+    d_tri = torch.from_numpy(tri.view(np.int32)).to(dev).view(torch.uint32)
+    d_vtx = torch.from_numpy(vtx).to(dev)
+    m_row = torch.from_numpy(np.ascontiguousarray(np.asarray(m).reshape(4, 4).T)).to(dev)
+    bvh, aabb = TriMesh3.make_bvhnodes_bvhnode2aabb(d_tri, d_vtx)
+    p2t = Pix2Tri.by_raycasting(d_tri, d_vtx, bvh, aabb, m_row, (IMG_W, IMG_H))
+    nd = 3
+    val = torch.rand((V, nd), device=dev)
+    depth = torch.zeros((IMG_H, IMG_W), device=dev)
+    g_depth = torch.rand((IMG_H, IMG_W), device=dev)
+    g_val = torch.rand((IMG_H, IMG_W, nd), device=dev)
+    gx = torch.zeros((V, 3), device=dev)
+    gv = torch.zeros((V, nd), device=dev)
+    flush = torch.empty((L2_FLUSH_BYTES,), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    ops = {
+        "depth_fwd": lambda: Pix2Depth.update(depth, p2t, d_tri, d_vtx, m_row),
+        "depth_bwd": lambda: Pix2Depth.bwd_wrt_vtx2xyz(gx, p2t, d_tri, d_vtx, g_depth, m_row),
+        "interp_fwd": lambda: Pix2Tri.interpolate_fwd(p2t, d_tri, d_vtx, val, m_row),
+        "interp_bwd": lambda: Pix2Tri.interpolate_bwd(p2t, d_tri, d_vtx, val, m_row, g_val, gx, gv),
+    }
+    hits = int((p2t != torch.iinfo(torch.uint32).max).sum().item())
+    # compulsory bytes per pixel: pix2tri 4 + (hit pixels) triangle 12 + 3 vertices 36 (+ values / grads)
+    per_hit = {"depth_fwd": 48, "depth_bwd": 48 + 36, "interp_fwd": 48 + 12 * nd,
+               "interp_bwd": 48 + 12 * nd + 36 + 12 * nd}
+    per_pix = {"depth_fwd": 4 + 4, "depth_bwd": 4 + 4, "interp_fwd": 4 + 4 * nd, "interp_bwd": 4 + 4 * nd}
+    peak, peak_kind = peaks()
+    res = {}
+    for name, fn in ops.items():
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        ms = statistics.median(times)
+        nbytes = per_pix[name] * R + per_hit[name] * hits
+        res[name] = {"ms": ms, "pixels_per_s": R / (ms * 1e-3), "algorithmic_bytes": nbytes,
+                     "hbm_frac": nbytes / (ms * 1e-3) / 1e9 / peak}
+    status = _native.device_status(clear=True)
+    line = {"metric": "pixels/s (depth / interpolation from a 1920x1080 pix2tri image, fwd and bwd)",
+            "unit": "pixels/s", "value": res["interp_fwd"]["pixels_per_s"], "steps": args.steps,
+            "config": {"workload": "config-2 torus (2,097,152 tris), 1920x1080 pinhole pix2tri, 3 value channels",
+                       "hit_pixels": hits, "l2": "flushed between repetitions"},
+            "ops": res, "peak": {"hbm_gbs": peak, "kind": peak_kind}, "device_status": status,
+            "note": "backward passes accumulate with atomicAdd, as the reference's kernels do"}
+    if not args.no_cpu:
+        from oracle import build as obuild
+        from oracle import oracle as O
+        obuild.build_oracle()
+        h_p2t = p2t.cpu().numpy()
+        hv, hg = val.cpu().numpy(), g_val.cpu().numpy()
+        t0 = time.perf_counter()
+        O.interpolate(h_p2t, tri, vtx, hv, np.asarray(m), IMG_W, IMG_H)
+        t_f = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        O.interpolate_bwd(h_p2t, tri, vtx, hv, np.asarray(m), hg, IMG_W, IMG_H)
+        t_b = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": R / t_f, "unit": "pixels/s", "cores": 1, "kind": "port",
+                                "sample": "one interpolation forward of the full image (1 thread)",
+                                "interp_bwd_pixels_per_s": R / t_b}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_soup(args):
     """Adversarial Morton distribution: 4,194,304-triangle soup whose centroids
     come from 32 Gaussian clusters (sigma 1e-3 in the unit cube), so many
@@ -640,7 +723,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--workload", choices=["single", "batched", "served", "soup"], default="single")
+    ap.add_argument("--workload", choices=["single", "batched", "served", "soup", "render"], default="single")
     ap.add_argument("--num-mesh", type=int, default=4096, help="meshes of the batched workload")
     ap.add_argument("--pool", type=int, default=512, help="meshes of the served pool")
     ap.add_argument("--requests", type=int, default=1000, help="requests per served trace")
@@ -657,6 +740,8 @@ def main():
         return run_served(args)
     if args.workload == "soup":
         return run_soup(args)
+    if args.workload == "render":
+        return run_render(args)
     return run_ours(args)
 
 

@@ -478,6 +478,76 @@ int dm_search_bvh3_first_intersection_ray(uint64_t stream_ptr, uint32_t num_ray,
   return DM_OK;
 }
 
+int dm_pix2depth_update(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, float* pix2depth,
+                        const uint32_t* pix2tri, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                        const float* vtx2xyz, const float* transform_ndc2world, void* scratch, size_t scratch_bytes) {
+  if (int e = check_mesh(num_tri, tri2vtx, num_vtx, vtx2xyz)) return e;
+  DM_REQUIRE(static_cast<uint64_t>(img_w) * img_h <= kMaxElems, "image of %u x %u pixels is too large", img_w, img_h);
+  DM_REQUIRE(pix2depth && pix2tri && transform_ndc2world, "NULL argument");
+  cudaStream_t s = as_stream(stream_ptr);
+  Scratch sc;
+  if (int e = sc.acquire(scratch, scratch_bytes, dm_render_scratch_bytes(), s, nullptr)) return e;
+  float* world2ndc = static_cast<float*>(sc.ptr);
+  dm::launch_inverse4(s, transform_ndc2world, world2ndc, status_ptr());
+  dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, nullptr, nullptr};
+  dm::launch_pix2depth(s, img_w, img_h, pix2depth, pix2tri, m, transform_ndc2world, world2ndc, status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+int dm_pix2depth_bwd_wrt_vtx2xyz(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, float* dldw_vtx2xyz,
+                                 const uint32_t* pix2tri, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                                 const float* vtx2xyz, const float* dldw_pix2depth, const float* transform_ndc2world,
+                                 void* scratch, size_t scratch_bytes) {
+  if (int e = check_mesh(num_tri, tri2vtx, num_vtx, vtx2xyz)) return e;
+  DM_REQUIRE(static_cast<uint64_t>(img_w) * img_h <= kMaxElems, "image of %u x %u pixels is too large", img_w, img_h);
+  DM_REQUIRE(dldw_vtx2xyz && pix2tri && dldw_pix2depth && transform_ndc2world, "NULL argument");
+  cudaStream_t s = as_stream(stream_ptr);
+  Scratch sc;
+  if (int e = sc.acquire(scratch, scratch_bytes, dm_render_scratch_bytes(), s, nullptr)) return e;
+  float* world2ndc = static_cast<float*>(sc.ptr);
+  dm::launch_inverse4(s, transform_ndc2world, world2ndc, status_ptr());
+  dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, nullptr, nullptr};
+  dm::launch_pix2depth_bwd(s, img_w, img_h, dldw_vtx2xyz, pix2tri, m, dldw_pix2depth, transform_ndc2world, world2ndc,
+                           status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+size_t dm_render_scratch_bytes(void) { return 256; }
+
+int dm_pix2tri_interpolate(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri,
+                           uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz,
+                           uint32_t num_vdim, const float* vtx2val, const float* transform_ndc2world, float* pix2val) {
+  if (int e = check_mesh(num_tri, tri2vtx, num_vtx, vtx2xyz)) return e;
+  DM_REQUIRE(static_cast<uint64_t>(img_w) * img_h * (num_vdim ? num_vdim : 1) <= (uint64_t{1} << 32) - 1,
+             "image of %u x %u x %u values is too large", img_w, img_h, num_vdim);
+  DM_REQUIRE(num_vdim >= 1, "num_vdim must be >= 1");
+  DM_REQUIRE(pix2tri && vtx2val && transform_ndc2world && pix2val, "NULL argument");
+  dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, nullptr, nullptr};
+  dm::launch_interpolate(as_stream(stream_ptr), img_w, img_h, pix2tri, m, num_vdim, vtx2val, transform_ndc2world,
+                         pix2val, status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+int dm_pix2tri_interpolate_bwd(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri,
+                               uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz,
+                               uint32_t num_vdim, const float* vtx2val, const float* transform_ndc2world,
+                               const float* dldw_pix2val, float* dldw_vtx2xyz, float* dldw_vtx2val) {
+  if (int e = check_mesh(num_tri, tri2vtx, num_vtx, vtx2xyz)) return e;
+  DM_REQUIRE(static_cast<uint64_t>(img_w) * img_h * (num_vdim ? num_vdim : 1) <= (uint64_t{1} << 32) - 1,
+             "image of %u x %u x %u values is too large", img_w, img_h, num_vdim);
+  DM_REQUIRE(num_vdim >= 1, "num_vdim must be >= 1");
+  DM_REQUIRE(pix2tri && vtx2val && transform_ndc2world && dldw_pix2val && dldw_vtx2xyz && dldw_vtx2val,
+             "NULL argument");
+  dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, nullptr, nullptr};
+  dm::launch_interpolate_bwd(as_stream(stream_ptr), img_w, img_h, pix2tri, m, num_vdim, vtx2val, transform_ndc2world,
+                             dldw_pix2val, dldw_vtx2xyz, dldw_vtx2val, status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
 size_t dm_batch_build_scratch_bytes(uint32_t num_mesh, uint32_t total_tri) {
   return batch_layout(num_mesh, total_tri).total;
 }

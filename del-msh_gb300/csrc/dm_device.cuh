@@ -18,6 +18,7 @@ enum DeviceStatusBits : uint32_t {
   kStatusSpinTimeout = 1u,  // a bounded wait in a kernel gave up
   kStatusStackOverflow = 2u,  // a traversal stack tier was too small
   kStatusBadIndex = 4u,  // an index read from an input array was out of range
+  kStatusSingular = 8u,  // a matrix to invert was singular (the result is NaN)
 };
 
 __device__ __forceinline__ void raise_status(uint32_t* status, uint32_t bits) {

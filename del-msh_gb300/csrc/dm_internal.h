@@ -194,4 +194,21 @@ void launch_batch_cast_pixels(cudaStream_t s, const Segments& seg, uint32_t max_
                               uint32_t img_h, const float* transforms, const CastOut& o, const CastScratch& sc,
                               uint32_t* status);
 
+// --------------------------------------------------------------- render.cu
+// Consumers of a pix2tri image (see render.cu): world2ndc = inverse(ndc2world)
+// on the device (one thread), depth and attribute interpolation, forward and
+// backward (the backward passes accumulate with atomicAdd).
+void launch_inverse4(cudaStream_t s, const float* m, float* inv, uint32_t* status);
+void launch_pix2depth(cudaStream_t s, uint32_t img_w, uint32_t img_h, float* pix2depth, const uint32_t* pix2tri,
+                      const MeshView& m, const float* ndc2world, const float* world2ndc, uint32_t* status);
+void launch_pix2depth_bwd(cudaStream_t s, uint32_t img_w, uint32_t img_h, float* dldw_vtx2xyz, const uint32_t* pix2tri,
+                          const MeshView& m, const float* dldw_pix2depth, const float* ndc2world,
+                          const float* world2ndc, uint32_t* status);
+void launch_interpolate(cudaStream_t s, uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri, const MeshView& m,
+                        uint32_t num_vdim, const float* vtx2val, const float* ndc2world, float* pix2val,
+                        uint32_t* status);
+void launch_interpolate_bwd(cudaStream_t s, uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri,
+                            const MeshView& m, uint32_t num_vdim, const float* vtx2val, const float* ndc2world,
+                            const float* dldw_pix2val, float* dldw_vtx2xyz, float* dldw_vtx2val, uint32_t* status);
+
 }  // namespace dm

@@ -20,6 +20,11 @@ _SIGNATURES = {
     "dm_last_error": (C.c_char_p, []),
     "dm_device_status": (i32, [C.POINTER(C.c_uint32), i32]),
     "dm_tuning_get": (i32, [vp]),
+    "dm_render_scratch_bytes": (sz, []),
+    "dm_pix2depth_update": (i32, [u64, u32, u32, vp, vp, u32, vp, u32, vp, vp, vp, sz]),
+    "dm_pix2depth_bwd_wrt_vtx2xyz": (i32, [u64, u32, u32, vp, vp, u32, vp, u32, vp, vp, vp, vp, sz]),
+    "dm_pix2tri_interpolate": (i32, [u64, u32, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp]),
+    "dm_pix2tri_interpolate_bwd": (i32, [u64, u32, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp, vp, vp]),
     "dm_tuning_set": (i32, [vp]),
     "dm_mortons_vtx2morton_from_vtx2co": (i32, [u64, u32, u32, vp, vp, vp]),
     "dm_array1d_argsort": (i32, [u64, u32, vp, vp, vp, sz]),

@@ -54,8 +54,9 @@ const char* dm_last_error(void);
 
 /* Reads the device status word of the current device (bits: 1 = a bounded
  * wait gave up, 2 = a traversal stack tier was too small, 4 = an index read
- * from an input array was out of range).  Synchronizes the device.  When
- * `clear` is non-zero the word is reset to 0.  No reference counterpart: the
+ * from an input array was out of range, 8 = a matrix to invert was singular).
+ * Synchronizes the device.  When `clear` is non-zero the word is reset to 0.
+ * No reference counterpart: the
  * reference's kernels use device asserts (mortons.cu:22-34,
  * bvhnode2aabb.cu:21-48), which this library replaces by this word. */
 int dm_device_status(uint32_t* bits, int clear);
@@ -188,6 +189,52 @@ int dm_search_bvh3_first_intersection_ray(uint64_t stream_ptr, uint32_t num_ray,
 
 /* Scratch size of dm_pix2tri_by_raycast / dm_search_bvh3_first_intersection_ray. */
 size_t dm_cast_scratch_bytes(uint32_t num_ray, uint32_t num_tri);
+
+/* ---- consumers of a pix2tri image: depth and attribute interpolation ----
+ * Pixel (iw, ih) uses the cast's ray (ray_for_pixel.h) and the ray/triangle
+ * intersection of its pix2tri entry; u32::MAX marks the background.  The
+ * backward entries ADD into their gradient arrays with atomics, so their
+ * sums may differ from a sequential sum by float reassociation. */
+
+/* Scratch size of dm_pix2depth_update / dm_pix2depth_bwd_wrt_vtx2xyz (the
+ * world->ndc matrix, inverted on the device). */
+size_t dm_render_scratch_bytes(void);
+
+/* Depth (ndc z + 1) / 2 of each pixel's hit point; 0 on the background.
+ * Replaces: del-msh-dlpack/src/pix2depth.rs:15-97 pix2depth_update (kernel
+ * del-msh-cuda-kernels/cuda/pix2depth.cu:12-50 fwd; CPU
+ * del-msh-cpu/src/pix2depth.rs:107-146).  The inverse of the transform is
+ * computed on the device (no host round trip); a singular transform raises
+ * status bit 8. */
+int dm_pix2depth_update(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, float* pix2depth,
+                        const uint32_t* pix2tri, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                        const float* vtx2xyz, const float* transform_ndc2world, void* scratch, size_t scratch_bytes);
+
+/* dldw_vtx2xyz += d(pix2depth)/d(vtx2xyz)^T dldw_pix2depth.
+ * Replaces: del-msh-dlpack/src/pix2depth.rs:100-189 pix2depth_bwd_wrt_vtx2xyz
+ * (kernel pix2depth.cu:52-97 bwd_wrt_vtx2xyz). */
+int dm_pix2depth_bwd_wrt_vtx2xyz(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, float* dldw_vtx2xyz,
+                                 const uint32_t* pix2tri, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                                 const float* vtx2xyz, const float* dldw_pix2depth, const float* transform_ndc2world,
+                                 void* scratch, size_t scratch_bytes);
+
+/* pix2val[p] = bc0 vtx2val[i0] + bc1 vtx2val[i1] + bc2 vtx2val[i2] with the
+ * barycentric coordinates of the pixel ray on its triangle; 0 on the
+ * background.  pix2val is f32[img_h][img_w][num_vdim].
+ * Replaces: del-msh-dlpack/src/pix2tri.rs:96-177 pix2tri_interpolate (kernel
+ * pix2tri.cu:79-120 interpolate; CPU del-msh-cpu/src/pix2tri.rs:176-226). */
+int dm_pix2tri_interpolate(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri,
+                           uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz,
+                           uint32_t num_vdim, const float* vtx2val, const float* transform_ndc2world, float* pix2val);
+
+/* Backward of dm_pix2tri_interpolate: adds to dldw_vtx2xyz (f32[V][3]) and
+ * dldw_vtx2val (f32[V][num_vdim]).
+ * Replaces: del-msh-dlpack/src/pix2tri.rs:179-270 pix2tri_interpolate_bwd
+ * (kernel pix2tri.cu:122-183 interpolate_bwd; CPU pix2tri.rs:228-304). */
+int dm_pix2tri_interpolate_bwd(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri,
+                               uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz,
+                               uint32_t num_vdim, const float* vtx2val, const float* transform_ndc2world,
+                               const float* dldw_pix2val, float* dldw_vtx2xyz, float* dldw_vtx2val);
 
 /* ---- batches: many independent meshes of uneven sizes in one call ----
  * The meshes are stored back to back.  mesh2tri / mesh2vtx are device

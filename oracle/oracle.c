@@ -742,3 +742,226 @@ uint32_t or_tree_height(const uint32_t* bvhnodes, uint32_t num_leaf) {
   free(stack);
   return best;
 }
+
+/* ------------------------------------------------------------------------
+ * Consumers of a pix2tri image: depth and attribute interpolation, forward
+ * and backward.  pix2depth.rs:107-146 / pix2depth.cu:12-97 and
+ * pix2tri.rs:176-304 / pix2tri.cu:79-183.  The formulas of the absent
+ * del-geo-core crate are restated (parity unpinned against it):
+ * Gauss-Jordan inverse with partial pivoting; Moller-Trumbore on the line
+ * through the pixel ray; the backward of (t, u, v) by implicit
+ * differentiation of o + t d = p0 + u e1 + v e2 with A = [-d | e1 | e2] and
+ * lambda = A^-T g: dL/dp0 = -(1-u-v) lambda, dL/dp1 = -u lambda,
+ * dL/dp2 = -v lambda; the Jacobian of the homogeneous transform
+ * (M_ij w - v_i M_3j) / w^2.  The backward passes add sequentially in pixel
+ * order, as the CPU reference does. */
+
+int or_mat4_inverse_pivot(const float m[16], float inv[16]) {
+  float a[4][8];
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) {
+      a[r][c] = m[c * 4 + r];
+      a[r][4 + c] = (r == c) ? 1.0f : 0.0f;
+    }
+  for (int col = 0; col < 4; ++col) {
+    int piv = col;
+    float best = fabsf(a[col][col]);
+    for (int r = col + 1; r < 4; ++r)
+      if (fabsf(a[r][col]) > best) {
+        best = fabsf(a[r][col]);
+        piv = r;
+      }
+    if (best == 0.0f) {
+      for (int k = 0; k < 16; ++k) inv[k] = NAN;
+      return 0;
+    }
+    if (piv != col)
+      for (int c = 0; c < 8; ++c) {
+        const float tmp = a[col][c];
+        a[col][c] = a[piv][c];
+        a[piv][c] = tmp;
+      }
+    const float d = a[col][col];
+    for (int c = 0; c < 8; ++c) a[col][c] = a[col][c] / d;
+    for (int r = 0; r < 4; ++r) {
+      if (r == col) continue;
+      const float f = a[r][col];
+      for (int c = 0; c < 8; ++c) a[r][c] = a[r][c] - f * a[col][c];
+    }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int c = 0; c < 4; ++c) inv[c * 4 + r] = a[r][4 + c];
+  return 1;
+}
+
+/* Moller-Trumbore without the inside / t >= 0 tests; 0 only for det == 0. */
+static int tri3_line(const float p0[3], const float p1[3], const float p2[3], const float org[3], const float dir[3],
+                     float* t, float* u, float* v) {
+  float e1[3], e2[3], tv[3], pv[3], qv[3];
+  for (int d = 0; d < 3; ++d) {
+    e1[d] = p1[d] - p0[d];
+    e2[d] = p2[d] - p0[d];
+    tv[d] = org[d] - p0[d];
+  }
+  cross3(pv, dir, e2);
+  const float det = dot3(e1, pv);
+  if (det == 0.0f) return 0;
+  const float inv_det = 1.0f / det;
+  *u = dot3(tv, pv) * inv_det;
+  cross3(qv, tv, e1);
+  *v = dot3(dir, qv) * inv_det;
+  *t = dot3(e2, qv) * inv_det;
+  return 1;
+}
+
+static void tri3_line_bwd(const float p0[3], const float p1[3], const float p2[3], const float dir[3], float u, float v,
+                          float gt, float gu, float gv, float d0[3], float d1[3], float d2[3]) {
+  float c0[3], c1[3], c2[3], x12[3], x20[3], x01[3];
+  for (int k = 0; k < 3; ++k) {
+    c0[k] = -dir[k];
+    c1[k] = p1[k] - p0[k];
+    c2[k] = p2[k] - p0[k];
+  }
+  cross3(x12, c1, c2);
+  cross3(x20, c2, c0);
+  cross3(x01, c0, c1);
+  const float det = dot3(c0, x12);
+  const float inv = 1.0f / det;
+  const float w0 = (1.0f - u) - v;
+  for (int k = 0; k < 3; ++k) {
+    const float lam = (gt * x12[k] + gu * x20[k] + gv * x01[k]) * inv;
+    d0[k] = lam * -w0;
+    d1[k] = lam * -u;
+    d2[k] = lam * -v;
+  }
+}
+
+static int tri_of_pixel(uint32_t it, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                        const float* vtx2xyz, uint32_t iv[3], const float* p[3]) {
+  if (it >= num_tri) return 0;
+  for (int k = 0; k < 3; ++k) {
+    iv[k] = tri2vtx[(size_t)it * 3 + k];
+    if (iv[k] >= num_vtx) return 0;
+    p[k] = vtx2xyz + (size_t)iv[k] * 3;
+  }
+  return 1;
+}
+
+int or_pix2depth(uint32_t img_w, uint32_t img_h, float* pix2depth, const uint32_t* pix2tri, uint32_t num_tri,
+                 const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz, const float ndc2world[16]) {
+  float w2n[16];
+  const int ok = or_mat4_inverse_pivot(ndc2world, w2n);
+  for (uint32_t i = 0; i < img_w * img_h; ++i) {
+    const uint32_t it = pix2tri[i];
+    if (it == OR_UMAX) {
+      pix2depth[i] = 0.0f;
+      continue;
+    }
+    uint32_t iv[3];
+    const float* p[3];
+    if (!tri_of_pixel(it, num_tri, tri2vtx, num_vtx, vtx2xyz, iv, p)) continue;
+    float o[3], d[3], t, bc[3];
+    or_ray_for_pixel(i, img_w, img_h, ndc2world, o, d);
+    if (!or_tri3_ray(p[0], p[1], p[2], o, d, &t, bc)) continue;
+    const float q[3] = {t * d[0] + o[0], t * d[1] + o[1], t * d[2] + o[2]};
+    float ndc[3];
+    or_transform_homogeneous(w2n, q, ndc);
+    pix2depth[i] = (ndc[2] + 1.0f) * 0.5f;
+  }
+  return ok;
+}
+
+int or_pix2depth_bwd(uint32_t img_w, uint32_t img_h, float* dldw_vtx2xyz, const uint32_t* pix2tri, uint32_t num_tri,
+                     const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz, const float* dldw_pix2depth,
+                     const float ndc2world[16]) {
+  float M[16];
+  const int ok = or_mat4_inverse_pivot(ndc2world, M);
+  for (uint32_t i = 0; i < img_w * img_h; ++i) {
+    const uint32_t it = pix2tri[i];
+    if (it == OR_UMAX) continue;
+    uint32_t iv[3];
+    const float* p[3];
+    if (!tri_of_pixel(it, num_tri, tri2vtx, num_vtx, vtx2xyz, iv, p)) continue;
+    float o[3], d[3], t, u, v;
+    or_ray_for_pixel(i, img_w, img_h, ndc2world, o, d);
+    if (!tri3_line(p[0], p[1], p[2], o, d, &t, &u, &v)) continue;
+    const float q[3] = {t * d[0] + o[0], t * d[1] + o[1], t * d[2] + o[2]};
+    float vv[4];
+    for (int r = 0; r < 4; ++r) vv[r] = M[r] * q[0] + M[4 + r] * q[1] + M[8 + r] * q[2] + M[12 + r];
+    const float w = vv[3], ww = w * w;
+    const float g_ndc[3] = {0.0f, 0.0f, 0.5f * dldw_pix2depth[i]};
+    float gq[3];
+    for (int j = 0; j < 3; ++j) {
+      float s = 0.0f;
+      for (int r = 0; r < 3; ++r) {
+        const float jij = (M[j * 4 + r] * w - vv[r] * M[j * 4 + 3]) / ww;
+        s = s + jij * g_ndc[r];
+      }
+      gq[j] = s;
+    }
+    const float gt = gq[0] * d[0] + gq[1] * d[1] + gq[2] * d[2];
+    float g[3][3];
+    tri3_line_bwd(p[0], p[1], p[2], d, u, v, gt, 0.0f, 0.0f, g[0], g[1], g[2]);
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) dldw_vtx2xyz[(size_t)iv[k] * 3 + c] += g[k][c];
+  }
+  return ok;
+}
+
+void or_interpolate(uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri, uint32_t num_tri, const uint32_t* tri2vtx,
+                    uint32_t num_vtx, const float* vtx2xyz, uint32_t num_vdim, const float* vtx2val,
+                    const float ndc2world[16], float* pix2val) {
+  for (uint32_t i = 0; i < img_w * img_h; ++i) {
+    float* out = pix2val + (size_t)i * num_vdim;
+    const uint32_t it = pix2tri[i];
+    uint32_t iv[3];
+    const float* p[3];
+    float t = 0.f, u = 0.f, v = 0.f;
+    int ok = it != OR_UMAX && tri_of_pixel(it, num_tri, tri2vtx, num_vtx, vtx2xyz, iv, p);
+    if (ok) {
+      float o[3], d[3];
+      or_ray_for_pixel(i, img_w, img_h, ndc2world, o, d);
+      ok = tri3_line(p[0], p[1], p[2], o, d, &t, &u, &v);
+    }
+    if (!ok) {
+      for (uint32_t k = 0; k < num_vdim; ++k) out[k] = 0.0f;
+      continue;
+    }
+    const float b0 = (1.0f - u) - v;
+    for (uint32_t k = 0; k < num_vdim; ++k)
+      out[k] = b0 * vtx2val[(size_t)iv[0] * num_vdim + k] + u * vtx2val[(size_t)iv[1] * num_vdim + k] +
+               v * vtx2val[(size_t)iv[2] * num_vdim + k];
+  }
+}
+
+void or_interpolate_bwd(uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri, uint32_t num_tri,
+                        const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz, uint32_t num_vdim,
+                        const float* vtx2val, const float ndc2world[16], const float* dldw_pix2val,
+                        float* dldw_vtx2xyz, float* dldw_vtx2val) {
+  for (uint32_t i = 0; i < img_w * img_h; ++i) {
+    const uint32_t it = pix2tri[i];
+    if (it == OR_UMAX) continue;
+    uint32_t iv[3];
+    const float* p[3];
+    if (!tri_of_pixel(it, num_tri, tri2vtx, num_vtx, vtx2xyz, iv, p)) continue;
+    const float* g = dldw_pix2val + (size_t)i * num_vdim;
+    float gb0 = 0.0f, gb1 = 0.0f, gb2 = 0.0f;
+    for (uint32_t k = 0; k < num_vdim; ++k) {
+      gb0 = gb0 + vtx2val[(size_t)iv[0] * num_vdim + k] * g[k];
+      gb1 = gb1 + vtx2val[(size_t)iv[1] * num_vdim + k] * g[k];
+      gb2 = gb2 + vtx2val[(size_t)iv[2] * num_vdim + k] * g[k];
+    }
+    gb1 = gb1 - gb0;
+    gb2 = gb2 - gb0;
+    float o[3], d[3], t, u, v;
+    or_ray_for_pixel(i, img_w, img_h, ndc2world, o, d);
+    if (!tri3_line(p[0], p[1], p[2], o, d, &t, &u, &v)) continue;
+    float dp[3][3];
+    tri3_line_bwd(p[0], p[1], p[2], d, u, v, 0.0f, gb1, gb2, dp[0], dp[1], dp[2]);
+    for (int c = 0; c < 3; ++c)
+      for (int k = 0; k < 3; ++k) dldw_vtx2xyz[(size_t)iv[k] * 3 + c] += dp[k][c];
+    const float b[3] = {(1.0f - u) - v, u, v};
+    for (uint32_t k = 0; k < num_vdim; ++k)
+      for (int j = 0; j < 3; ++j) dldw_vtx2val[(size_t)iv[j] * num_vdim + k] += g[k] * b[j];
+  }
+}

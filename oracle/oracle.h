@@ -121,6 +121,21 @@ int or_check_bvh_topology(const uint32_t* bvhnodes, uint32_t num_leaf);
 int or_check_morton_code_range_split(const uint32_t* idx2morton, uint32_t n);
 
 /* Height of the tree (number of nodes on the longest root-to-leaf path). */
+/* consumers of a pix2tri image (pix2depth.rs:107-146, pix2tri.rs:176-304) */
+int or_mat4_inverse_pivot(const float m[16], float inv[16]);
+int or_pix2depth(uint32_t img_w, uint32_t img_h, float* pix2depth, const uint32_t* pix2tri, uint32_t num_tri,
+                 const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz, const float ndc2world[16]);
+int or_pix2depth_bwd(uint32_t img_w, uint32_t img_h, float* dldw_vtx2xyz, const uint32_t* pix2tri, uint32_t num_tri,
+                     const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz, const float* dldw_pix2depth,
+                     const float ndc2world[16]);
+void or_interpolate(uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri, uint32_t num_tri, const uint32_t* tri2vtx,
+                    uint32_t num_vtx, const float* vtx2xyz, uint32_t num_vdim, const float* vtx2val,
+                    const float ndc2world[16], float* pix2val);
+void or_interpolate_bwd(uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri, uint32_t num_tri,
+                        const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz, uint32_t num_vdim,
+                        const float* vtx2val, const float ndc2world[16], const float* dldw_pix2val,
+                        float* dldw_vtx2xyz, float* dldw_vtx2val);
+
 uint32_t or_tree_height(const uint32_t* bvhnodes, uint32_t num_leaf);
 
 #ifdef __cplusplus

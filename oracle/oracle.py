@@ -57,6 +57,15 @@ def lib():
         L.or_check_morton_code_range_split.argtypes = [_u32p, u32]
         L.or_tree_height.restype = u32
         L.or_tree_height.argtypes = [_u32p, u32]
+        L.or_mat4_inverse_pivot.restype = i32
+        L.or_mat4_inverse_pivot.argtypes = [_f32p, _f32p]
+        L.or_pix2depth.restype = i32
+        L.or_pix2depth.argtypes = [u32, u32, _f32p, _u32p, u32, _u32p, u32, _f32p, _f32p]
+        L.or_pix2depth_bwd.restype = i32
+        L.or_pix2depth_bwd.argtypes = [u32, u32, _f32p, _u32p, u32, _u32p, u32, _f32p, _f32p, _f32p]
+        L.or_interpolate.argtypes = [u32, u32, _u32p, u32, _u32p, u32, _f32p, u32, _f32p, _f32p, _f32p]
+        L.or_interpolate_bwd.argtypes = [u32, u32, _u32p, u32, _u32p, u32, _f32p, u32, _f32p, _f32p, _f32p, _f32p,
+                                         _f32p]
         _lib = L
     return _lib
 
@@ -229,6 +238,55 @@ def check_morton_code_range_split(idx2morton):
 
 def tree_height(bvhnodes, num_leaf):
     return int(lib().or_tree_height(_c(bvhnodes, np.uint32).reshape(-1), num_leaf))
+
+
+# ------------------------------------- consumers of a pix2tri image
+
+def mat4_inverse_pivot(m_colmajor):
+    inv = np.empty(16, np.float32)
+    ok = lib().or_mat4_inverse_pivot(_c(m_colmajor, np.float32).reshape(-1), inv)
+    return inv, bool(ok)
+
+
+def pix2depth(pix2tri, tri2vtx, vtx2xyz, t_ndc2world_colmajor, img_w, img_h, init=None):
+    """pix2depth.rs:107-146 restated; pixels whose ray misses their triangle
+    keep `init` (zeros by default)."""
+    out = np.zeros(img_w * img_h, np.float32) if init is None else _c(init, np.float32).reshape(-1).copy()
+    tri2vtx, vtx2xyz = _c(tri2vtx, np.uint32), _c(vtx2xyz, np.float32)
+    lib().or_pix2depth(img_w, img_h, out, _c(pix2tri, np.uint32).reshape(-1), tri2vtx.size // 3, tri2vtx.reshape(-1),
+                       vtx2xyz.size // 3, vtx2xyz.reshape(-1), _c(t_ndc2world_colmajor, np.float32).reshape(-1))
+    return out.reshape(img_h, img_w)
+
+
+def pix2depth_bwd(pix2tri, tri2vtx, vtx2xyz, dldw_pix2depth, t_ndc2world_colmajor, img_w, img_h, init=None):
+    tri2vtx, vtx2xyz = _c(tri2vtx, np.uint32), _c(vtx2xyz, np.float32)
+    g = np.zeros(vtx2xyz.size, np.float32) if init is None else _c(init, np.float32).reshape(-1).copy()
+    lib().or_pix2depth_bwd(img_w, img_h, g, _c(pix2tri, np.uint32).reshape(-1), tri2vtx.size // 3,
+                           tri2vtx.reshape(-1), vtx2xyz.size // 3, vtx2xyz.reshape(-1),
+                           _c(dldw_pix2depth, np.float32).reshape(-1), _c(t_ndc2world_colmajor, np.float32).reshape(-1))
+    return g.reshape(-1, 3)
+
+
+def interpolate(pix2tri, tri2vtx, vtx2xyz, vtx2val, t_ndc2world_colmajor, img_w, img_h):
+    tri2vtx, vtx2xyz, vtx2val = _c(tri2vtx, np.uint32), _c(vtx2xyz, np.float32), _c(vtx2val, np.float32)
+    nd = vtx2val.shape[1]
+    out = np.empty(img_w * img_h * nd, np.float32)
+    lib().or_interpolate(img_w, img_h, _c(pix2tri, np.uint32).reshape(-1), tri2vtx.size // 3, tri2vtx.reshape(-1),
+                         vtx2xyz.size // 3, vtx2xyz.reshape(-1), nd, vtx2val.reshape(-1),
+                         _c(t_ndc2world_colmajor, np.float32).reshape(-1), out)
+    return out.reshape(img_h, img_w, nd)
+
+
+def interpolate_bwd(pix2tri, tri2vtx, vtx2xyz, vtx2val, t_ndc2world_colmajor, dldw_pix2val, img_w, img_h):
+    tri2vtx, vtx2xyz, vtx2val = _c(tri2vtx, np.uint32), _c(vtx2xyz, np.float32), _c(vtx2val, np.float32)
+    nd = vtx2val.shape[1]
+    gx = np.zeros(vtx2xyz.size, np.float32)
+    gv = np.zeros(vtx2val.size, np.float32)
+    lib().or_interpolate_bwd(img_w, img_h, _c(pix2tri, np.uint32).reshape(-1), tri2vtx.size // 3, tri2vtx.reshape(-1),
+                             vtx2xyz.size // 3, vtx2xyz.reshape(-1), nd, vtx2val.reshape(-1),
+                             _c(t_ndc2world_colmajor, np.float32).reshape(-1),
+                             _c(dldw_pix2val, np.float32).reshape(-1), gx, gv)
+    return gx.reshape(-1, 3), gv.reshape(-1, nd)
 
 
 # ---------------------------------------------------------- reference code
