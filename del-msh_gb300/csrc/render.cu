@@ -88,40 +88,58 @@ __device__ __forceinline__ bool tri_vertices(const uint32_t* __restrict__ tri2vt
 // column raises kStatusSingular and leaves NaN.
 __global__ void k_inverse4(const float* __restrict__ m, float* inv, uint32_t* status) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  // fully unrolled so that the 4x8 array stays in registers; the row swap
+  // selects instead of indexing with the pivot row
   float a[4][8];
+#pragma unroll
   for (int r = 0; r < 4; ++r)
+#pragma unroll
     for (int c = 0; c < 4; ++c) {
       a[r][c] = m[c * 4 + r];
       a[r][4 + c] = (r == c) ? 1.0f : 0.0f;
     }
+  bool singular = false;
+#pragma unroll
   for (int col = 0; col < 4; ++col) {
     int piv = col;
     float best = fabsf(a[col][col]);
+#pragma unroll
     for (int r = col + 1; r < 4; ++r)
       if (fabsf(a[r][col]) > best) {
         best = fabsf(a[r][col]);
         piv = r;
       }
-    if (best == 0.0f) {
-      raise_status(status, kStatusSingular);
-      for (int k = 0; k < 16; ++k) inv[k] = NAN;
-      return;
-    }
-    if (piv != col)
+    singular = singular || (best == 0.0f);
+#pragma unroll
+    for (int r = col + 1; r < 4; ++r) {
+      const bool sw = (r == piv);
+#pragma unroll
       for (int c = 0; c < 8; ++c) {
-        const float tmp = a[col][c];
-        a[col][c] = a[piv][c];
-        a[piv][c] = tmp;
+        const float x = a[col][c], y = a[r][c];
+        a[col][c] = sw ? y : x;
+        a[r][c] = sw ? x : y;
       }
+    }
     const float d = a[col][col];
+#pragma unroll
     for (int c = 0; c < 8; ++c) a[col][c] = __fdiv_rn(a[col][c], d);
+#pragma unroll
     for (int r = 0; r < 4; ++r) {
       if (r == col) continue;
       const float f = a[r][col];
+#pragma unroll
       for (int c = 0; c < 8; ++c) a[r][c] = __fsub_rn(a[r][c], __fmul_rn(f, a[col][c]));
     }
   }
+  if (singular) {
+    raise_status(status, kStatusSingular);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) inv[k] = NAN;
+    return;
+  }
+#pragma unroll
   for (int r = 0; r < 4; ++r)
+#pragma unroll
     for (int c = 0; c < 4; ++c) inv[c * 4 + r] = a[r][4 + c];
 }
 

@@ -14,6 +14,12 @@ from .. import _native
 from ..util_torch import assert_shape_dtype_device, ptr, require_cuda, stream_ptr
 
 
+def _scratch(device) -> torch.Tensor:
+    """Room for the device-side world->ndc matrix, from torch's caching
+    allocator (256-byte aligned)."""
+    return torch.empty((_native.load().dm_render_scratch_bytes(),), dtype=torch.uint8, device=device)
+
+
 def update(pix2depth: torch.Tensor, pix2tri: torch.Tensor, tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor,
            transform_ndc2world: torch.Tensor):
     """Writes the depth of every pixel into pix2depth (img_h, img_w) float32."""
@@ -27,9 +33,10 @@ def update(pix2depth: torch.Tensor, pix2tri: torch.Tensor, tri2vtx: torch.Tensor
     assert_shape_dtype_device(transform_ndc2world, (4, 4), torch.float32, device)
     require_cuda(device)
     colmajor = transform_ndc2world.T.contiguous()
+    scratch = _scratch(device)
     _native.call("dm_pix2depth_update", stream_ptr(device), img_w, img_h, ptr(pix2depth), ptr(pix2tri.contiguous()),
                  num_tri, ptr(tri2vtx.contiguous()), num_vtx, ptr(vtx2xyz.detach().contiguous()), ptr(colmajor),
-                 None, 0)
+                 ptr(scratch), scratch.numel())
 
 
 def bwd_wrt_vtx2xyz(dldw_vtx2xyz: torch.Tensor, pix2tri: torch.Tensor, tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor,
@@ -46,9 +53,11 @@ def bwd_wrt_vtx2xyz(dldw_vtx2xyz: torch.Tensor, pix2tri: torch.Tensor, tri2vtx: 
     assert_shape_dtype_device(transform_ndc2world, (4, 4), torch.float32, device)
     require_cuda(device)
     colmajor = transform_ndc2world.T.contiguous()
+    scratch = _scratch(device)
     _native.call("dm_pix2depth_bwd_wrt_vtx2xyz", stream_ptr(device), img_w, img_h, ptr(dldw_vtx2xyz),
                  ptr(pix2tri.contiguous()), num_tri, ptr(tri2vtx.contiguous()), num_vtx,
-                 ptr(vtx2xyz.detach().contiguous()), ptr(dldw_pix2depth.contiguous()), ptr(colmajor), None, 0)
+                 ptr(vtx2xyz.detach().contiguous()), ptr(dldw_pix2depth.contiguous()), ptr(colmajor), ptr(scratch),
+                 scratch.numel())
 
 
 class AutogradFunction(torch.autograd.Function):
