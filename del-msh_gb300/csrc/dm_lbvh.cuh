@@ -59,23 +59,22 @@ __device__ __forceinline__ void topology_node(uint32_t n, const Codes& c, const 
       r1 = run_end(c, n, ib + 1, mc1);
     } else {
       const int dd = __clz(mc1 ^ mc2) - __clz(mc1 ^ mc0);
-      const int d = dd > 0 ? 1 : -1;
-      const int delta_min = __clz(mc1 ^ (d > 0 ? mc0 : mc2));
-      int64_t lmax = 2;
-      for (;;) {
-        const int64_t j = static_cast<int64_t>(ib) + lmax * d;
-        if (j < 0 || j >= static_cast<int64_t>(n)) break;
-        if (__clz(mc1 ^ c(static_cast<uint32_t>(j))) <= delta_min) break;
-        lmax *= 2;
+      const bool up = dd > 0;  // direction d = +1 (else -1)
+      const int delta_min = __clz(mc1 ^ (up ? mc0 : mc2));
+      // 32-bit steps: lim is the largest step that stays inside [0, n) in
+      // direction d (n < 2^30, so lmax <= 2 (lim + 1) fits), and a step s
+      // lands on ib + s or ib - s
+      const uint32_t lim = up ? n - 1 - ib : ib;
+      uint32_t lmax = 2;
+      while (lmax <= lim && __clz(mc1 ^ c(up ? ib + lmax : ib - lmax)) > delta_min) lmax *= 2;
+      uint32_t l = 0;
+      for (uint32_t t = lmax / 2; t >= 1; t /= 2) {
+        const uint32_t s = l + t;
+        if (s <= lim && __clz(mc1 ^ c(up ? ib + s : ib - s)) > delta_min) l = s;
       }
-      int64_t l = 0;
-      for (int64_t t = lmax / 2; t >= 1; t /= 2) {
-        const int64_t j = static_cast<int64_t>(ib) + (l + t) * d;
-        if (j >= 0 && j < static_cast<int64_t>(n) && __clz(mc1 ^ c(static_cast<uint32_t>(j))) > delta_min) l += t;
-      }
-      const uint32_t j = static_cast<uint32_t>(static_cast<int64_t>(ib) + l * d);
-      r0 = ib <= j ? ib : j;
-      r1 = ib <= j ? j : ib;
+      const uint32_t j = up ? ib + l : ib - l;
+      r0 = up ? ib : j;
+      r1 = up ? j : ib;
     }
   }
   uint32_t isplit = r0;
