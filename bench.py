@@ -612,6 +612,76 @@ def run_render(args):
     return 0
 
 
+def run_octree(args):
+    """Quad/oct-tree construction from 2,097,152 sorted unique 30-bit Morton
+    codes (3-D, uniform random points): binary radix tree + depth +
+    octree-node map, then the octree; each phase timed with CUDA events (L2
+    flushed between repetitions), the oracle on one host thread beside it."""
+    import torch
+    from del_msh_gb300 import _native
+    from del_msh_gb300.QuadOctTree import torch as QOT
+    from oracle import build as obuild
+    from oracle import oracle as O
+    dev = torch.device("cuda", 0)
+    _native.load(build_if_missing=True)
+    obuild.build_oracle()
+    rng = np.random.default_rng(SEED)
+    pts = rng.random((2_300_000, 3)).astype(np.float32)
+    codes = np.unique(O.vtx2morton(pts, np.eye(4, dtype=np.float32).reshape(-1)))[:2_097_152]
+    n = codes.size
+    d = torch.from_numpy(codes.view(np.int32)).to(dev).view(torch.uint32)
+    flush = torch.empty((L2_FLUSH_BYTES,), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    bn, b2d, b2o, i2b = QOT.bnodes_and_bnode2depth_and_bnode2onode_and_idx2bnode(d, 3)
+    num_onode = int(b2o[-1].item()) + 1
+    L = _native.load()
+    sp = stream.cuda_stream
+    scr = torch.empty((L.dm_quad_oct_tree_scratch_bytes(n),), dtype=torch.uint8, device=dev)
+    on = torch.full((num_onode, 9), 2 ** 32 - 1, device=dev, dtype=torch.uint32)
+    o2d = torch.zeros((num_onode,), device=dev, dtype=torch.uint32)
+    o2c = torch.empty((num_onode, 3), device=dev)
+    i2o = torch.empty((n,), device=dev, dtype=torch.uint32)
+    i2c = torch.empty((n, 3), device=dev)
+
+    def phase1():
+        _native.call("dm_quad_oct_tree_bnodes_and_bnode2depth_and_bnode2onode_and_idx2bnode", sp, n, d.data_ptr(), 3,
+                     10, bn.data_ptr(), b2d.data_ptr(), b2o.data_ptr(), i2b.data_ptr(), scr.data_ptr(), scr.numel())
+
+    def phase2():
+        _native.call("dm_quad_oct_tree_make_tree_from_binary_radix_tree", sp, n, bn.data_ptr(), b2o.data_ptr(),
+                     b2d.data_ptr(), i2b.data_ptr(), d.data_ptr(), 3, 10, num_onode, on.data_ptr(), o2d.data_ptr(),
+                     o2c.data_ptr(), i2o.data_ptr(), i2c.data_ptr())
+
+    res = {}
+    for name, fn in (("binary_tree_and_map", phase1), ("octree", phase2)):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        times = []
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        res[name] = {"ms": statistics.median(times)}
+    total = res["binary_tree_and_map"]["ms"] + res["octree"]["ms"]
+    line = {"metric": "points/s (quad/oct-tree from sorted unique Morton codes)", "unit": "points/s",
+            "value": n / (total * 1e-3), "steps": args.steps,
+            "config": {"workload": f"{n} unique 30-bit codes of uniform random 3-D points", "num_onode": num_onode,
+                       "l2": "flushed between repetitions"},
+            "phases": res, "device_status": _native.device_status(clear=True)}
+    if not args.no_cpu:
+        t0 = time.perf_counter()
+        O.quad_oct_tree(codes, 3)
+        t_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": n / t_cpu, "unit": "points/s", "cores": 1, "kind": "port",
+                                "sample": "one full construction (1 thread)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_soup(args):
     """Adversarial Morton distribution: 4,194,304-triangle soup whose centroids
     come from 32 Gaussian clusters (sigma 1e-3 in the unit cube), so many
@@ -723,7 +793,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--workload", choices=["single", "batched", "served", "soup", "render"], default="single")
+    ap.add_argument("--workload", choices=["single", "batched", "served", "soup", "render", "octree"],
+                    default="single")
     ap.add_argument("--num-mesh", type=int, default=4096, help="meshes of the batched workload")
     ap.add_argument("--pool", type=int, default=512, help="meshes of the served pool")
     ap.add_argument("--requests", type=int, default=1000, help="requests per served trace")
@@ -742,6 +813,8 @@ def main():
         return run_soup(args)
     if args.workload == "render":
         return run_render(args)
+    if args.workload == "octree":
+        return run_octree(args)
     return run_ours(args)
 
 

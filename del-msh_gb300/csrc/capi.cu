@@ -548,6 +548,58 @@ int dm_pix2tri_interpolate_bwd(uint64_t stream_ptr, uint32_t img_w, uint32_t img
   return DM_OK;
 }
 
+size_t dm_quad_oct_tree_scratch_bytes(uint32_t num_idx) { return dm::octree_scratch_bytes(num_idx); }
+
+int dm_quad_oct_tree_bnodes_and_bnode2depth_and_bnode2onode_and_idx2bnode(
+    uint64_t stream_ptr, uint32_t num_idx, const uint32_t* idx2morton, uint32_t num_dim, uint32_t max_depth,
+    uint32_t* bnodes, uint32_t* bnode2depth, uint32_t* bnode2onode, uint32_t* idx2bnode, void* scratch,
+    size_t scratch_bytes) {
+  DM_REQUIRE(num_idx >= 2, "num_idx must be >= 2 (got %u)", num_idx);
+  DM_REQUIRE(num_idx <= kMaxElems, "num_idx %u exceeds the supported maximum", num_idx);
+  DM_REQUIRE(num_dim == 2 || num_dim == 3, "num_dim must be 2 or 3 (got %u)", num_dim);
+  DM_REQUIRE(max_depth >= 1 && num_dim * max_depth <= 32, "num_dim * max_depth must be in 1..32");
+  DM_REQUIRE(idx2morton && bnodes && bnode2depth && bnode2onode && idx2bnode, "NULL argument");
+  cudaStream_t s = as_stream(stream_ptr);
+  Scratch sc;
+  if (int e = sc.acquire(scratch, scratch_bytes, dm::octree_scratch_bytes(num_idx), s, nullptr)) return e;
+  dm::launch_octree_brt(s, num_idx, idx2morton, num_dim, max_depth, bnodes, bnode2depth, bnode2onode, idx2bnode,
+                        static_cast<uint32_t*>(sc.ptr), status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+int dm_quad_oct_tree_make_tree_from_binary_radix_tree(
+    uint64_t stream_ptr, uint32_t num_idx, const uint32_t* bnodes, const uint32_t* bnode2onode,
+    const uint32_t* bnode2depth, const uint32_t* idx2bnode, const uint32_t* idx2morton, uint32_t num_dim,
+    uint32_t max_depth, uint32_t num_onode, uint32_t* onodes, uint32_t* onode2depth, float* onode2center,
+    uint32_t* idx2onode, float* idx2center) {
+  DM_REQUIRE(num_idx >= 2 && num_idx <= kMaxElems, "num_idx must be in 2..%u (got %u)", kMaxElems, num_idx);
+  DM_REQUIRE(num_dim == 2 || num_dim == 3, "num_dim must be 2 or 3 (got %u)", num_dim);
+  DM_REQUIRE(max_depth >= 1 && num_dim * max_depth <= 32, "num_dim * max_depth must be in 1..32");
+  DM_REQUIRE(num_onode >= 1 && num_onode <= num_idx - 1, "num_onode must be in 1..num_idx-1 (got %u)", num_onode);
+  DM_REQUIRE(bnodes && bnode2onode && bnode2depth && idx2bnode && idx2morton && onodes && onode2depth &&
+                 onode2center && idx2onode && idx2center,
+             "NULL argument");
+  dm::launch_octree_make(as_stream(stream_ptr), num_idx, bnodes, bnode2onode, bnode2depth, idx2bnode, idx2morton,
+                         num_onode, max_depth, num_dim, onodes, onode2depth, onode2center, idx2onode, idx2center,
+                         status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
+int dm_quad_oct_tree_aggregate(uint64_t stream_ptr, uint32_t num_idx, uint32_t num_vdim, const float* idx2val,
+                               const uint32_t* idx2onode, uint32_t num_link, const uint32_t* onodes,
+                               uint32_t num_onode, float* onode2aggval) {
+  DM_REQUIRE(num_link == 5 || num_link == 9, "num_link must be 5 (quadtree) or 9 (octree), got %u", num_link);
+  DM_REQUIRE(idx2val && idx2onode && onodes && onode2aggval, "NULL argument");
+  cudaStream_t s = as_stream(stream_ptr);
+  DM_CUDA(cudaMemsetAsync(onode2aggval, 0, sizeof(float) * num_onode * num_vdim, s));
+  dm::launch_octree_aggregate(s, num_idx, num_vdim, idx2val, idx2onode, num_link, onodes, num_onode, onode2aggval,
+                              status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
 size_t dm_batch_build_scratch_bytes(uint32_t num_mesh, uint32_t total_tri) {
   return batch_layout(num_mesh, total_tri).total;
 }

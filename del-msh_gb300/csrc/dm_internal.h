@@ -211,4 +211,19 @@ void launch_interpolate_bwd(cudaStream_t s, uint32_t img_w, uint32_t img_h, cons
                             const MeshView& m, uint32_t num_vdim, const float* vtx2val, const float* ndc2world,
                             const float* dldw_pix2val, float* dldw_vtx2xyz, float* dldw_vtx2val, uint32_t* status);
 
+// -------------------------------------------------------------- octree.cu
+// Quad/oct-trees from the binary radix tree of sorted unique Morton codes.
+size_t octree_scratch_bytes(uint32_t num_idx);
+void launch_octree_brt(cudaStream_t s, uint32_t num_idx, const uint32_t* idx2morton, uint32_t num_dim,
+                       uint32_t max_depth, uint32_t* bnodes, uint32_t* bnode2depth, uint32_t* bnode2onode,
+                       uint32_t* idx2bnode, uint32_t* tile_sums, uint32_t* status);
+void launch_octree_make(cudaStream_t s, uint32_t num_idx, const uint32_t* bnodes, const uint32_t* bnode2onode,
+                        const uint32_t* bnode2depth, const uint32_t* idx2bnode, const uint32_t* idx2morton,
+                        uint32_t num_onode, uint32_t max_depth, uint32_t num_dim, uint32_t* onodes,
+                        uint32_t* onode2depth, float* onode2center, uint32_t* idx2onode, float* idx2center,
+                        uint32_t* status);
+void launch_octree_aggregate(cudaStream_t s, uint32_t num_idx, uint32_t num_vdim, const float* idx2val,
+                             const uint32_t* idx2onode, uint32_t num_link, const uint32_t* onodes, uint32_t num_onode,
+                             float* onode2aggval, uint32_t* status);
+
 }  // namespace dm

@@ -41,14 +41,12 @@ __device__ __forceinline__ uint32_t run_end(const Codes& c, uint32_t n, uint32_t
   return lo;
 }
 
-// One branch ib of the radix tree over n sorted codes: mortons.rs:221-288
-// (range), 290-325 (split) and bvhnodes_morton.rs:24-47 (writes).  The
-// branch index is always one end of its range; the other end is written to
-// other_end[ib] when other_end != nullptr (used by the windowed refit).
-template <typename Codes, typename Objs>
-__device__ __forceinline__ void topology_node(uint32_t n, const Codes& c, const Objs& obj, uint32_t* bvhnodes,
-                                              uint32_t ib, uint32_t* other_end) {
-  uint32_t r0, r1;
+// Range [r0, r1] and split of branch ib of the radix tree over n sorted codes:
+// mortons.rs:221-288 (range) and 290-325 (split).  The branch index is always
+// one end of its range.
+template <typename Codes>
+__device__ __forceinline__ void karras_range_split(uint32_t n, const Codes& c, uint32_t ib, uint32_t& r0,
+                                                   uint32_t& r1, uint32_t& isplit) {
   if (ib == 0) {
     r0 = 0;
     r1 = n - 1;
@@ -77,20 +75,29 @@ __device__ __forceinline__ void topology_node(uint32_t n, const Codes& c, const 
       r1 = up ? j : ib;
     }
   }
-  uint32_t isplit = r0;
-  {
-    const uint32_t mc_start = c(r0);
-    const int common = __clz(mc_start ^ c(r1));
-    if (common != 32) {
-      uint32_t step = r1 - r0;
-      while (step > 1) {
-        step = (step + 1) / 2;
-        const uint32_t cand = isplit + step;
-        if (cand >= r1) continue;
-        if (__clz(mc_start ^ c(cand)) > common) isplit = cand;
-      }
+  isplit = r0;
+  const uint32_t mc_start = c(r0);
+  const int common = __clz(mc_start ^ c(r1));
+  if (common != 32) {
+    uint32_t step = r1 - r0;
+    while (step > 1) {
+      step = (step + 1) / 2;
+      const uint32_t cand = isplit + step;
+      if (cand >= r1) continue;
+      if (__clz(mc_start ^ c(cand)) > common) isplit = cand;
     }
   }
+}
+
+// One branch ib of the radix tree over n sorted codes (karras_range_split)
+// written in the bvhnodes layout (bvhnodes_morton.rs:24-47).  The other end
+// of the branch's range is written to other_end[ib] when other_end !=
+// nullptr (used by the refit).
+template <typename Codes, typename Objs>
+__device__ __forceinline__ void topology_node(uint32_t n, const Codes& c, const Objs& obj, uint32_t* bvhnodes,
+                                              uint32_t ib, uint32_t* other_end) {
+  uint32_t r0, r1, isplit;
+  karras_range_split(n, c, ib, r0, r1, isplit);
   if (other_end) other_end[ib] = (r0 == ib) ? r1 : r0;
   const uint32_t nb = n - 1;
   uint32_t* me = bvhnodes + static_cast<size_t>(ib) * 3;

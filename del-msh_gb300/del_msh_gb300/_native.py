@@ -21,6 +21,12 @@ _SIGNATURES = {
     "dm_device_status": (i32, [C.POINTER(C.c_uint32), i32]),
     "dm_tuning_get": (i32, [vp]),
     "dm_render_scratch_bytes": (sz, []),
+    "dm_quad_oct_tree_scratch_bytes": (sz, [u32]),
+    "dm_quad_oct_tree_bnodes_and_bnode2depth_and_bnode2onode_and_idx2bnode":
+        (i32, [u64, u32, vp, u32, u32, vp, vp, vp, vp, vp, sz]),
+    "dm_quad_oct_tree_make_tree_from_binary_radix_tree":
+        (i32, [u64, u32, vp, vp, vp, vp, vp, u32, u32, u32, vp, vp, vp, vp, vp]),
+    "dm_quad_oct_tree_aggregate": (i32, [u64, u32, u32, vp, vp, u32, vp, u32, vp]),
     "dm_pix2depth_update": (i32, [u64, u32, u32, vp, vp, u32, vp, u32, vp, vp, vp, sz]),
     "dm_pix2depth_bwd_wrt_vtx2xyz": (i32, [u64, u32, u32, vp, vp, u32, vp, u32, vp, vp, vp, vp, sz]),
     "dm_pix2tri_interpolate": (i32, [u64, u32, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp]),

@@ -236,6 +236,43 @@ int dm_pix2tri_interpolate_bwd(uint64_t stream_ptr, uint32_t img_w, uint32_t img
                                uint32_t num_vdim, const float* vtx2val, const float* transform_ndc2world,
                                const float* dldw_pix2val, float* dldw_vtx2xyz, float* dldw_vtx2val);
 
+/* ---- quad/oct-trees from the binary radix tree of sorted unique Morton codes ----
+ * Layouts of del-msh-cpu/src/quad_oct_tree.rs: bnodes u32[num_idx-1][3]
+ * (branch links; a leaf child i is encoded num_idx-1+i), onodes
+ * u32[num_onode][1 + 2^num_dim] (parent, then children; a leaf child idx is
+ * encoded num_onode+idx, no child = u32::MAX), centres f32[.][num_dim]. */
+
+/* Scratch size of dm_quad_oct_tree_bnodes_and_bnode2depth_and_bnode2onode_and_idx2bnode. */
+size_t dm_quad_oct_tree_scratch_bytes(uint32_t num_idx);
+
+/* Binary radix tree with per-branch depth, the branch -> octree-node map
+ * (exclusive scan of "depth differs from the parent's") and each leaf's
+ * parent branch.  num_onode = bnode2onode[num_idx-2] + 1.
+ * Replaces: del-msh-dlpack/src/quad_oct_tree.rs:22-123 (kernels
+ * quad_oct_tree.cu:26-101 + a cumsum; CPU quad_oct_tree.rs:2-50,88-125). */
+int dm_quad_oct_tree_bnodes_and_bnode2depth_and_bnode2onode_and_idx2bnode(
+    uint64_t stream_ptr, uint32_t num_idx, const uint32_t* idx2morton, uint32_t num_dim, uint32_t max_depth,
+    uint32_t* bnodes, uint32_t* bnode2depth, uint32_t* bnode2onode, uint32_t* idx2bnode, void* scratch,
+    size_t scratch_bytes);
+
+/* The quad/oct-tree.  onodes must be filled with u32::MAX and onode2depth
+ * with 0 beforehand (as the reference's wrapper does).
+ * Replaces: del-msh-dlpack/src/quad_oct_tree.rs:125-224 (kernel
+ * quad_oct_tree.cu:103-205; CPU quad_oct_tree.rs:127-233). */
+int dm_quad_oct_tree_make_tree_from_binary_radix_tree(
+    uint64_t stream_ptr, uint32_t num_idx, const uint32_t* bnodes, const uint32_t* bnode2onode,
+    const uint32_t* bnode2depth, const uint32_t* idx2bnode, const uint32_t* idx2morton, uint32_t num_dim,
+    uint32_t max_depth, uint32_t num_onode, uint32_t* onodes, uint32_t* onode2depth, float* onode2center,
+    uint32_t* idx2onode, float* idx2center);
+
+/* onode2aggval[n] = sum of idx2val over the leaves below octree node n
+ * (zeroed first; added with atomics).
+ * Replaces: del-msh-dlpack/src/quad_oct_tree.rs:226-290 (kernel
+ * quad_oct_tree.cu:207-233; CPU quad_oct_tree.rs:420-451). */
+int dm_quad_oct_tree_aggregate(uint64_t stream_ptr, uint32_t num_idx, uint32_t num_vdim, const float* idx2val,
+                               const uint32_t* idx2onode, uint32_t num_link, const uint32_t* onodes,
+                               uint32_t num_onode, float* onode2aggval);
+
 /* ---- batches: many independent meshes of uneven sizes in one call ----
  * The meshes are stored back to back.  mesh2tri / mesh2vtx are device
  * u32[num_mesh+1] prefix offsets (mesh m owns triangles mesh2tri[m] ..

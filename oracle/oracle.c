@@ -965,3 +965,165 @@ void or_interpolate_bwd(uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri,
       for (int j = 0; j < 3; ++j) dldw_vtx2val[(size_t)iv[j] * num_vdim + k] += g[k] * b[j];
   }
 }
+
+/* ------------------------------------------------------------------------
+ * Quad/oct-trees from the binary radix tree of sorted unique Morton codes:
+ * quad_oct_tree.rs:2-63 (binary tree + depth, morton2center), 88-125
+ * (bnode2onode, idx2bnode), 127-233 (the tree), 235-338 (check_octree),
+ * 420-451 (aggregate). */
+
+void or_qot_binary_radix_tree_and_depth(uint32_t num_idx, const uint32_t* idx2morton, uint32_t num_dim,
+                                        uint32_t max_depth, uint32_t* bnodes, uint32_t* bnode2depth) {
+  const uint32_t num_bnode = num_idx - 1;
+  bnodes[0] = OR_UMAX;
+  for (uint32_t ib = 0; ib < num_bnode; ++ib) {
+    uint32_t r0, r1;
+    or_range_of_binary_radix_tree_node(idx2morton, num_idx, ib, &r0, &r1);
+    const uint32_t isplit = or_split_of_binary_radix_tree_node(idx2morton, r0, r1);
+    if (r0 == isplit) {
+      bnodes[ib * 3 + 1] = num_bnode + isplit;
+    } else {
+      bnodes[ib * 3 + 1] = isplit;
+      bnodes[isplit * 3] = ib;
+    }
+    if (r1 == isplit + 1) {
+      bnodes[ib * 3 + 2] = num_bnode + isplit + 1;
+    } else {
+      bnodes[ib * 3 + 2] = isplit + 1;
+      bnodes[(isplit + 1) * 3] = ib;
+    }
+    const uint32_t delta = (uint32_t)clz32(idx2morton[isplit] ^ idx2morton[isplit + 1]);
+    const uint32_t offset = 32u - num_dim * max_depth;
+    bnode2depth[ib] = (delta - offset) / num_dim;
+  }
+}
+
+void or_qot_bnode2onode_and_idx2bnode(uint32_t num_idx, const uint32_t* bnodes, const uint32_t* bnode2depth,
+                                      uint32_t* bnode2onode, uint32_t* idx2bnode) {
+  const uint32_t num_bnode = num_idx - 1;
+  uint32_t* iso = (uint32_t*)calloc(num_bnode, sizeof(uint32_t));
+  for (uint32_t ib = 0; ib < num_bnode; ++ib) {
+    if (bnodes[ib * 3 + 1] >= num_bnode) idx2bnode[bnodes[ib * 3 + 1] - num_bnode] = ib;
+    if (bnodes[ib * 3 + 2] >= num_bnode) idx2bnode[bnodes[ib * 3 + 2] - num_bnode] = ib;
+    if (ib == 0) continue;
+    const uint32_t parent = bnodes[ib * 3];
+    if (bnode2depth[ib] != bnode2depth[parent]) iso[ib - 1] = 1;
+  }
+  bnode2onode[0] = 0;
+  for (uint32_t ib = 1; ib < num_bnode; ++ib) bnode2onode[ib] = bnode2onode[ib - 1] + iso[ib - 1];
+  free(iso);
+}
+
+static void qot_morton2center(uint32_t morton, uint32_t num_dim, uint32_t depth, uint32_t max_depth, float c[3]) {
+  uint32_t key = morton >> ((max_depth - depth) * num_dim);
+  for (uint32_t d = 0; d < num_dim; ++d) c[d] = 0.5f;
+  for (uint32_t i = 0; i < depth; ++i)
+    for (uint32_t d = 0; d < num_dim; ++d) {
+      const uint32_t j = num_dim - d - 1;
+      c[j] = (c[j] + (float)(key & 1u)) * 0.5f;
+      key >>= 1;
+    }
+}
+
+static void qot_parent(uint32_t cur, const uint32_t* bnodes, const uint32_t* b2o, const uint32_t* b2d, uint32_t* on,
+                       uint32_t* depth) {
+  for (;;) {
+    if (cur == 0 || b2o[cur] != b2o[cur - 1]) {
+      *on = b2o[cur];
+      *depth = b2d[cur];
+      return;
+    }
+    cur = bnodes[cur * 3];
+  }
+}
+
+void or_qot_make_tree(uint32_t num_idx, const uint32_t* bnodes, const uint32_t* b2o, const uint32_t* b2d,
+                      const uint32_t* idx2bnode, const uint32_t* idx2morton, uint32_t num_onode, uint32_t max_depth,
+                      uint32_t num_dim, uint32_t* onodes, uint32_t* onode2depth, float* onode2center,
+                      uint32_t* idx2onode, float* idx2center) {
+  const uint32_t num_child = 1u << num_dim, nlink = num_child + 1;
+  for (uint32_t i = 0; i < num_idx; ++i) {
+    uint32_t op, dp;
+    qot_parent(idx2bnode[i], bnodes, b2o, b2d, &op, &dp);
+    const uint32_t key = idx2morton[i];
+    const uint32_t ic = (key >> ((max_depth - 1 - dp) * num_dim)) & (num_child - 1);
+    onodes[op * nlink + 1 + ic] = i + num_onode;
+    idx2onode[i] = op;
+    float c[3];
+    qot_morton2center(key, num_dim, max_depth, max_depth, c);
+    for (uint32_t d = 0; d < num_dim; ++d) idx2center[i * num_dim + d] = c[d];
+    if (i + 1 >= num_idx) continue;
+    const uint32_t ib = i;
+    if (ib == 0) {
+      for (uint32_t d = 0; d < num_dim; ++d) onode2center[d] = 0.5f;
+      continue;
+    }
+    if (b2o[ib - 1] == b2o[ib]) continue;
+    qot_parent(bnodes[ib * 3], bnodes, b2o, b2d, &op, &dp);
+    const uint32_t morton = idx2morton[ib];
+    const uint32_t icb = (morton >> ((max_depth - 1 - dp) * num_dim)) & (num_child - 1);
+    const uint32_t on = b2o[ib];
+    onodes[op * nlink + 1 + icb] = on;
+    onodes[on * nlink] = op;
+    const uint32_t depth = b2d[ib];
+    qot_morton2center(morton, num_dim, depth, max_depth, c);
+    for (uint32_t d = 0; d < num_dim; ++d) onode2center[on * num_dim + d] = c[d];
+    onode2depth[on] = depth;
+  }
+}
+
+void or_qot_aggregate(uint32_t num_idx, uint32_t num_vdim, const float* idx2val, const uint32_t* idx2onode,
+                      uint32_t num_link, const uint32_t* onodes, uint32_t num_onode, float* onode2aggval) {
+  for (uint32_t k = 0; k < num_onode * num_vdim; ++k) onode2aggval[k] = 0.0f;
+  for (uint32_t idx = 0; idx < num_idx; ++idx) {
+    uint32_t on = idx2onode[idx];
+    while (on != OR_UMAX && on < num_onode) {
+      for (uint32_t d = 0; d < num_vdim; ++d) onode2aggval[on * num_vdim + d] += idx2val[idx * num_vdim + d];
+      on = onodes[on * num_link];
+    }
+  }
+}
+
+/* quad_oct_tree.rs:235-338: every leaf reached exactly once from the root,
+ * children strictly deeper than their parent and inside its cell. */
+static int qot_visit(uint32_t node, uint32_t nlink, uint32_t nchild, const uint32_t* onodes, uint32_t num_onode,
+                     uint32_t* seen, uint32_t num_idx, uint32_t budget) {
+  if (budget == 0) return 0;
+  for (uint32_t k = 0; k < nchild; ++k) {
+    const uint32_t ch = onodes[node * nlink + 1 + k];
+    if (ch == OR_UMAX) continue;
+    if (ch >= num_onode) {
+      if (ch - num_onode >= num_idx) return 0;
+      seen[ch - num_onode] += 1;
+    } else if (!qot_visit(ch, nlink, nchild, onodes, num_onode, seen, num_idx, budget - 1)) {
+      return 0;
+    }
+  }
+  return 1;
+}
+
+int or_qot_check(uint32_t num_idx, uint32_t num_dim, const uint32_t* idx2onode, const float* idx2center,
+                 const uint32_t* onodes, const uint32_t* onode2depth, const float* onode2center, uint32_t num_onode,
+                 uint32_t max_depth) {
+  const uint32_t nchild = 1u << num_dim, nlink = nchild + 1;
+  uint32_t* seen = (uint32_t*)calloc(num_idx, sizeof(uint32_t));
+  int ok = qot_visit(0, nlink, nchild, onodes, num_onode, seen, num_idx, 64);
+  for (uint32_t i = 0; ok && i < num_idx; ++i) ok = seen[i] == 1;
+  free(seen);
+  for (uint32_t n = 0; ok && n < num_onode + num_idx; ++n) {
+    const uint32_t depth = n < num_onode ? onode2depth[n] : max_depth;
+    const float h = 0.5f / (float)(1u << depth);
+    const float* c = n < num_onode ? onode2center + n * num_dim : idx2center + (n - num_onode) * num_dim;
+    const uint32_t p = n < num_onode ? onodes[n * nlink] : idx2onode[n - num_onode];
+    if (p == OR_UMAX) continue;
+    if (p >= num_onode) return 0;
+    const uint32_t dp = onode2depth[p];
+    if (!(depth > dp)) return 0;
+    const float hp = 0.5f / (float)(1u << dp);
+    for (uint32_t d = 0; d < num_dim; ++d) {
+      const float dd = fabsf(c[d] - onode2center[p * num_dim + d]);
+      if (!(dd + h < hp * (1.0f + 1.0e-7f))) return 0;
+    }
+  }
+  return ok;
+}

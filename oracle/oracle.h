@@ -136,6 +136,21 @@ void or_interpolate_bwd(uint32_t img_w, uint32_t img_h, const uint32_t* pix2tri,
                         const float* vtx2val, const float ndc2world[16], const float* dldw_pix2val,
                         float* dldw_vtx2xyz, float* dldw_vtx2val);
 
+/* quad/oct-trees (quad_oct_tree.rs) */
+void or_qot_binary_radix_tree_and_depth(uint32_t num_idx, const uint32_t* idx2morton, uint32_t num_dim,
+                                        uint32_t max_depth, uint32_t* bnodes, uint32_t* bnode2depth);
+void or_qot_bnode2onode_and_idx2bnode(uint32_t num_idx, const uint32_t* bnodes, const uint32_t* bnode2depth,
+                                      uint32_t* bnode2onode, uint32_t* idx2bnode);
+void or_qot_make_tree(uint32_t num_idx, const uint32_t* bnodes, const uint32_t* b2o, const uint32_t* b2d,
+                      const uint32_t* idx2bnode, const uint32_t* idx2morton, uint32_t num_onode, uint32_t max_depth,
+                      uint32_t num_dim, uint32_t* onodes, uint32_t* onode2depth, float* onode2center,
+                      uint32_t* idx2onode, float* idx2center);
+void or_qot_aggregate(uint32_t num_idx, uint32_t num_vdim, const float* idx2val, const uint32_t* idx2onode,
+                      uint32_t num_link, const uint32_t* onodes, uint32_t num_onode, float* onode2aggval);
+int or_qot_check(uint32_t num_idx, uint32_t num_dim, const uint32_t* idx2onode, const float* idx2center,
+                 const uint32_t* onodes, const uint32_t* onode2depth, const float* onode2center, uint32_t num_onode,
+                 uint32_t max_depth);
+
 uint32_t or_tree_height(const uint32_t* bvhnodes, uint32_t num_leaf);
 
 #ifdef __cplusplus

@@ -64,6 +64,13 @@ def lib():
         L.or_pix2depth_bwd.restype = i32
         L.or_pix2depth_bwd.argtypes = [u32, u32, _f32p, _u32p, u32, _u32p, u32, _f32p, _f32p, _f32p]
         L.or_interpolate.argtypes = [u32, u32, _u32p, u32, _u32p, u32, _f32p, u32, _f32p, _f32p, _f32p]
+        L.or_qot_binary_radix_tree_and_depth.argtypes = [u32, _u32p, u32, u32, _u32p, _u32p]
+        L.or_qot_bnode2onode_and_idx2bnode.argtypes = [u32, _u32p, _u32p, _u32p, _u32p]
+        L.or_qot_make_tree.argtypes = [u32, _u32p, _u32p, _u32p, _u32p, _u32p, u32, u32, u32, _u32p, _u32p, _f32p,
+                                       _u32p, _f32p]
+        L.or_qot_aggregate.argtypes = [u32, u32, _f32p, _u32p, u32, _u32p, u32, _f32p]
+        L.or_qot_check.restype = i32
+        L.or_qot_check.argtypes = [u32, u32, _u32p, _f32p, _u32p, _u32p, _f32p, u32, u32]
         L.or_interpolate_bwd.argtypes = [u32, u32, _u32p, u32, _u32p, u32, _f32p, u32, _f32p, _f32p, _f32p, _f32p,
                                          _f32p]
         _lib = L
@@ -287,6 +294,49 @@ def interpolate_bwd(pix2tri, tri2vtx, vtx2xyz, vtx2val, t_ndc2world_colmajor, dl
                              _c(t_ndc2world_colmajor, np.float32).reshape(-1),
                              _c(dldw_pix2val, np.float32).reshape(-1), gx, gv)
     return gx.reshape(-1, 3), gv.reshape(-1, nd)
+
+
+# ---------------------------------------------------------- quad/oct-trees
+
+def quad_oct_tree(idx2morton, num_dim, max_depth=None):
+    """quad_oct_tree.rs restated: binary radix tree, bnode2onode, idx2bnode
+    and the quad/oct-tree of sorted unique codes; returns a dict."""
+    c = _c(idx2morton, np.uint32).reshape(-1)
+    max_depth = 32 // num_dim if max_depth is None else max_depth
+    n = c.size
+    bnodes = np.zeros((n - 1) * 3, np.uint32)
+    b2d = np.zeros(n - 1, np.uint32)
+    lib().or_qot_binary_radix_tree_and_depth(n, c, num_dim, max_depth, bnodes, b2d)
+    b2o = np.zeros(n - 1, np.uint32)
+    i2b = np.full(n, 0xFFFFFFFF, np.uint32)
+    lib().or_qot_bnode2onode_and_idx2bnode(n, bnodes, b2d, b2o, i2b)
+    num_onode = int(b2o[-1]) + 1
+    nlink = 1 + 2 ** num_dim
+    onodes = np.full(num_onode * nlink, 0xFFFFFFFF, np.uint32)
+    o2d = np.zeros(num_onode, np.uint32)
+    o2c = np.zeros(num_onode * num_dim, np.float32)
+    i2o = np.zeros(n, np.uint32)
+    i2c = np.zeros(n * num_dim, np.float32)
+    lib().or_qot_make_tree(n, bnodes, b2o, b2d, i2b, c, num_onode, max_depth, num_dim, onodes, o2d, o2c, i2o, i2c)
+    return dict(bnodes=bnodes.reshape(-1, 3), bnode2depth=b2d, bnode2onode=b2o, idx2bnode=i2b, num_onode=num_onode,
+                onodes=onodes.reshape(num_onode, nlink), onode2depth=o2d, onode2center=o2c.reshape(-1, num_dim),
+                idx2onode=i2o, idx2center=i2c.reshape(-1, num_dim), max_depth=max_depth)
+
+
+def quad_oct_tree_check(t, num_dim):
+    return bool(lib().or_qot_check(t["idx2onode"].size, num_dim, t["idx2onode"], _c(t["idx2center"], np.float32),
+                                   _c(t["onodes"], np.uint32), t["onode2depth"], _c(t["onode2center"], np.float32),
+                                   t["num_onode"], t["max_depth"]))
+
+
+def quad_oct_tree_aggregate(idx2val, idx2onode, onodes):
+    v = _c(idx2val, np.float32)
+    nd = v.shape[1]
+    on = _c(onodes, np.uint32)
+    out = np.zeros(on.shape[0] * nd, np.float32)
+    lib().or_qot_aggregate(v.shape[0], nd, v.reshape(-1), _c(idx2onode, np.uint32), on.shape[1], on.reshape(-1),
+                           on.shape[0], out)
+    return out.reshape(-1, nd)
 
 
 # ---------------------------------------------------------- reference code
