@@ -682,6 +682,68 @@ def run_octree(args):
     return 0
 
 
+def run_selfx(args):
+    """Self-intersection through the BVH: two copies of a displaced torus
+    (724x724 grid each, 2,096,704 triangles in all), the second shifted so
+    that the two interpenetrate; the LBVH of both is built first, then the
+    query is timed with CUDA events (L2 flushed between repetitions), with the
+    oracle's recursive search on one host thread beside it."""
+    import torch
+    from del_msh_gb300 import _native
+    from del_msh_gb300 import workloads as W
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    dev = torch.device("cuda", 0)
+    _native.load(build_if_missing=True)
+    t, v = W.displaced_torus(724, seed=SEED)
+    tri = np.concatenate([t, t + v.shape[0]]).astype(np.uint32)
+    vtx = np.concatenate([v, v + np.array([0.35, 0.2, 0.1], np.float32)]).astype(np.float32)
+    T, V = tri.shape[0], vtx.shape[0]
+    d_tri = torch.from_numpy(tri.view(np.int32)).to(dev).view(torch.uint32)
+    d_vtx = torch.from_numpy(vtx).to(dev)
+    bvh, aabb = TriMesh3.make_bvhnodes_bvhnode2aabb(d_tri, d_vtx)
+    segs, pairs = TriMesh3.self_intersection(d_tri, d_vtx, bvh, aabb)
+    cap = max(int(pairs.shape[0]) * 2, 1024)
+    out_p = torch.empty((cap, 2), dtype=torch.uint32, device=dev)
+    out_s = torch.empty((cap, 2, 3), dtype=torch.float32, device=dev)
+    count = torch.zeros((1,), dtype=torch.int32, device=dev)
+    flush = torch.empty((L2_FLUSH_BYTES,), dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream(dev)
+
+    def query():
+        _native.call("dm_trimesh3_self_intersection", stream.cuda_stream, T, d_tri.data_ptr(), V, d_vtx.data_ptr(),
+                     bvh.data_ptr(), aabb.data_ptr(), cap, out_p.data_ptr(), out_s.data_ptr(), count.data_ptr())
+
+    for _ in range(max(args.warmup, 3)):
+        query()
+    times = []
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        query()
+        b.record(stream)
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = statistics.median(times)
+    line = {"metric": "triangles/s (self-intersection query through the LBVH)", "unit": "triangles/s",
+            "value": T / (ms * 1e-3), "ms": ms, "steps": args.steps,
+            "config": {"workload": f"two interpenetrating displaced tori, {T} triangles", "pairs": int(count.item()),
+                       "l2": "flushed between repetitions"},
+            "device_status": _native.device_status(clear=True)}
+    if not args.no_cpu:
+        from oracle import build as obuild
+        from oracle import oracle as O
+        obuild.build_oracle()
+        h_bvh, h_aabb = bvh.cpu().numpy(), aabb.cpu().numpy()
+        t0 = time.perf_counter()
+        rp, _ = O.self_intersection(tri, vtx, h_bvh, h_aabb)
+        t_cpu = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": T / t_cpu, "unit": "triangles/s", "cores": 1, "kind": "port",
+                                "sample": "one full recursive search (1 thread)", "pairs": int(len(rp))}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_soup(args):
     """Adversarial Morton distribution: 4,194,304-triangle soup whose centroids
     come from 32 Gaussian clusters (sigma 1e-3 in the unit cube), so many
@@ -793,7 +855,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
-    ap.add_argument("--workload", choices=["single", "batched", "served", "soup", "render", "octree"],
+    ap.add_argument("--workload", choices=["single", "batched", "served", "soup", "render", "octree", "selfx"],
                     default="single")
     ap.add_argument("--num-mesh", type=int, default=4096, help="meshes of the batched workload")
     ap.add_argument("--pool", type=int, default=512, help="meshes of the served pool")
@@ -815,6 +877,8 @@ def main():
         return run_render(args)
     if args.workload == "octree":
         return run_octree(args)
+    if args.workload == "selfx":
+        return run_selfx(args)
     return run_ours(args)
 
 

@@ -600,6 +600,19 @@ int dm_quad_oct_tree_aggregate(uint64_t stream_ptr, uint32_t num_idx, uint32_t n
   return DM_OK;
 }
 
+int dm_trimesh3_self_intersection(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                                  const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb,
+                                  uint32_t capacity, uint32_t* pairs, float* segments, uint32_t* count) {
+  if (int e = check_mesh(num_tri, tri2vtx, num_vtx, vtx2xyz)) return e;
+  DM_REQUIRE(bvhnodes && bvhnode2aabb && count && (capacity == 0 || (pairs && segments)), "NULL argument");
+  cudaStream_t s = as_stream(stream_ptr);
+  DM_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
+  dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb};
+  dm::launch_self_intersection(s, m, capacity, pairs, segments, count, status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+
 size_t dm_batch_build_scratch_bytes(uint32_t num_mesh, uint32_t total_tri) {
   return batch_layout(num_mesh, total_tri).total;
 }

@@ -226,4 +226,11 @@ void launch_octree_aggregate(cudaStream_t s, uint32_t num_idx, uint32_t num_vdim
                              const uint32_t* idx2onode, uint32_t num_link, const uint32_t* onodes, uint32_t num_onode,
                              float* onode2aggval, uint32_t* status);
 
+// --------------------------------------------------------------- selfx.cu
+// Self-intersecting triangle pairs through the BVH: pairs u32[capacity][2],
+// segments f32[capacity][6]; *count (zero on entry) receives the number
+// found, which may exceed capacity (then only capacity are written).
+void launch_self_intersection(cudaStream_t s, const MeshView& m, uint32_t capacity, uint32_t* pairs, float* segments,
+                              uint32_t* count, uint32_t* status);
+
 }  // namespace dm

@@ -98,3 +98,30 @@ def update_bvhnode2aabb(tri2vtx: torch.Tensor, vtx2xyz0: torch.Tensor, bvhnodes:
 def make_bvhnode2aabb_from_bvhnodes(tri2vtx, vtx2xyz0, vtx2xyz1, bvhnodes, bvhnode2aabb):
     """Name of the reference's DLPack-level helper (TriMesh3/__init__.py:39-46)."""
     return update_bvhnode2aabb(tri2vtx, vtx2xyz0, bvhnodes, bvhnode2aabb, vtx2xyz1)
+
+
+def self_intersection(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor, bvhnodes: torch.Tensor,
+                      bvhnode2aabb: torch.Tensor, capacity: int = 1 << 16):
+    """Self-intersecting triangle pairs through the BVH (the GPU form of
+    ``del_msh_cpu::trimesh3_intersection::search_with_bvh_inside_branch``, as
+    returned by del-msh-numpy's mesh_intersection binding): (edge2node2xyz
+    (k, 2, 3) float32 segments, edge2tri (k, 2) uint32 triangle pairs), in no
+    particular order.  Grows its buffer and repeats when more pairs exist."""
+    num_tri, num_vtx = tri2vtx.shape[0], vtx2xyz.shape[0]
+    device = tri2vtx.device
+    assert_shape_dtype_device(tri2vtx, (num_tri, 3), torch.uint32, device)
+    assert_shape_dtype_device(vtx2xyz, (num_vtx, 3), torch.float32, device)
+    assert_shape_dtype_device(bvhnodes, (2 * num_tri - 1, 3), torch.uint32, device)
+    assert_shape_dtype_device(bvhnode2aabb, (2 * num_tri - 1, 6), torch.float32, device)
+    require_cuda(device)
+    count = torch.zeros((1,), dtype=torch.int32, device=device)
+    while True:
+        pairs = torch.empty((capacity, 2), dtype=torch.uint32, device=device)
+        segs = torch.empty((capacity, 2, 3), dtype=torch.float32, device=device)
+        _native.call("dm_trimesh3_self_intersection", stream_ptr(device), num_tri, ptr(tri2vtx.contiguous()),
+                     num_vtx, ptr(vtx2xyz.detach().contiguous()), ptr(bvhnodes.contiguous()),
+                     ptr(bvhnode2aabb.contiguous()), capacity, ptr(pairs), ptr(segs), ptr(count))
+        n = int(count.item())
+        if n <= capacity:
+            return segs[:n], pairs[:n]
+        capacity = n

@@ -21,6 +21,7 @@ _SIGNATURES = {
     "dm_device_status": (i32, [C.POINTER(C.c_uint32), i32]),
     "dm_tuning_get": (i32, [vp]),
     "dm_render_scratch_bytes": (sz, []),
+    "dm_trimesh3_self_intersection": (i32, [u64, u32, vp, u32, vp, vp, vp, u32, vp, vp, vp]),
     "dm_quad_oct_tree_scratch_bytes": (sz, [u32]),
     "dm_quad_oct_tree_bnodes_and_bnode2depth_and_bnode2onode_and_idx2bnode":
         (i32, [u64, u32, vp, u32, u32, vp, vp, vp, vp, vp, sz]),

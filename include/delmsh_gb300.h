@@ -236,6 +236,20 @@ int dm_pix2tri_interpolate_bwd(uint64_t stream_ptr, uint32_t img_w, uint32_t img
                                uint32_t num_vdim, const float* vtx2val, const float* transform_ndc2world,
                                const float* dldw_pix2val, float* dldw_vtx2xyz, float* dldw_vtx2val);
 
+/* Self-intersecting triangle pairs of a mesh through its BVH: for each pair
+ * (i, j) (the triangle of the left subtree first) the segment (p0, p1) where
+ * they cross.  Pairs sharing two vertices are never reported; a pair sharing
+ * one vertex reports the segment from that vertex to where an opposite edge
+ * pierces the other triangle.  *count (device u32) receives the number of
+ * pairs, which may exceed `capacity`, in which case only `capacity` pairs are
+ * written (call again with a larger buffer).  The list is unordered.  Deep
+ * trees whose node-pair stack exceeds 192 entries raise status bit 2.
+ * Replaces: del-msh-cpu/src/trimesh3_intersection.rs:86-179
+ * search_with_bvh_inside_branch (binding del-msh-numpy/src/mesh_intersection.rs). */
+int dm_trimesh3_self_intersection(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                                  const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb,
+                                  uint32_t capacity, uint32_t* pairs, float* segments, uint32_t* count);
+
 /* ---- quad/oct-trees from the binary radix tree of sorted unique Morton codes ----
  * Layouts of del-msh-cpu/src/quad_oct_tree.rs: bnodes u32[num_idx-1][3]
  * (branch links; a leaf child i is encoded num_idx-1+i), onodes

@@ -1127,3 +1127,203 @@ int or_qot_check(uint32_t num_idx, uint32_t num_dim, const uint32_t* idx2onode, 
   }
   return ok;
 }
+
+/* ------------------------------------------------------------------------
+ * Self-intersection through the BVH: trimesh3_intersection.rs:10-179
+ * (pair logic, search_with_bvh_between_branches, _inside_branch).  The
+ * del-geo-core segment formulas are restated (parity unpinned): tri/tri by
+ * the two plane-crossing segments overlapped along n_a x n_b (reported when
+ * of non-zero length; coplanar pairs are not); a shared vertex by
+ * Moller-Trumbore of the opposite edges (0 <= t <= 1) against the other
+ * triangle.  Three shared vertices: not reported (the reference panics). */
+
+static void lerp_cross(const float vi[3], const float vj[3], float di, float dj, float out[3]) {
+  const float s = di / (di - dj);
+  for (int k = 0; k < 3; ++k) out[k] = vi[k] + (vj[k] - vi[k]) * s;
+}
+
+static int plane_segment(const float* v[3], const float d[3], float s0[3], float s1[3]) {
+  float pts[4][3];
+  int n = 0;
+  for (int k = 0; k < 3; ++k)
+    if (d[k] == 0.0f) {
+      memcpy(pts[n], v[k], sizeof(float) * 3);
+      ++n;
+    }
+  for (int k = 0; k < 3; ++k) {
+    const int i = k, j = (k + 1) % 3;
+    if ((d[i] > 0.0f && d[j] < 0.0f) || (d[i] < 0.0f && d[j] > 0.0f)) {
+      lerp_cross(v[i], v[j], d[i], d[j], pts[n]);
+      ++n;
+    }
+  }
+  if (n < 2) return 0;
+  memcpy(s0, pts[0], sizeof(float) * 3);
+  memcpy(s1, pts[1], sizeof(float) * 3);
+  return 1;
+}
+
+static void sub3v(float o[3], const float a[3], const float b[3]) {
+  for (int k = 0; k < 3; ++k) o[k] = a[k] - b[k];
+}
+
+static int tri_tri_segment(const float* a[3], const float* b[3], float p0[3], float p1[3]) {
+  float e1[3], e2[3], nb[3], na[3], da[3], dbv[3];
+  sub3v(e1, b[1], b[0]);
+  sub3v(e2, b[2], b[0]);
+  cross3(nb, e1, e2);
+  const float db = -dot3(nb, b[0]);
+  for (int k = 0; k < 3; ++k) da[k] = dot3(nb, a[k]) + db;
+  if ((da[0] > 0.0f && da[1] > 0.0f && da[2] > 0.0f) || (da[0] < 0.0f && da[1] < 0.0f && da[2] < 0.0f)) return 0;
+  if (da[0] == 0.0f && da[1] == 0.0f && da[2] == 0.0f) return 0;
+  sub3v(e1, a[1], a[0]);
+  sub3v(e2, a[2], a[0]);
+  cross3(na, e1, e2);
+  const float dA = -dot3(na, a[0]);
+  for (int k = 0; k < 3; ++k) dbv[k] = dot3(na, b[k]) + dA;
+  if ((dbv[0] > 0.0f && dbv[1] > 0.0f && dbv[2] > 0.0f) || (dbv[0] < 0.0f && dbv[1] < 0.0f && dbv[2] < 0.0f))
+    return 0;
+  float sa0[3], sa1[3], sb0[3], sb1[3], D[3];
+  if (!plane_segment(a, da, sa0, sa1) || !plane_segment(b, dbv, sb0, sb1)) return 0;
+  cross3(D, na, nb);
+  float ta0 = dot3(D, sa0), ta1 = dot3(D, sa1), tb0 = dot3(D, sb0), tb1 = dot3(D, sb1);
+  if (ta1 < ta0) {
+    float t[3];
+    memcpy(t, sa0, sizeof t);
+    memcpy(sa0, sa1, sizeof t);
+    memcpy(sa1, t, sizeof t);
+    const float x = ta0;
+    ta0 = ta1;
+    ta1 = x;
+  }
+  if (tb1 < tb0) {
+    float t[3];
+    memcpy(t, sb0, sizeof t);
+    memcpy(sb0, sb1, sizeof t);
+    memcpy(sb1, t, sizeof t);
+    const float x = tb0;
+    tb0 = tb1;
+    tb1 = x;
+  }
+  const float lo = ta0 >= tb0 ? ta0 : tb0, hi = ta1 <= tb1 ? ta1 : tb1;
+  if (!(lo < hi)) return 0;
+  memcpy(p0, ta0 >= tb0 ? sa0 : sb0, sizeof(float) * 3);
+  memcpy(p1, ta1 <= tb1 ? sa1 : sb1, sizeof(float) * 3);
+  return 1;
+}
+
+static int edge_tri(const float e0[3], const float e1[3], const float* t0, const float* t1, const float* t2,
+                    float x[3]) {
+  float dir[3], t;
+  sub3v(dir, e1, e0);
+  if (!or_tri3_ray(t0, t1, t2, e0, dir, &t, NULL) || !(t <= 1.0f)) return 0;
+  for (int k = 0; k < 3; ++k) x[k] = e0[k] + t * dir[k];
+  return 1;
+}
+
+int or_tri_pair_segment(const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t it, uint32_t jt, float p0[3],
+                        float p1[3]) {
+  if (it == jt) return 0;
+  const uint32_t* vi = tri2vtx + (size_t)it * 3;
+  const uint32_t* vj = tri2vtx + (size_t)jt * 3;
+  int ci[3], cj[3], shared = 0;
+  for (int k = 0; k < 3; ++k) {
+    ci[k] = vi[k] == vj[0] || vi[k] == vj[1] || vi[k] == vj[2];
+    cj[k] = vj[k] == vi[0] || vj[k] == vi[1] || vj[k] == vi[2];
+    shared += ci[k];
+  }
+  if (shared >= 2) return 0;
+  const float* a[3];
+  const float* b[3];
+  for (int k = 0; k < 3; ++k) {
+    a[k] = vtx2xyz + (size_t)vi[k] * 3;
+    b[k] = vtx2xyz + (size_t)vj[k] * 3;
+  }
+  if (shared == 0) return tri_tri_segment(a, b, p0, p1);
+  const int si = ci[0] ? 0 : (ci[1] ? 1 : 2), sj = cj[0] ? 0 : (cj[1] ? 1 : 2);
+  const float *s = a[si], *pa = a[(si + 1) % 3], *pb = a[(si + 2) % 3], *qa = b[(sj + 1) % 3], *qb = b[(sj + 2) % 3];
+  float x[3];
+  if (edge_tri(qa, qb, s, pa, pb, x) || edge_tri(pa, pb, s, qa, qb, x)) {
+    memcpy(p0, s, sizeof(float) * 3);
+    memcpy(p1, x, sizeof(float) * 3);
+    return 1;
+  }
+  return 0;
+}
+
+typedef struct {
+  const uint32_t* tri2vtx;
+  const float* vtx2xyz;
+  const uint32_t* bvhnodes;
+  const float* aabb;
+  uint32_t cap, cnt;
+  uint32_t* pairs;
+  float* segs;
+} SelfxCtx;
+
+static int boxes_overlap(const float* a, const float* b) {
+  return a[0] <= b[3] && b[0] <= a[3] && a[1] <= b[4] && b[1] <= a[4] && a[2] <= b[5] && b[2] <= a[5];
+}
+
+static void selfx_between(SelfxCtx* c, uint32_t n0, uint32_t n1) {
+  if (!boxes_overlap(c->aabb + (size_t)n0 * 6, c->aabb + (size_t)n1 * 6)) return;
+  const uint32_t a0 = c->bvhnodes[n0 * 3 + 1], a1 = c->bvhnodes[n0 * 3 + 2];
+  const uint32_t b0 = c->bvhnodes[n1 * 3 + 1], b1 = c->bvhnodes[n1 * 3 + 2];
+  const int la = a1 == OR_UMAX, lb = b1 == OR_UMAX;
+  if (!la && !lb) {
+    selfx_between(c, a0, b0);
+    selfx_between(c, a1, b0);
+    selfx_between(c, a0, b1);
+    selfx_between(c, a1, b1);
+  } else if (!la) {
+    selfx_between(c, a0, n1);
+    selfx_between(c, a1, n1);
+  } else if (!lb) {
+    selfx_between(c, n0, b0);
+    selfx_between(c, n0, b1);
+  } else {
+    float p0[3], p1[3];
+    if (or_tri_pair_segment(c->tri2vtx, c->vtx2xyz, a0, b0, p0, p1)) {
+      if (c->cnt < c->cap) {
+        c->pairs[c->cnt * 2] = a0;
+        c->pairs[c->cnt * 2 + 1] = b0;
+        memcpy(c->segs + (size_t)c->cnt * 6, p0, sizeof p0);
+        memcpy(c->segs + (size_t)c->cnt * 6 + 3, p1, sizeof p1);
+      }
+      ++c->cnt;
+    }
+  }
+}
+
+static void selfx_inside(SelfxCtx* c, uint32_t n) {
+  const uint32_t c0 = c->bvhnodes[n * 3 + 1], c1 = c->bvhnodes[n * 3 + 2];
+  if (c1 == OR_UMAX) return;
+  selfx_between(c, c0, c1);
+  selfx_inside(c, c0);
+  selfx_inside(c, c1);
+}
+
+uint32_t or_self_intersection(const uint32_t* tri2vtx, const float* vtx2xyz, const uint32_t* bvhnodes,
+                              const float* aabb, uint32_t cap, uint32_t* pairs, float* segs) {
+  SelfxCtx c = {tri2vtx, vtx2xyz, bvhnodes, aabb, cap, 0, pairs, segs};
+  selfx_inside(&c, 0);
+  return c.cnt;
+}
+
+uint32_t or_self_intersection_brute(uint32_t num_tri, const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t cap,
+                                    uint32_t* pairs, float* segs) {
+  uint32_t cnt = 0;
+  for (uint32_t i = 0; i < num_tri; ++i)
+    for (uint32_t j = i + 1; j < num_tri; ++j) {
+      float p0[3], p1[3];
+      if (!or_tri_pair_segment(tri2vtx, vtx2xyz, i, j, p0, p1)) continue;
+      if (cnt < cap) {
+        pairs[cnt * 2] = i;
+        pairs[cnt * 2 + 1] = j;
+        memcpy(segs + (size_t)cnt * 6, p0, sizeof p0);
+        memcpy(segs + (size_t)cnt * 6 + 3, p1, sizeof p1);
+      }
+      ++cnt;
+    }
+  return cnt;
+}

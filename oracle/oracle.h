@@ -151,6 +151,14 @@ int or_qot_check(uint32_t num_idx, uint32_t num_dim, const uint32_t* idx2onode, 
                  const uint32_t* onodes, const uint32_t* onode2depth, const float* onode2center, uint32_t num_onode,
                  uint32_t max_depth);
 
+/* self-intersection (trimesh3_intersection.rs) */
+int or_tri_pair_segment(const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t it, uint32_t jt, float p0[3],
+                        float p1[3]);
+uint32_t or_self_intersection(const uint32_t* tri2vtx, const float* vtx2xyz, const uint32_t* bvhnodes,
+                              const float* aabb, uint32_t cap, uint32_t* pairs, float* segs);
+uint32_t or_self_intersection_brute(uint32_t num_tri, const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t cap,
+                                    uint32_t* pairs, float* segs);
+
 uint32_t or_tree_height(const uint32_t* bvhnodes, uint32_t num_leaf);
 
 #ifdef __cplusplus

@@ -69,6 +69,10 @@ def lib():
         L.or_qot_make_tree.argtypes = [u32, _u32p, _u32p, _u32p, _u32p, _u32p, u32, u32, u32, _u32p, _u32p, _f32p,
                                        _u32p, _f32p]
         L.or_qot_aggregate.argtypes = [u32, u32, _f32p, _u32p, u32, _u32p, u32, _f32p]
+        L.or_self_intersection.restype = u32
+        L.or_self_intersection.argtypes = [_u32p, _f32p, _u32p, _f32p, u32, _u32p, _f32p]
+        L.or_self_intersection_brute.restype = u32
+        L.or_self_intersection_brute.argtypes = [u32, _u32p, _f32p, u32, _u32p, _f32p]
         L.or_qot_check.restype = i32
         L.or_qot_check.argtypes = [u32, u32, _u32p, _f32p, _u32p, _u32p, _f32p, u32, u32]
         L.or_interpolate_bwd.argtypes = [u32, u32, _u32p, u32, _u32p, u32, _f32p, u32, _f32p, _f32p, _f32p, _f32p,
@@ -337,6 +341,28 @@ def quad_oct_tree_aggregate(idx2val, idx2onode, onodes):
     lib().or_qot_aggregate(v.shape[0], nd, v.reshape(-1), _c(idx2onode, np.uint32), on.shape[1], on.reshape(-1),
                            on.shape[0], out)
     return out.reshape(-1, nd)
+
+
+# ------------------------------------------------------- self-intersection
+
+def self_intersection(tri2vtx, vtx2xyz, bvhnodes, aabb, brute=False):
+    """trimesh3_intersection.rs restated: (pairs u32[k][2], segments f32[k][6])
+    in the reference's visiting order (BVH search), or i < j order (brute)."""
+    tri2vtx, vtx2xyz = _c(tri2vtx, np.uint32), _c(vtx2xyz, np.float32)
+    cap = 1 << 16
+    while True:
+        pairs = np.zeros(cap * 2, np.uint32)
+        segs = np.zeros(cap * 6, np.float32)
+        if brute:
+            n = lib().or_self_intersection_brute(tri2vtx.size // 3, tri2vtx.reshape(-1), vtx2xyz.reshape(-1), cap,
+                                                 pairs, segs)
+        else:
+            n = lib().or_self_intersection(tri2vtx.reshape(-1), vtx2xyz.reshape(-1),
+                                           _c(bvhnodes, np.uint32).reshape(-1), _c(aabb, np.float32).reshape(-1),
+                                           cap, pairs, segs)
+        if n <= cap:
+            return pairs[: 2 * n].reshape(-1, 2), segs[: 6 * n].reshape(-1, 6)
+        cap = n
 
 
 # ---------------------------------------------------------- reference code
