@@ -606,9 +606,13 @@ int dm_trimesh3_self_intersection(uint64_t stream_ptr, uint32_t num_tri, const u
   if (int e = check_mesh(num_tri, tri2vtx, num_vtx, vtx2xyz)) return e;
   DM_REQUIRE(bvhnodes && bvhnode2aabb && count && (capacity == 0 || (pairs && segments)), "NULL argument");
   cudaStream_t s = as_stream(stream_ptr);
+  Scratch sc;
+  const size_t need = dm::self_intersection_scratch_bytes(num_tri);
+  if (int e = sc.acquire(nullptr, 0, need, s, nullptr)) return e;
   DM_CUDA(cudaMemsetAsync(count, 0, sizeof(uint32_t), s));
   dm::MeshView m{num_tri, num_vtx, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb};
-  dm::launch_self_intersection(s, m, capacity, pairs, segments, count, status_ptr());
+  if (dm::launch_self_intersection(s, m, capacity, pairs, segments, count, sc.ptr, need, status_ptr()) != 0)
+    return fail(DM_ERR_CUDA, "self-intersection round failed: %s", cudaGetErrorString(cudaGetLastError()));
   DM_CUDA(cudaGetLastError());
   return DM_OK;
 }

@@ -230,7 +230,10 @@ void launch_octree_aggregate(cudaStream_t s, uint32_t num_idx, uint32_t num_vdim
 // Self-intersecting triangle pairs through the BVH: pairs u32[capacity][2],
 // segments f32[capacity][6]; *count (zero on entry) receives the number
 // found, which may exceed capacity (then only capacity are written).
-void launch_self_intersection(cudaStream_t s, const MeshView& m, uint32_t capacity, uint32_t* pairs, float* segments,
-                              uint32_t* count, uint32_t* status);
+// Synchronizes the stream once per round (to size the next).  scratch:
+// self_intersection_scratch_bytes(num_tri).  Returns 0, or -1 on a CUDA error.
+size_t self_intersection_scratch_bytes(uint32_t num_tri);
+int launch_self_intersection(cudaStream_t s, const MeshView& m, uint32_t capacity, uint32_t* pairs, float* segments,
+                             uint32_t* count, void* scratch, size_t scratch_bytes, uint32_t* status);
 
 }  // namespace dm

@@ -2,9 +2,12 @@
 // (trimesh3_intersection.rs:1-179: search_with_bvh_inside_branch and
 // search_with_bvh_between_branches).  The recursion inside(root) visits, at
 // every branch n, between(left(n), right(n)) and recurses; so the pairs are
-// exactly the union over branches n of between(left(n), right(n)), and each
-// thread runs one such tandem traversal with an explicit stack of node
-// pairs.  Every unordered pair of leaves meets at exactly one branch (their
+// exactly the union over branches n of between(left(n), right(n)).  Each
+// start pair is searched depth-first by one thread with an explicit stack of
+// node pairs, in rounds: a thread that has visited kBudget pairs hands its
+// remaining stack to the next round, so that the few large subtree pairs
+// near the root spread over many threads instead of one.
+// Every unordered pair of leaves meets at exactly one branch (their
 // lowest common ancestor), with the triangle of the left subtree first, as
 // in the recursion; only the order of the output list differs.
 //
@@ -158,17 +161,68 @@ __device__ __forceinline__ bool boxes_overlap(const float* a, const float* b) {
   return a[0] <= b[3] && b[0] <= a[3] && a[1] <= b[4] && b[1] <= a[4] && a[2] <= b[5] && b[2] <= a[5];
 }
 
-// One thread per branch n: between(left(n), right(n)).
-__global__ void __launch_bounds__(kThreads) k_selfx(MeshView m, uint32_t capacity, uint32_t* pairs, float* segments,
-                                                   uint32_t* count, uint32_t* status) {
+__device__ __forceinline__ void report_pair(const MeshView& m, uint32_t a0, uint32_t b0, uint32_t capacity,
+                                            uint32_t* pairs, float* segments, uint32_t* count, uint32_t* status) {
+  float3 p0, p1;
+  if (!tri_pair(m, a0, b0, p0, p1, status)) return;
+  const uint32_t slot = atomicAdd(count, 1u);
+  if (slot >= capacity) return;
+  pairs[static_cast<size_t>(slot) * 2] = a0;
+  pairs[static_cast<size_t>(slot) * 2 + 1] = b0;
+  float* sg = segments + static_cast<size_t>(slot) * 6;
+  sg[0] = p0.x;
+  sg[1] = p0.y;
+  sg[2] = p0.z;
+  sg[3] = p1.x;
+  sg[4] = p1.y;
+  sg[5] = p1.z;
+}
+
+// The first round starts from (left(n), right(n)) for every branch n.
+__global__ void __launch_bounds__(kThreads) k_selfx_init(MeshView m, uint2* frontier) {
   const uint32_t n = blockIdx.x * kThreads + threadIdx.x;
   if (m.num_tri < 2 || n >= m.num_tri - 1) return;
+  frontier[n] = make_uint2(__ldg(m.bvhnodes + static_cast<size_t>(n) * 3 + 1),
+                           __ldg(m.bvhnodes + static_cast<size_t>(n) * 3 + 2));
+}
+
+// One round: each thread searches depth-first from one start pair with an
+// explicit stack; after kBudget node-pair visits it hands its remaining stack
+// to the next round (when all of it fits there; otherwise it finishes alone),
+// so that the few large subtree pairs near the root are split over many
+// threads in the following rounds.
+constexpr uint32_t kBudget = 512;
+
+__global__ void __launch_bounds__(kThreads) k_selfx_round(MeshView m, const uint2* __restrict__ start,
+                                                         uint32_t num_start, uint2* next, uint32_t* num_next,
+                                                         uint64_t next_cap, uint32_t capacity, uint32_t* pairs,
+                                                         float* segments, uint32_t* count, uint32_t* status) {
+  const uint32_t k = blockIdx.x * kThreads + threadIdx.x;
+  if (k >= num_start) return;
   const uint32_t num_node = 2 * m.num_tri - 1;
   const uint32_t* bn = m.bvhnodes;
   uint2 stack[kPairStack];
   int sp = 0;
-  stack[sp++] = make_uint2(__ldg(bn + static_cast<size_t>(n) * 3 + 1), __ldg(bn + static_cast<size_t>(n) * 3 + 2));
+  stack[sp++] = start[k];
+  uint32_t visits = 0;
   while (sp > 0) {
+    if (++visits > kBudget && sp > 1) {
+      // reserve room only if the whole stack fits, so that the next round's
+      // list has no unwritten holes (a bounded number of attempts)
+      uint32_t cur = *reinterpret_cast<volatile uint32_t*>(num_next);
+      bool handed = false;
+      for (int attempt = 0; attempt < 64 && cur + static_cast<uint64_t>(sp) <= next_cap; ++attempt) {
+        const uint32_t seen = atomicCAS(num_next, cur, cur + static_cast<uint32_t>(sp));
+        if (seen == cur) {
+          for (int q = 0; q < sp; ++q) next[cur + q] = stack[q];
+          handed = true;
+          break;
+        }
+        cur = seen;
+      }
+      if (handed) return;
+      visits = 0;  // no room: keep going alone
+    }
     const uint2 pr = stack[--sp];
     if (pr.x >= num_node || pr.y >= num_node) {
       raise_status(status, kStatusBadIndex);
@@ -179,21 +233,7 @@ __global__ void __launch_bounds__(kThreads) k_selfx(MeshView m, uint32_t capacit
     const uint32_t b0 = __ldg(bn + static_cast<size_t>(pr.y) * 3 + 1), b1 = __ldg(bn + static_cast<size_t>(pr.y) * 3 + 2);
     const bool la = a1 == kUMax, lb = b1 == kUMax;
     if (la && lb) {
-      float3 p0, p1;
-      if (tri_pair(m, a0, b0, p0, p1, status)) {
-        const uint32_t slot = atomicAdd(count, 1u);
-        if (slot < capacity) {
-          pairs[static_cast<size_t>(slot) * 2] = a0;
-          pairs[static_cast<size_t>(slot) * 2 + 1] = b0;
-          float* sg = segments + static_cast<size_t>(slot) * 6;
-          sg[0] = p0.x;
-          sg[1] = p0.y;
-          sg[2] = p0.z;
-          sg[3] = p1.x;
-          sg[4] = p1.y;
-          sg[5] = p1.z;
-        }
-      }
+      report_pair(m, a0, b0, capacity, pairs, segments, count, status);
       continue;
     }
     const int need = (!la && !lb) ? 4 : 2;
@@ -219,11 +259,35 @@ __global__ void __launch_bounds__(kThreads) k_selfx(MeshView m, uint32_t capacit
 
 }  // namespace
 
-void launch_self_intersection(cudaStream_t s, const MeshView& m, uint32_t capacity, uint32_t* pairs, float* segments,
-                              uint32_t* count, uint32_t* status) {
-  if (m.num_tri < 2) return;
-  const uint32_t branches = m.num_tri - 1;
-  k_selfx<<<(branches + kThreads - 1) / kThreads, kThreads, 0, s>>>(m, capacity, pairs, segments, count, status);
+size_t self_intersection_scratch_bytes(uint32_t num_tri) {
+  const uint64_t cap = num_tri < (1u << 20) ? (1u << 20) : num_tri;  // start pairs per round
+  return 256 + 2 * cap * sizeof(uint2);
+}
+
+int launch_self_intersection(cudaStream_t s, const MeshView& m, uint32_t capacity, uint32_t* pairs, float* segments,
+                             uint32_t* count, void* scratch, size_t scratch_bytes, uint32_t* status) {
+  if (m.num_tri < 2) return 0;
+  uint32_t* num_next = static_cast<uint32_t*>(scratch);
+  const uint64_t cap = (scratch_bytes - 256) / (2 * sizeof(uint2));
+  uint2* fa = reinterpret_cast<uint2*>(static_cast<char*>(scratch) + 256);
+  uint2* fb = fa + cap;
+  uint32_t num_cur = m.num_tri - 1;
+  k_selfx_init<<<(num_cur + kThreads - 1) / kThreads, kThreads, 0, s>>>(m, fa);
+  // rounds until no thread hands work on (each round either finishes its
+  // threads' work or splits it, so there are few; bounded here)
+  for (int round = 0; round < 1000 && num_cur > 0; ++round) {
+    if (cudaMemsetAsync(num_next, 0, sizeof(uint32_t), s) != cudaSuccess) return -1;
+    k_selfx_round<<<(num_cur + kThreads - 1) / kThreads, kThreads, 0, s>>>(m, fa, num_cur, fb, num_next, cap,
+                                                                           capacity, pairs, segments, count, status);
+    uint32_t n = 0;
+    if (cudaMemcpyAsync(&n, num_next, sizeof(uint32_t), cudaMemcpyDeviceToHost, s) != cudaSuccess) return -1;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return -1;
+    num_cur = n;  // every reservation was written in full
+    uint2* t = fa;
+    fa = fb;
+    fb = t;
+  }
+  return 0;
 }
 
 }  // namespace dm

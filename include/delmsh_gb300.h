@@ -242,8 +242,12 @@ int dm_pix2tri_interpolate_bwd(uint64_t stream_ptr, uint32_t img_w, uint32_t img
  * one vertex reports the segment from that vertex to where an opposite edge
  * pierces the other triangle.  *count (device u32) receives the number of
  * pairs, which may exceed `capacity`, in which case only `capacity` pairs are
- * written (call again with a larger buffer).  The list is unordered.  Deep
- * trees whose node-pair stack exceeds 192 entries raise status bit 2.
+ * written (call again with a larger buffer).  The list is unordered.  The
+ * search runs depth-first per thread (192-entry node-pair stack; status bit
+ * 2 if one overflows) in rounds that rebalance the remaining work; each round
+ * reads the next round's size back to the host, so the call synchronizes the
+ * stream.  Its working memory (16 MB per million triangles, at least 16 MB)
+ * comes from cudaMallocAsync.
  * Replaces: del-msh-cpu/src/trimesh3_intersection.rs:86-179
  * search_with_bvh_inside_branch (binding del-msh-numpy/src/mesh_intersection.rs). */
 int dm_trimesh3_self_intersection(uint64_t stream_ptr, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
