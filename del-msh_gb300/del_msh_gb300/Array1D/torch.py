@@ -7,7 +7,7 @@ from __future__ import annotations
 import torch
 
 from .. import _native
-from ..util_torch import ptr, require_cuda, stream_ptr
+from ..util_torch import ptr, require_cuda, scratch, stream_ptr
 
 
 def argsort(idx2val: torch.Tensor):
@@ -26,5 +26,6 @@ def argsort(idx2val: torch.Tensor):
     require_cuda(device)
     jdx2idx = torch.empty(size=(n,), device=device, dtype=torch.uint32)
     jdx2val = idx2val.clone()
-    _native.call("dm_array1d_argsort", stream_ptr(device), n, ptr(jdx2val), ptr(jdx2idx), None, 0)
+    scr = scratch(device, _native.load().dm_array1d_argsort_scratch_bytes(n))
+    _native.call("dm_array1d_argsort", stream_ptr(device), n, ptr(jdx2val), ptr(jdx2idx), ptr(scr), scr.numel())
     return jdx2idx, jdx2val

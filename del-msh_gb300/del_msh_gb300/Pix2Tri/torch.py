@@ -12,7 +12,7 @@ from typing import Tuple
 import torch
 
 from .. import _native
-from ..util_torch import assert_shape_dtype_device, ptr, require_cuda, stream_ptr
+from ..util_torch import assert_shape_dtype_device, ptr, require_cuda, scratch, stream_ptr
 
 
 def by_raycasting(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor, bvhnodes: torch.Tensor, bvhnode2aabb: torch.Tensor,
@@ -35,9 +35,10 @@ def by_raycasting(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor, bvhnodes: torch.
     pix2tri = torch.empty((img_h, img_w), dtype=torch.uint32, device=device)
     pix2t = torch.empty((img_h, img_w), dtype=torch.float32, device=device) if return_depth else None
     colmajor = transform_ndc2world.T.contiguous()
+    scr = scratch(device, _native.load().dm_cast_scratch_bytes(img_w * img_h, num_tri))
     _native.call("dm_pix2tri_by_raycast", stream_ptr(device), img_w, img_h, ptr(pix2tri), ptr(pix2t), num_tri,
                  ptr(tri2vtx.contiguous()), num_vtx, ptr(vtx2xyz.contiguous()), ptr(bvhnodes.contiguous()),
-                 ptr(bvhnode2aabb.contiguous()), ptr(colmajor), None, 0)
+                 ptr(bvhnode2aabb.contiguous()), ptr(colmajor), ptr(scr), scr.numel())
     return (pix2tri, pix2t) if return_depth else pix2tri
 
 

@@ -6,7 +6,7 @@ from __future__ import annotations
 import torch
 
 from .. import _native
-from ..util_torch import assert_shape_dtype_device, ptr, require_cuda, stream_ptr
+from ..util_torch import assert_shape_dtype_device, ptr, require_cuda, scratch, stream_ptr
 
 
 def first_intersection_ray(ray_org: torch.Tensor, ray_dir: torch.Tensor, tri2vtx: torch.Tensor,
@@ -28,8 +28,9 @@ def first_intersection_ray(ray_org: torch.Tensor, ray_dir: torch.Tensor, tri2vtx
     hit_tri = torch.empty((num_ray,), dtype=torch.uint32, device=device)
     hit_t = torch.empty((num_ray,), dtype=torch.float32, device=device)
     hit_bc = torch.empty((num_ray, 3), dtype=torch.float32, device=device) if return_bc else None
+    scr = scratch(device, _native.load().dm_cast_scratch_bytes(num_ray, num_tri))
     _native.call("dm_search_bvh3_first_intersection_ray", stream_ptr(device), num_ray,
                  ptr(ray_org.detach().contiguous()), ptr(ray_dir.detach().contiguous()), ptr(hit_tri), ptr(hit_t),
                  ptr(hit_bc), num_tri, ptr(tri2vtx.contiguous()), num_vtx, ptr(vtx2xyz.detach().contiguous()),
-                 ptr(bvhnodes.contiguous()), ptr(bvhnode2aabb.contiguous()), None, 0)
+                 ptr(bvhnodes.contiguous()), ptr(bvhnode2aabb.contiguous()), ptr(scr), scr.numel())
     return (hit_tri, hit_t, hit_bc) if return_bc else (hit_tri, hit_t)

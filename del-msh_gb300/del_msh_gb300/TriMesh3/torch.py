@@ -12,7 +12,7 @@ from __future__ import annotations
 import torch
 
 from .. import _native
-from ..util_torch import assert_shape_dtype_device, ptr, require_cuda, stream_ptr
+from ..util_torch import assert_shape_dtype_device, ptr, require_cuda, scratch, stream_ptr
 
 
 def make_bvhnodes_bvhnode2aabb(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor):
@@ -34,8 +34,9 @@ def make_bvhnodes_bvhnode2aabb(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor):
     require_cuda(device)
     bvhnodes = torch.empty((2 * num_tri - 1, 3), dtype=torch.uint32, device=device)
     bvhnode2aabb = torch.empty((2 * num_tri - 1, 6), dtype=torch.float32, device=device)
+    scr = scratch(device, _native.load().dm_trimesh3_build_scratch_bytes(num_tri))
     _native.call("dm_trimesh3_make_bvhnodes_bvhnode2aabb", stream_ptr(device), num_tri, ptr(tri2vtx.contiguous()),
-                 num_vtx, ptr(vtx2xyz.contiguous()), ptr(bvhnodes), ptr(bvhnode2aabb), None, 0)
+                 num_vtx, ptr(vtx2xyz.contiguous()), ptr(bvhnodes), ptr(bvhnode2aabb), ptr(scr), scr.numel())
     return bvhnodes, bvhnode2aabb
 
 
@@ -58,10 +59,11 @@ def make_bvhnodes_bvhnode2aabb_ex(tri2vtx: torch.Tensor, vtx2xyz: torch.Tensor, 
                idx2tri=torch.empty((num_tri,), dtype=torch.uint32, device=device),
                idx2morton=torch.empty((num_tri,), dtype=torch.uint32, device=device),
                height=torch.zeros((1,), dtype=torch.int32, device=device) if want_height else None)
+    scr = scratch(device, _native.load().dm_trimesh3_build_scratch_bytes(num_tri))
     _native.call("dm_trimesh3_build_ex", stream_ptr(device), num_tri, ptr(tri2vtx.contiguous()), num_vtx,
                  ptr(vtx2xyz), ptr(out["bvhnodes"]), ptr(out["bvhnode2aabb"]), ptr(out["transform"]),
                  ptr(out["tri2morton"]), ptr(out["idx2tri"]), ptr(out["idx2morton"]),
-                 ptr(out["height"]) if want_height else None, None, 0)
+                 ptr(out["height"]) if want_height else None, ptr(scr), scr.numel())
     out["transform"] = out["transform"].view(4, 4).T.contiguous()
     out["height"] = int(out["height"].item()) if want_height else None
     return out

@@ -27,3 +27,10 @@ def ptr(t):
         return None
     assert t.is_contiguous(), "tensor must be contiguous"
     return t.data_ptr()
+
+
+def scratch(device: torch.device, nbytes: int) -> torch.Tensor:
+    """Working memory for one C-ABI call, from torch's caching allocator (so
+    repeated calls reuse it instead of allocating on the device each time);
+    its blocks are 512-byte aligned, as the C ABI requires 256."""
+    return torch.empty((max(int(nbytes), 1),), dtype=torch.uint8, device=device)
