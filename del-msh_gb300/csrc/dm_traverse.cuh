@@ -233,6 +233,7 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
     const Hit saved{__uint_as_float(f.z), f.w};
     uint32_t far;
     float far_enter;
+    bool pop = true;
     if (f.x & kChainBit) {
       // level j = f.y of a chain frame: far child = leaf j, saved = none
       // unless j is the chain's first link
@@ -245,19 +246,20 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
       float te = 0.f, tx = 0.f;
       node_slab(m, r, far, te, tx);  // hit when the frame was pushed; same value again
       far_enter = te;
-      if (j == first) {
-        --s.sp;
-        s.best = pick(saved, s.best);
-      } else {
-        stack.store(s.sp - 1, make_uint4(f.x, j - 1, f.z, f.w));
-      }
+      pop = j == first;
+      if (pop) --s.sp;
+      else stack.store(s.sp - 1, make_uint4(f.x, j - 1, f.z, f.w));
     } else {
       --s.sp;
       far = f.x;
       far_enter = __uint_as_float(f.y);
-      s.best = pick(saved, s.best);
     }
+    // The far test sees R(near) alone (search_bvh3.rs:168-189); only then is
+    // the enclosing level's result folded in.  Deciding on the folded value
+    // instead agrees only while every hit lies at or beyond its box's entry
+    // t, which rounding does not guarantee (a triangle on a box face).
     const bool skip = (s.best.id != kUMax) && far_enter > s.best.t;
+    if (pop) s.best = pick(saved, s.best);
     if (!skip) {
       s.node = far;
       if (s.node >= num_node) {

@@ -22,3 +22,34 @@ def bits(a):
     if a.dtype == np.float32:
         a[np.isnan(a)] = np.float32("nan")
     return np.ascontiguousarray(a).view(np.uint32)
+
+
+_CUBE_VTX = np.array([[0, 0, 0], [1, 0, 0], [1, 1, 0], [0, 1, 0], [0, 0, 1], [1, 0, 1], [1, 1, 1], [0, 1, 1]])
+_CUBE_TRI = np.array([[0, 2, 1], [0, 3, 2], [4, 5, 6], [4, 6, 7], [0, 1, 5], [0, 5, 4], [1, 2, 6], [1, 6, 5],
+                      [2, 3, 7], [2, 7, 6], [3, 0, 4], [3, 4, 7]])
+
+
+def voxel_cubes(rng, grid, num_cube, scale):
+    """Surfaces of `num_cube` unit cubes at random cells of a grid^3 lattice,
+    scaled by `scale` in f32 (so that lattice coordinates round), each face as
+    two triangles whose vertex order is rotated at random.  Cubes may coincide
+    or touch, so faces overlap and many hits lie on bounding-box faces."""
+    cells = rng.integers(0, grid, size=(num_cube, 3))
+    vtx = ((cells[:, None, :] + _CUBE_VTX[None]).reshape(-1, 3).astype(np.float32) * np.float32(scale))
+    rot = rng.integers(0, 3, size=(num_cube, 12))
+    cols = (np.arange(3)[None, None, :] + rot[:, :, None]) % 3
+    tri = np.take_along_axis(np.broadcast_to(_CUBE_TRI, (num_cube, 12, 3)), cols, axis=2)
+    tri = tri + 8 * np.arange(num_cube)[:, None, None]
+    return np.ascontiguousarray(tri.reshape(-1, 3).astype(np.uint32)), np.ascontiguousarray(vtx)
+
+
+def lattice_rays(rng, grid, scale, num_ray):
+    """Rays from random points around the lattice aimed at lattice points or
+    quarter points on its edges; about one coordinate in seven of the origin
+    equals the target's, giving axis-parallel directions."""
+    g = rng.integers(0, grid + 1, size=(num_ray, 3)).astype(np.float64)
+    g += np.where(rng.random((num_ray, 3)) < 0.5, rng.integers(0, 4, size=(num_ray, 3)) * 0.25, 0.0)
+    tgt = (g * scale).astype(np.float32)
+    org = ((rng.random((num_ray, 3)) * 2 - 0.5) * (grid + 2) * scale).astype(np.float32)
+    org = np.where(rng.random((num_ray, 3)) < 0.15, tgt, org)
+    return np.ascontiguousarray(org), np.ascontiguousarray(tgt - org)

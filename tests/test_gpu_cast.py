@@ -6,7 +6,7 @@ import math
 import numpy as np
 import pytest
 
-from helpers import bits, to_dev, to_np
+from helpers import bits, lattice_rays, to_dev, to_np, voxel_cubes
 
 from del_msh_gb300 import workloads as W
 
@@ -79,6 +79,40 @@ def test_cast_rays_duplicate_soup_deep_tiers(cuda, oracle):
     bc = to_np(bc, torch)
     ok = r_hit != UMAX
     assert np.allclose(bc[ok].sum(1), 1.0, atol=1e-5)
+    assert _status() == 0
+
+
+def face_tie_cases(num_mesh=40, num_ray=20000):
+    """Seeded voxel surfaces with rays aimed at lattice points: hits on
+    bounding-box faces and ties in t between triangles.  Where a hit's t
+    rounds below its box's entry t, the far-child test must see the near
+    child's result alone, as search_bvh3.rs:168-189 does; a test on the
+    result folded with the enclosing level's differs on about one ray in
+    10^4 of these."""
+    for seed in range(num_mesh):
+        rng = np.random.default_rng(1000 + seed)
+        grid = 3 + seed % 4
+        scale = np.float32(0.1 + rng.random())
+        tri, vtx = voxel_cubes(rng, grid, int(rng.integers(1, 7)), scale)
+        org, d = lattice_rays(rng, grid, scale, num_ray)
+        yield tri, vtx, org, d
+
+
+def test_cast_rays_box_face_ties(cuda, oracle):
+    from del_msh_gb300.SearchBvh3 import torch as SearchBvh3
+    torch = cuda
+    hits = 0
+    for tri, vtx, org, d in face_tie_cases():
+        ref = oracle.build(tri, vtx)
+        mesh = _dev_mesh(torch, tri, vtx)
+        assert np.array_equal(to_np(mesh[2], torch), ref["bvhnodes"])
+        hit, t = SearchBvh3.first_intersection_ray(to_dev(org, torch), to_dev(d, torch), *mesh)
+        r_hit, r_t = oracle.cast_rays(org, d, tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"])
+        hit, t = to_np(hit, torch), to_np(t, torch)
+        assert np.array_equal(hit, r_hit)
+        assert np.array_equal(bits(t[r_hit != UMAX]), bits(r_t[r_hit != UMAX]))
+        hits += int((r_hit != UMAX).sum())
+    assert hits > 100000
     assert _status() == 0
 
 
