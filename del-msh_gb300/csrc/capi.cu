@@ -286,7 +286,9 @@ bool set_tuning(const Tuning& t) {
   for (const auto& v : kCastVariants) cast_ok = cast_ok || (v[0] == t.cast_threads && v[1] == t.cast_stack);
   const bool tile_ok = t.tile_w == 2 || t.tile_w == 4 || t.tile_w == 8 || t.tile_w == 16 || t.tile_w == 32;
   const bool sort_ok = t.sort_window == 4 || t.sort_window == 8;
+  const auto phase_ok = [](uint32_t v) { return v >= 1 && v <= 32; };
   if (!cast_ok || !tile_ok || !sort_ok) return false;
+  if (!phase_ok(t.cast_refill_min) || !phase_ok(t.cast_leaf_min) || !phase_ok(t.cast_ascend_min)) return false;
   std::lock_guard<std::mutex> lk(g_tuning_mutex);
   g_tuning = t;
   return true;
@@ -314,7 +316,8 @@ int dm_device_status(uint32_t* bits, int clear) {
 int dm_tuning_get(dm_tuning* out) {
   DM_REQUIRE(out, "NULL argument");
   const dm::Tuning t = dm::get_tuning();
-  *out = dm_tuning{t.cast_threads, t.cast_stack, t.tile_w, t.sort_window, {0, 0, 0, 0}};
+  *out = dm_tuning{t.cast_threads, t.cast_stack,     t.tile_w,        t.sort_window,
+                   t.cast_refill_min, t.cast_leaf_min, t.cast_ascend_min, 0};
   return DM_OK;
 }
 
@@ -325,8 +328,14 @@ int dm_tuning_set(const dm_tuning* in) {
   t.cast_stack = in->cast_stack;
   t.tile_w = in->tile_w;
   t.sort_window = in->sort_window;
-  DM_REQUIRE(dm::set_tuning(t), "unsupported tuning (cast %u threads x %u frames, tile_w %u, sort window %u)",
-             in->cast_threads, in->cast_stack, in->tile_w, in->sort_window);
+  const auto phase = [](uint32_t v) { return v == 0 ? dm::kDefaultPhaseMin : v; };
+  t.cast_refill_min = phase(in->cast_refill_min);
+  t.cast_leaf_min = phase(in->cast_leaf_min);
+  t.cast_ascend_min = phase(in->cast_ascend_min);
+  DM_REQUIRE(dm::set_tuning(t),
+             "unsupported tuning (cast %u threads x %u frames, tile_w %u, sort window %u, phase minima %u/%u/%u)",
+             in->cast_threads, in->cast_stack, in->tile_w, in->sort_window, t.cast_refill_min, t.cast_leaf_min,
+             t.cast_ascend_min);
   return DM_OK;
 }
 

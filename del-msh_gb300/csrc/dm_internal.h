@@ -143,11 +143,18 @@ constexpr int kCastStack = 64;  // default frames of the on-chip (local) travers
 // Launch parameters picked by the autotuner (del_msh_gb300/autotune.py) and
 // set through dm_tuning_set.  Every choice gives the same results; only the
 // speed differs.  Read at each launch.
+constexpr uint32_t kDefaultPhaseMin = 6;
 struct Tuning {
   uint32_t cast_threads = 128;  // threads per block of the persistent cast
   uint32_t cast_stack = 64;     // on-chip frames per ray
   uint32_t tile_w = 8;          // pixel tile of one warp: tile_w x (32 / tile_w)
   uint32_t sort_window = 4;     // predecessors read per look-back round of the sort
+  // lanes of a warp that must wait for a phase of the persistent cast before
+  // the warp runs it (1 = whenever any lane waits): taking new rays, testing
+  // triangles, popping frames
+  uint32_t cast_refill_min = kDefaultPhaseMin;
+  uint32_t cast_leaf_min = kDefaultPhaseMin;
+  uint32_t cast_ascend_min = kDefaultPhaseMin;
 };
 // (threads, stack) pairs compiled for the persistent cast
 constexpr uint32_t kCastVariants[][2] = {{128, 64}, {64, 64}, {256, 64}, {128, 32}, {128, 96}};

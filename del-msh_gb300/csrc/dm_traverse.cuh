@@ -31,10 +31,11 @@
 // slab entry.  The stack then grows with the number of runs, not their
 // length, and the decisions are exactly those of the uncompressed frames.
 //
-// Execution.  The traversal is a step function (one node entry plus the
-// ascent that follows it) run by persistent warps: a lane whose ray is
+// Execution.  The traversal is split into phases (entering a branch, testing
+// a triangle, popping frames) run by persistent warps: a lane whose ray is
 // finished takes the next ray index from a global counter (one atomic per
-// warp), so lanes stay busy while long rays finish.  Frames live in a
+// warp), so lanes stay busy while long rays finish, and the rarer phases
+// wait until several lanes need them (k_cast_persistent).  Frames live in a
 // kCastStack-entry on-chip (local) stack; a ray that needs more is appended to
 // an overflow list and re-cast from scratch by a second kernel whose per-ray
 // stacks are carved from a global pool (capacity chosen on the device from
@@ -110,13 +111,16 @@ struct GlobalStack {
 
 constexpr uint32_t kChainBit = 0x80000000u;  // frame.x flag of a chain frame (node ids are < 2^31)
 
-// Per-ray traversal state between steps.
+// Per-ray traversal state between phases.
 struct Trav {
   uint32_t node;         // node to enter next
   uint32_t left, right;  // its record (bvhnodes[node*3+1], [node*3+2]), fetched ahead
   uint32_t sp;           // frames in use
   uint32_t steps;        // node entries so far (bounded by the node count)
   uint32_t chain_next;   // the link that would extend the top chain frame, or kUMax
+  uint32_t leaf_tri;     // triangle of a pending leaf test
+  float far_enter;       // slab entry of the far child that follows a near leaf
+  bool leaf_far;         // a far child (node/left/right) follows the pending leaf
   Hit best;              // accumulator of the current level
 };
 
@@ -128,105 +132,119 @@ __device__ __forceinline__ void load_record(const uint32_t* __restrict__ bn, uin
 
 enum StepResult : int { kStepContinue = 0, kStepDone = 1, kStepOverflow = 2 };
 
+// What a ray does next.  A step of the recursion is split into phases so
+// that the lanes of a warp can run each phase together: entering a branch
+// (kLaneInner), testing one triangle (kLaneLeaf), and popping frames until a
+// far child is to be searched or the ray is finished (kLaneAscend).
+enum LaneState : int {
+  kLaneIdle = 0,
+  kLaneInner = 1,
+  kLaneLeaf = 2,
+  kLaneAscend = 3,
+  kLaneOverflow = 4,  // the on-chip stack is full: the ray is re-cast by a deeper tier
+  kLaneDone = 5,      // s.best is the ray's result
+};
+
 // Starts a ray: a miss of the root box finishes it immediately.
 __device__ __forceinline__ bool trav_begin(const MeshView& m, const Ray& r, Trav& s) {
   s.node = 0;
   s.sp = 0;
   s.steps = 0;
   s.chain_next = kUMax;
+  s.leaf_tri = kUMax;
+  s.far_enter = 0.f;
+  s.leaf_far = false;
   s.best = Hit{INFINITY, kUMax};
   load_record(m.bvhnodes, 0, s.left, s.right);
   float te, tx;
   return node_slab(m, r, 0, te, tx);
 }
 
-// One node entry and the ascent that follows it.  On kStepDone the ray's
-// result is s.best.  The records of both children are fetched together with
-// their boxes, so descending costs one dependent memory round trip per level.
+// Entering node s.node.  A leaf (reached as the root or as a far child)
+// becomes a pending test.  A branch tests both child boxes; the records of
+// both children are fetched together with their boxes, so descending costs
+// one dependent memory round trip per level.  A near leaf becomes a pending
+// test with the far child (if its box is hit) parked in s.node/left/right.
 // A malformed tree (child index out of range, or more node entries than the
 // tree has nodes) finishes the ray and sets `bad`.
 template <typename StackT>
-__device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT stack, uint32_t cap, Trav& s,
-                                         bool& bad) {
+__device__ __forceinline__ int phase_inner(const MeshView& m, const Ray& r, StackT stack, uint32_t cap, Trav& s,
+                                           bool& bad) {
   const uint32_t* __restrict__ bn = m.bvhnodes;
   const uint32_t num_node = 2 * m.num_tri - 1;
   if (++s.steps > num_node + 1) {
     bad = true;
-    return kStepDone;
+    return kLaneDone;
   }
-  bool ascend = false;
-  // At most one triangle test per step, issued from one place so that lanes
-  // testing a root / far leaf and lanes testing a near leaf share it.
-  uint32_t leaf_tri = kUMax;
-  bool leaf_near = false, has_far = false;
-  uint32_t nf = 0, f_l = 0, f_r = 0;
-  float far_enter = 0.f;
-  if (s.right == kUMax) {  // a leaf reached as the root or as a far child
-    leaf_tri = s.left;
-  } else {
-    const uint32_t node = s.node, left = s.left, right = s.right;
-    if (left >= num_node || right >= num_node) {
-      bad = true;
-      return kStepDone;
-    }
-    uint32_t ll, lr, rl, rr;
-    load_record(bn, left, ll, lr);
-    load_record(bn, right, rl, rr);
-    float l0 = 0.f, l1 = 0.f, r0 = 0.f, r1 = 0.f;
-    const bool hl = node_slab(m, r, left, l0, l1);
-    const bool hr = node_slab(m, r, right, r0, r1);
-    if (!hl && !hr) {
-      ascend = true;
+  if (s.right == kUMax) {
+    s.leaf_tri = s.left;
+    s.leaf_far = false;
+    return kLaneLeaf;
+  }
+  const uint32_t node = s.node, left = s.left, right = s.right;
+  if (left >= num_node || right >= num_node) {
+    bad = true;
+    return kLaneDone;
+  }
+  uint32_t ll, lr, rl, rr;
+  load_record(bn, left, ll, lr);
+  load_record(bn, right, rl, rr);
+  float l0 = 0.f, l1 = 0.f, r0 = 0.f, r1 = 0.f;
+  const bool hl = node_slab(m, r, left, l0, l1);
+  const bool hr = node_slab(m, r, right, r0, r1);
+  if (!hl && !hr) return kLaneAscend;
+  const bool near_left = (hl && hr) ? tuple_lt(l0, l1, r0, r1) : hl;
+  const uint32_t nn = near_left ? left : right, nf = near_left ? right : left;
+  const uint32_t n_l = near_left ? ll : rl, n_r = near_left ? lr : rr;
+  const bool has_far = hl && hr;
+  const float far_enter = near_left ? r0 : l0;
+  if (n_r == kUMax) {  // near child is a leaf holding triangle n_l
+    s.leaf_tri = n_l;
+    s.leaf_far = has_far;
+    s.far_enter = far_enter;
+    s.node = nf;
+    s.left = near_left ? rl : ll;
+    s.right = near_left ? rr : lr;
+    return kLaneLeaf;
+  }
+  if (has_far) {
+    const bool link = !near_left && left == m.num_tri - 1 + node && right == node + 1;
+    if (link && node == s.chain_next && s.best.id == kUMax) {
+      // extend the chain frame on top: its last link becomes `node`
+      const uint4 f = stack.load(s.sp - 1);
+      stack.store(s.sp - 1, make_uint4(f.x, node, f.z, f.w));
     } else {
-      const bool near_left = (hl && hr) ? tuple_lt(l0, l1, r0, r1) : hl;
-      const uint32_t nn = near_left ? left : right;
-      nf = near_left ? right : left;
-      const uint32_t n_l = near_left ? ll : rl, n_r = near_left ? lr : rr;
-      f_l = near_left ? rl : ll;
-      f_r = near_left ? rr : lr;
-      has_far = hl && hr;
-      far_enter = near_left ? r0 : l0;
-      if (n_r == kUMax) {  // near child is a leaf holding triangle n_l
-        leaf_tri = n_l;
-        leaf_near = true;
-      } else if (!has_far) {
-        s.node = nn;  // R(node) == R(near): no pending decision, no frame
-        s.left = n_l;
-        s.right = n_r;
-      } else {
-        const bool link = !near_left && left == m.num_tri - 1 + node && right == node + 1;
-        if (link && node == s.chain_next && s.best.id == kUMax) {
-          // extend the chain frame on top: its last link becomes `node`
-          const uint4 f = stack.load(s.sp - 1);
-          stack.store(s.sp - 1, make_uint4(f.x, node, f.z, f.w));
-        } else {
-          if (s.sp >= cap) return kStepOverflow;
-          if (link)
-            stack.store(s.sp++, make_uint4(kChainBit | node, node, __float_as_uint(s.best.t), s.best.id));
-          else
-            stack.store(s.sp++, make_uint4(nf, __float_as_uint(far_enter), __float_as_uint(s.best.t), s.best.id));
-        }
-        s.chain_next = link ? node + 1 : kUMax;
-        s.best = Hit{INFINITY, kUMax};
-        s.node = nn;
-        s.left = n_l;
-        s.right = n_r;
-      }
+      if (s.sp >= cap) return kLaneOverflow;
+      if (link)
+        stack.store(s.sp++, make_uint4(kChainBit | node, node, __float_as_uint(s.best.t), s.best.id));
+      else
+        stack.store(s.sp++, make_uint4(nf, __float_as_uint(far_enter), __float_as_uint(s.best.t), s.best.id));
     }
+    s.chain_next = link ? node + 1 : kUMax;
+    s.best = Hit{INFINITY, kUMax};
   }
-  if (leaf_tri != kUMax) {
-    float t, u, v;
-    const bool h = leaf_hit(m, r, leaf_tri, t, u, v, bad);
-    if (h) s.best = pick(s.best, Hit{t, leaf_tri});
-    if (!leaf_near || !has_far || (h && far_enter > t)) {
-      ascend = true;
-    } else {  // the far child of a near leaf
-      s.node = nf;
-      s.left = f_l;
-      s.right = f_r;
-    }
-  }
-  if (!ascend) return kStepContinue;
+  // without a far child R(node) == R(near): no pending decision, no frame
+  s.node = nn;
+  s.left = n_l;
+  s.right = n_r;
+  return kLaneInner;
+}
+
+// The pending triangle test.  After a near leaf the far child is searched
+// unless the leaf was hit before the far box is entered (search_bvh3.rs:168-189).
+__device__ __forceinline__ int phase_leaf(const MeshView& m, const Ray& r, Trav& s, bool& bad) {
+  float t, u, v;
+  const bool h = leaf_hit(m, r, s.leaf_tri, t, u, v, bad);
+  if (h) s.best = pick(s.best, Hit{t, s.leaf_tri});
+  if (!s.leaf_far || (h && s.far_enter > t)) return kLaneAscend;
+  return kLaneInner;
+}
+
+// Pops frames until a far child is to be searched (kLaneInner) or the stack
+// is empty (kLaneDone).
+template <typename StackT>
+__device__ __forceinline__ int phase_ascend(const MeshView& m, const Ray& r, StackT stack, Trav& s, bool& bad) {
+  const uint32_t num_node = 2 * m.num_tri - 1;
   s.chain_next = kUMax;
   while (s.sp > 0) {
     const uint4 f = stack.load(s.sp - 1);
@@ -241,7 +259,7 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
       far = m.num_tri - 1 + j;
       if (far >= num_node) {
         bad = true;
-        return kStepDone;
+        return kLaneDone;
       }
       float te = 0.f, tx = 0.f;
       node_slab(m, r, far, te, tx);  // hit when the frame was pushed; same value again
@@ -264,13 +282,24 @@ __device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT
       s.node = far;
       if (s.node >= num_node) {
         bad = true;
-        return kStepDone;
+        return kLaneDone;
       }
-      load_record(bn, s.node, s.left, s.right);
-      return kStepContinue;
+      load_record(m.bvhnodes, s.node, s.left, s.right);
+      return kLaneInner;
     }
   }
-  return kStepDone;
+  return kLaneDone;
+}
+
+// One node entry and everything up to the next one (the phases back to
+// back), for one ray at a time.  On kStepDone the ray's result is s.best.
+template <typename StackT>
+__device__ __forceinline__ int trav_step(const MeshView& m, const Ray& r, StackT stack, uint32_t cap, Trav& s,
+                                         bool& bad) {
+  int st = phase_inner(m, r, stack, cap, s, bad);
+  if (st == kLaneLeaf) st = phase_leaf(m, r, s, bad);
+  if (st == kLaneAscend) st = phase_ascend(m, r, stack, s, bad);
+  return st == kLaneInner ? kStepContinue : (st == kLaneOverflow ? kStepOverflow : kStepDone);
 }
 
 // Barycentrics of a final hit (recomputed once per ray when asked for).
@@ -295,18 +324,34 @@ constexpr int kCastThreads = 128;
 //                                                   false: w is padding, nothing to do
 //   __device__ void write(uint32_t out, const MeshView& m, const Ray& r, const Hit& h) const;
 
-// Persistent warps with per-lane ray refill.  Rays overflowing the on-chip
-// stack go to ovf_list (their work index).  kThreads threads per block and
-// kStack on-chip frames per ray are tuning choices (Tuning); the register
-// bound (64 registers) keeps 2048 resident threads per SM.
+// Thresholds of the phased loop: a phase runs when at least this many lanes
+// of the warp wait for it, or when nothing else can run.
+struct PhaseMins {
+  uint32_t refill, leaf, ascend;
+};
+
+// Persistent warps with per-lane ray refill, run in phases.  Each lane holds
+// one ray in a LaneState; per iteration the warp enters one node in every
+// lane that is at a branch, then runs the triangle tests, then the ascents,
+// then takes new rays for its idle lanes.  The triangle test, the ascent and
+// the refill each happen about once per ray but in some lane nearly every
+// iteration, so running them whenever any lane needs one leaves most lanes
+// idle through them; waiting until `mins` lanes need one runs each for more
+// lanes at once, while the others go on entering nodes.  Every lane still
+// makes the same decisions in the same order, so results do not depend on
+// the thresholds.  Rays overflowing the on-chip stack go to ovf_list (their
+// work index).  kThreads threads per block and kStack on-chip frames per ray
+// are tuning choices (Tuning); the register bound (64 registers) keeps 2048
+// resident threads per SM.
 template <typename Job, int kThreads, int kStack>
 __global__ void __launch_bounds__(kThreads, 65536 / (64 * kThreads)) k_cast_persistent(Job job, uint32_t* work_counter,
                                                                                  uint32_t* ovf_list,
                                                                                  uint32_t* ovf_count,
-                                                                                 uint32_t* status) {
+                                                                                 uint32_t* status, PhaseMins mins) {
   __shared__ float smem[64];
   job.prepare(smem);
   __syncthreads();
+  constexpr uint32_t kAll = 0xffffffffu;
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t lt_mask = (1u << lane) - 1u;
   uint4 frames[kStack];
@@ -315,37 +360,46 @@ __global__ void __launch_bounds__(kThreads, 65536 / (64 * kThreads)) k_cast_pers
   Ray r{};
   Trav s{};
   uint32_t out = 0, work = kUMax;
-  bool active = false, exhausted = false, bad = false;
+  int state = kLaneIdle;
+  bool exhausted = false, bad = false;
   for (;;) {
     // refill idle lanes with consecutive work indices
-    const uint32_t idle = __ballot_sync(0xffffffffu, !active);
-    if (idle != 0u && !exhausted) {
+    const uint32_t idle = __ballot_sync(kAll, state == kLaneIdle);
+    if (idle != 0u && !exhausted && (idle == kAll || static_cast<uint32_t>(__popc(idle)) >= mins.refill)) {
       uint32_t base = 0;
       if (lane == static_cast<uint32_t>(__ffs(idle) - 1)) base = atomicAdd(work_counter, __popc(idle));
-      base = __shfl_sync(0xffffffffu, base, __ffs(idle) - 1);
+      base = __shfl_sync(kAll, base, __ffs(idle) - 1);
       if (base >= job.num_work) exhausted = true;  // warp-uniform
-      if (!active) {
+      if (state == kLaneIdle) {
         const uint32_t w = base + __popc(idle & lt_mask);
         if (w < job.num_work && job.fetch(w, smem, m, r, out)) {
           work = w;
-          if (trav_begin(m, r, s)) active = true;
+          if (trav_begin(m, r, s)) state = kLaneInner;
           else job.write(out, m, r, s.best);
         }
       }
     }
-    if (__all_sync(0xffffffffu, !active)) {
+    if (__all_sync(kAll, state == kLaneIdle)) {
       if (exhausted) break;
       continue;
     }
-    if (active) {
-      const int rc = trav_step(m, r, stack, kStack, s, bad);
-      if (rc == kStepDone) {
-        job.write(out, m, r, s.best);
-        active = false;
-      } else if (rc == kStepOverflow) {
-        ovf_list[atomicAdd(ovf_count, 1u)] = work;
-        active = false;
-      }
+    if (state == kLaneInner) state = phase_inner(m, r, stack, kStack, s, bad);
+    uint32_t inner = __ballot_sync(kAll, state == kLaneInner);
+    const uint32_t leaf = __ballot_sync(kAll, state == kLaneLeaf);
+    if (leaf != 0u && (inner == 0u || static_cast<uint32_t>(__popc(leaf)) >= mins.leaf)) {
+      if (state == kLaneLeaf) state = phase_leaf(m, r, s, bad);
+      inner = __ballot_sync(kAll, state == kLaneInner);
+    }
+    const uint32_t asc = __ballot_sync(kAll, state == kLaneAscend);
+    if (asc != 0u && (inner == 0u || static_cast<uint32_t>(__popc(asc)) >= mins.ascend)) {
+      if (state == kLaneAscend) state = phase_ascend(m, r, stack, s, bad);
+    }
+    if (state == kLaneDone) {
+      job.write(out, m, r, s.best);
+      state = kLaneIdle;
+    } else if (state == kLaneOverflow) {
+      ovf_list[atomicAdd(ovf_count, 1u)] = work;
+      state = kLaneIdle;
     }
   }
   if (bad) raise_status(status, kStatusBadIndex);
@@ -425,8 +479,10 @@ inline void launch_persistent(cudaStream_t s, const Job& job, const CastScratch&
   int grid = persistent_grid<Job, kThreads, kStack>();
   const uint32_t needed = (job.num_work + kThreads - 1) / kThreads;
   if (static_cast<uint32_t>(grid) > needed) grid = static_cast<int>(needed);
+  const Tuning t = get_tuning();
+  const PhaseMins mins{t.cast_refill_min, t.cast_leaf_min, t.cast_ascend_min};
   k_cast_persistent<Job, kThreads, kStack><<<grid, kThreads, 0, s>>>(job, sc.counters, sc.list1, sc.counters + 1,
-                                                                     status);
+                                                                     status, mins);
 }
 
 // The three-tier cast of every work index of `job`.  sc.counters (4 words)

@@ -5,7 +5,10 @@ The choices it sweeps are compiled into the library:
 - the persistent cast's block size and on-chip stack depth (frames per ray
   before the overflow tiers), as (threads, frames) pairs;
 - the pixel tile of one warp (tile_w x 32/tile_w);
-- the radix sort's look-back window (predecessor tiles read per round).
+- the radix sort's look-back window (predecessor tiles read per round);
+- the phase minima of the persistent cast (how many lanes of a warp must
+  wait to take new rays, to test a triangle, or to pop frames before the
+  warp runs that phase), swept at the fastest cast shape.
 
 Every choice gives the same results, and the sweep checks that: each
 candidate's output must equal the default's bit for bit, or the candidate is
@@ -36,7 +39,10 @@ DEFAULT_TABLE = pathlib.Path(__file__).resolve().parent / "tuning.json"
 CAST_CHOICES = [(128, 64), (64, 64), (256, 64), (128, 32), (128, 96)]
 TILE_CHOICES = [4, 8, 16, 32]
 SORT_WINDOWS = [4, 8]
-DEFAULT = dict(cast_threads=128, cast_stack=64, tile_w=8, sort_window=4)
+PHASE_CHOICES = [(1, 1, 1), (4, 4, 4), (6, 6, 6), (8, 8, 8), (4, 8, 8), (6, 8, 8), (8, 6, 6), (12, 8, 8)]
+DEFAULT = dict(cast_threads=128, cast_stack=64, tile_w=8, sort_window=4, cast_refill_min=6, cast_leaf_min=6,
+               cast_ascend_min=6)
+_PHASE_KEYS = ("cast_refill_min", "cast_leaf_min", "cast_ascend_min")
 
 
 def _device_name(device) -> str | None:
@@ -60,7 +66,8 @@ def apply(path=DEFAULT_TABLE, device="cuda:0") -> dict | None:
     if name is None or table.get("device") != name:
         return None
     best = table["best"]
-    _native.set_tuning(best["cast_threads"], best["cast_stack"], best["tile_w"], best["sort_window"])
+    _native.set_tuning(best["cast_threads"], best["cast_stack"], best["tile_w"], best["sort_window"],
+                       *(best.get(k, 0) for k in _PHASE_KEYS))  # 0: the library default
     return best
 
 
@@ -130,29 +137,38 @@ def tune(device="cuda:0", out=DEFAULT_TABLE, reps: int = 15, ndiv: int = 1024, i
     def same_img():
         return bool(torch.equal(p2t, ref_img[0]) and torch.equal(tt.view(torch.int32), ref_img[1]))
 
-    sweep = {"cast": [], "sort": []}
+    sweep = {"cast": [], "sort": [], "phase": []}
+    phase0 = tuple(DEFAULT[k] for k in _PHASE_KEYS)
     for threads, frames in CAST_CHOICES:
         for tile_w in TILE_CHOICES:
-            _native.set_tuning(threads, frames, tile_w, DEFAULT["sort_window"])
+            _native.set_tuning(threads, frames, tile_w, DEFAULT["sort_window"], *phase0)
             for _ in range(3):
                 cast()
             ms = _events_ms(torch, stream, cast, flush, reps)
             sweep["cast"].append(dict(cast_threads=threads, cast_stack=frames, tile_w=tile_w, ms=ms,
                                       identical=same_img()))
     for window in SORT_WINDOWS:
-        _native.set_tuning(DEFAULT["cast_threads"], DEFAULT["cast_stack"], DEFAULT["tile_w"], window)
+        _native.set_tuning(DEFAULT["cast_threads"], DEFAULT["cast_stack"], DEFAULT["tile_w"], window, *phase0)
         for _ in range(3):
             build()
         ms = _events_ms(torch, stream, build, flush, reps)
         sweep["sort"].append(dict(sort_window=window, build_ms=ms, identical=same_tree()))
+    ok_cast = [c for c in sweep["cast"] if c["identical"]]
+    bc = min(ok_cast, key=lambda c: c["ms"])
+    for mins in PHASE_CHOICES:
+        _native.set_tuning(bc["cast_threads"], bc["cast_stack"], bc["tile_w"], DEFAULT["sort_window"], *mins)
+        for _ in range(3):
+            cast()
+        ms = _events_ms(torch, stream, cast, flush, reps)
+        sweep["phase"].append(dict(zip(_PHASE_KEYS, mins), ms=ms, identical=same_img()))
     status = _native.device_status(clear=True)
 
-    ok_cast = [c for c in sweep["cast"] if c["identical"]]
     ok_sort = [c for c in sweep["sort"] if c["identical"]]
-    bc = min(ok_cast, key=lambda c: c["ms"])
+    ok_phase = [c for c in sweep["phase"] if c["identical"]]
     bsrt = min(ok_sort, key=lambda c: c["build_ms"])
+    bph = min(ok_phase, key=lambda c: c["ms"])
     best = dict(cast_threads=bc["cast_threads"], cast_stack=bc["cast_stack"], tile_w=bc["tile_w"],
-                sort_window=bsrt["sort_window"])
+                sort_window=bsrt["sort_window"], **{k: bph[k] for k in _PHASE_KEYS})
     table = {
         "device": torch.cuda.get_device_name(dev),
         "sm_count": torch.cuda.get_device_properties(dev).multi_processor_count,
@@ -166,8 +182,10 @@ def tune(device="cuda:0", out=DEFAULT_TABLE, reps: int = 15, ndiv: int = 1024, i
         "speedup_cast_vs_default": next(c["ms"] for c in sweep["cast"]
                                         if c["cast_threads"] == DEFAULT["cast_threads"]
                                         and c["cast_stack"] == DEFAULT["cast_stack"]
-                                        and c["tile_w"] == DEFAULT["tile_w"]) / bc["ms"],
-        "rejected": [c for c in sweep["cast"] + sweep["sort"] if not c["identical"]],
+                                        and c["tile_w"] == DEFAULT["tile_w"]) / min(bc["ms"], bph["ms"]),
+        "speedup_phase_vs_any_lane": next(c["ms"] for c in sweep["phase"]
+                                          if all(c[k] == 1 for k in _PHASE_KEYS)) / bph["ms"],
+        "rejected": [c for c in sweep["cast"] + sweep["sort"] + sweep["phase"] if not c["identical"]],
         "device_status": status,
         "sweep": sweep,
         "sweep_s": time.time() - start,

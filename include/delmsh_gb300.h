@@ -71,7 +71,14 @@ typedef struct dm_tuning {
   uint32_t cast_stack;   /* on-chip traversal frames per ray before the overflow tiers */
   uint32_t tile_w;       /* pixel tile of one warp is tile_w x (32 / tile_w): 2, 4, 8, 16 or 32 */
   uint32_t sort_window;  /* predecessor tiles read per look-back round of the radix sort: 4 or 8 */
-  uint32_t reserved[4];  /* zero */
+  /* The persistent cast runs a phase (taking new rays / testing triangles /
+     popping frames) once this many of a warp's 32 lanes wait for it, or when
+     nothing else can run: 1..32, 0 = the default (6).  Results do not depend
+     on them. */
+  uint32_t cast_refill_min;
+  uint32_t cast_leaf_min;
+  uint32_t cast_ascend_min;
+  uint32_t reserved;     /* zero */
 } dm_tuning;
 
 /* The current launch parameters. */

@@ -10,17 +10,23 @@ from del_msh_gb300 import workloads as W
 
 def test_tuning_roundtrip_and_validation():
     from del_msh_gb300 import _native
-    from del_msh_gb300.autotune import CAST_CHOICES, DEFAULT, SORT_WINDOWS, TILE_CHOICES
+    from del_msh_gb300.autotune import CAST_CHOICES, DEFAULT, PHASE_CHOICES, SORT_WINDOWS, TILE_CHOICES
     before = _native.get_tuning()
     try:
         for threads, frames in CAST_CHOICES:
             for tile_w in TILE_CHOICES:
                 for window in SORT_WINDOWS:
-                    _native.set_tuning(threads, frames, tile_w, window)
+                    _native.set_tuning(threads, frames, tile_w, window)  # phase minima 0: the default, 6
                     assert _native.get_tuning() == dict(cast_threads=threads, cast_stack=frames, tile_w=tile_w,
-                                                        sort_window=window)
+                                                        sort_window=window, cast_refill_min=6, cast_leaf_min=6,
+                                                        cast_ascend_min=6)
+        for mins in PHASE_CHOICES + [(1, 32, 32), (32, 1, 32), (32, 32, 1)]:
+            _native.set_tuning(128, 64, 8, 4, *mins)
+            assert tuple(_native.get_tuning()[k] for k in ("cast_refill_min", "cast_leaf_min",
+                                                           "cast_ascend_min")) == mins
         _native.set_tuning(**DEFAULT)
-        for bad in [(96, 64, 8, 4), (128, 48, 8, 4), (128, 64, 3, 4), (128, 64, 64, 4), (128, 64, 8, 5)]:
+        for bad in [(96, 64, 8, 4), (128, 48, 8, 4), (128, 64, 3, 4), (128, 64, 64, 4), (128, 64, 8, 5),
+                    (128, 64, 8, 4, 33, 6, 6), (128, 64, 8, 4, 6, 40, 6), (128, 64, 8, 4, 6, 6, 33)]:
             with pytest.raises(_native.DelMshError):
                 _native.set_tuning(*bad)
             assert _native.get_tuning() == DEFAULT  # a rejected choice changes nothing
@@ -43,7 +49,7 @@ def test_apply_ignores_foreign_table(tmp_path):
 def test_every_tuning_choice_matches_oracle(cuda, oracle):
     torch = cuda
     from del_msh_gb300 import _native
-    from del_msh_gb300.autotune import CAST_CHOICES, SORT_WINDOWS, TILE_CHOICES
+    from del_msh_gb300.autotune import CAST_CHOICES, PHASE_CHOICES, SORT_WINDOWS, TILE_CHOICES
     from del_msh_gb300.Pix2Tri import torch as Pix2Tri
     from del_msh_gb300.TriMesh3 import torch as TriMesh3
     tri, vtx = W.displaced_torus(96, seed=11)
@@ -65,6 +71,13 @@ def test_every_tuning_choice_matches_oracle(cuda, oracle):
                 p2t, tt = Pix2Tri.by_raycasting(d_tri, d_vtx, bvh, aabb, m_row, (200, 150), return_depth=True)
                 assert np.array_equal(to_np(p2t, torch), r_p2t), (threads, frames, tile_w)
                 assert np.array_equal(bits(to_np(tt, torch)), bits(r_tt)), (threads, frames, tile_w)
+        # results do not depend on when a warp runs each phase
+        for mins in PHASE_CHOICES + [(1, 32, 32), (32, 1, 32), (32, 32, 1), (32, 32, 32)]:
+            _native.set_tuning(before["cast_threads"], before["cast_stack"], before["tile_w"], before["sort_window"],
+                               *mins)
+            p2t, tt = Pix2Tri.by_raycasting(d_tri, d_vtx, bvh, aabb, m_row, (200, 150), return_depth=True)
+            assert np.array_equal(to_np(p2t, torch), r_p2t), mins
+            assert np.array_equal(bits(to_np(tt, torch)), bits(r_tt)), mins
     finally:
         _native.set_tuning(**before)
     assert _native.device_status(clear=True) == 0
