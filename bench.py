@@ -511,13 +511,13 @@ def run_served(args):
             rate = frac * plain_cap
             reqs, arr = wl.stream(n, rate)
             rays = sum(r.num_ray if r.kind == 2 else r.img_w * r.img_h for r in reqs)
-            s = latency_stats(srv.run_trace(reqs, arr))
+            s = latency_stats(srv.run_trace(reqs, arr), kinds=[r.kind for r in reqs])
             entry = {"offered_rps": rate, "fraction_of_plain_capacity": frac, "served": s,
                      "served_rays_per_s": rays / s["span_s"]}
             if frac <= 0.9:
                 reqs_p, arr_p = wl.stream(min(n, 600), rate)
                 rays_p = sum(r.num_ray if r.kind == 2 else r.img_w * r.img_h for r in reqs_p)
-                p = latency_stats(srv.run_plain(reqs_p, arr_p))
+                p = latency_stats(srv.run_plain(reqs_p, arr_p), kinds=[r.kind for r in reqs_p])
                 entry["plain"] = p
                 entry["plain_rays_per_s"] = rays_p / p["span_s"]
                 entry["served_p99_below_plain_p50"] = s["p99_ms"] < p["p50_ms"]

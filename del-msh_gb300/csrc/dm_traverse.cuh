@@ -337,9 +337,11 @@ struct PhaseMins {
 // the refill each happen about once per ray but in some lane nearly every
 // iteration, so running them whenever any lane needs one leaves most lanes
 // idle through them; waiting until `mins` lanes need one runs each for more
-// lanes at once, while the others go on entering nodes.  Every lane still
-// makes the same decisions in the same order, so results do not depend on
-// the thresholds.  Rays overflowing the on-chip stack go to ovf_list (their
+// lanes at once, while the others go on entering nodes.  Once the warp's
+// refill finds no more work, a waiting lane would only lengthen the warp's
+// longest ray, so from then on every phase runs whenever a lane needs it.
+// Every lane still makes the same decisions in the same order, so results do
+// not depend on the thresholds.  Rays overflowing the on-chip stack go to ovf_list (their
 // work index).  kThreads threads per block and kStack on-chip frames per ray
 // are tuning choices (Tuning); the register bound (64 registers) keeps 2048
 // resident threads per SM.
@@ -369,7 +371,7 @@ __global__ void __launch_bounds__(kThreads, 65536 / (64 * kThreads)) k_cast_pers
       uint32_t base = 0;
       if (lane == static_cast<uint32_t>(__ffs(idle) - 1)) base = atomicAdd(work_counter, __popc(idle));
       base = __shfl_sync(kAll, base, __ffs(idle) - 1);
-      if (base >= job.num_work) exhausted = true;  // warp-uniform
+      if (base + __popc(idle) >= job.num_work) exhausted = true;  // warp-uniform: no work after this
       if (state == kLaneIdle) {
         const uint32_t w = base + __popc(idle & lt_mask);
         if (w < job.num_work && job.fetch(w, smem, m, r, out)) {
@@ -383,15 +385,16 @@ __global__ void __launch_bounds__(kThreads, 65536 / (64 * kThreads)) k_cast_pers
       if (exhausted) break;
       continue;
     }
+    const uint32_t leaf_min = exhausted ? 1u : mins.leaf, ascend_min = exhausted ? 1u : mins.ascend;
     if (state == kLaneInner) state = phase_inner(m, r, stack, kStack, s, bad);
     uint32_t inner = __ballot_sync(kAll, state == kLaneInner);
     const uint32_t leaf = __ballot_sync(kAll, state == kLaneLeaf);
-    if (leaf != 0u && (inner == 0u || static_cast<uint32_t>(__popc(leaf)) >= mins.leaf)) {
+    if (leaf != 0u && (inner == 0u || static_cast<uint32_t>(__popc(leaf)) >= leaf_min)) {
       if (state == kLaneLeaf) state = phase_leaf(m, r, s, bad);
       inner = __ballot_sync(kAll, state == kLaneInner);
     }
     const uint32_t asc = __ballot_sync(kAll, state == kLaneAscend);
-    if (asc != 0u && (inner == 0u || static_cast<uint32_t>(__popc(asc)) >= mins.ascend)) {
+    if (asc != 0u && (inner == 0u || static_cast<uint32_t>(__popc(asc)) >= ascend_min)) {
       if (state == kLaneAscend) state = phase_ascend(m, r, stack, s, bad);
     }
     if (state == kLaneDone) {

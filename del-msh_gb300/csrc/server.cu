@@ -7,8 +7,12 @@
 // the device-memory budget.  Admitted requests run concurrently, one per
 // slot, so requests arriving while others are on the GPU are admitted as
 // slots and memory free up and their work overlaps on the device.  Work on
-// one mesh is ordered across slots by the mesh's completion event; a host
-// callback completes each request (latency timestamps on the steady clock).
+// one mesh is ordered across slots by the mesh's completion event.  A
+// completion thread polls the slots' events while requests are in flight
+// (and sleeps otherwise), so a finished request is seen within microseconds;
+// a host-function callback in the stream would add the driver's callback
+// thread to every request's latency.  Latency timestamps are on the steady
+// clock.
 //
 // Results are a pure function of the request, so a request gives the same
 // bits alone or in any mix: a mesh's tree topology is always built from its
@@ -132,6 +136,7 @@ struct Slot {
   float* d_rays = nullptr;  // max_out origins then max_out directions
   uint32_t* d_hit = nullptr;
   float* d_t = nullptr;
+  cudaEvent_t done = nullptr;  // recorded after the slot's current request
   bool busy = false;
 };
 
@@ -160,7 +165,10 @@ struct dm_server {
   std::unordered_map<uint64_t, dm::Job*> jobs;
   uint64_t next_ticket = 1, use_clock = 0;
   std::thread dispatcher;
+  std::thread completer;
+  std::vector<dm::Job*> inflight;  // admitted requests whose work is on the GPU
   bool stop = false;
+  bool stop_completer = false;  // set once the dispatcher has exited
   dm_server_stats stats{};  // guarded by mu, except the two counters below
   std::atomic<uint64_t> builds{0}, refits{0};
 };
@@ -235,17 +243,43 @@ int cast_request(cudaStream_t st, const HostMesh& hm, const DevMesh& m, const dm
   return cudaGetLastError() == cudaSuccess ? DM_OK : DM_ERR_CUDA;
 }
 
-void CUDART_CB on_done(void* p) {
-  Job* j = static_cast<Job*>(p);
-  dm_server* S = j->srv;
-  std::lock_guard<std::mutex> lk(S->mu);
-  j->res.t_done_ns = now_ns();
+// Marks job j finished (status e) at time t; called with the lock held.
+void finish(dm_server* S, Job* j, int e, uint64_t t) {
+  if (e != DM_OK) j->res.status = e;
+  j->res.t_done_ns = t;
   j->done = true;
   S->slots[j->slot].busy = false;
   auto it = S->dev.find(j->req.mesh_id);
   if (it != S->dev.end()) it->second.inflight--;
   S->stats.completed++;
-  S->cv.notify_all();
+}
+
+// Polls the completion events of the requests in flight.
+void complete_loop(dm_server* S) {
+  cudaSetDevice(S->device);
+  std::vector<Job*> pending;
+  std::vector<std::pair<Job*, int>> finished;
+  std::unique_lock<std::mutex> lk(S->mu);
+  for (;;) {
+    S->cv.wait(lk, [&] { return S->stop_completer || !S->inflight.empty(); });
+    if (S->inflight.empty()) break;  // stopping, and nothing left in flight
+    pending = S->inflight;
+    lk.unlock();
+    finished.clear();
+    for (Job* j : pending) {
+      const cudaError_t e = cudaEventQuery(S->slots[j->slot].done);
+      if (e != cudaErrorNotReady) finished.emplace_back(j, e == cudaSuccess ? DM_OK : DM_ERR_CUDA);
+    }
+    const uint64_t t = now_ns();
+    if (finished.empty()) std::this_thread::yield();
+    lk.lock();
+    if (finished.empty()) continue;
+    for (auto& f : finished) {
+      S->inflight.erase(std::find(S->inflight.begin(), S->inflight.end(), f.first));
+      finish(S, f.first, f.second, t);
+    }
+    S->cv.notify_all();
+  }
 }
 
 int free_slot(dm_server* S) {
@@ -346,29 +380,28 @@ void dispatch_loop(dm_server* S) {
     const HostMesh& hm = S->host.at(j->req.mesh_id);
     lk.unlock();
     // Only this thread changes mesh state and enqueues work, so the mesh
-    // fields below are safe without the lock (on_done only touches inflight).
+    // fields below are safe without the lock (the completion thread only touches inflight).
     const cudaStream_t st = sl.stream;
     int rc = DM_OK;
     if (m->has_last && cudaStreamWaitEvent(st, m->last, 0) != cudaSuccess) rc = DM_ERR_CUDA;
     if (rc == DM_OK) rc = prepare_mesh(st, hm, *m, j->req.kind, j->req.frame, j->req.deform_amplitude, sl, S);
     if (rc == DM_OK) rc = cast_request(st, hm, *m, j->req, sl);
     if (rc == DM_OK && cudaEventRecord(m->last, st) != cudaSuccess) rc = DM_ERR_CUDA;
+    if (rc == DM_OK && cudaEventRecord(sl.done, st) != cudaSuccess) rc = DM_ERR_CUDA;
     if (rc == DM_OK) {
       m->has_last = true;
       j->res.status = DM_OK;
-      if (cudaLaunchHostFunc(st, on_done, j) != cudaSuccess) rc = DM_ERR_CUDA;
+    } else {
+      cudaStreamSynchronize(st);
     }
-    if (rc != DM_OK) cudaStreamSynchronize(st);  // never with the lock held: callbacks take it
     lk.lock();
-    if (rc != DM_OK) {
+    if (rc == DM_OK) {
+      S->inflight.push_back(j);
+    } else {
       fill_error(&j->res, rc);
-      j->res.t_done_ns = now_ns();
-      j->done = true;
-      sl.busy = false;
-      m->inflight--;
-      S->stats.completed++;
-      S->cv.notify_all();
+      finish(S, j, rc, now_ns());
     }
+    S->cv.notify_all();
   }
 }
 
@@ -417,6 +450,7 @@ int dm_server_create(int device, size_t budget_bytes, int num_slots, uint32_t ma
     sl.build_bytes = build_scratch_bytes(max_tri);
     sl.cast_bytes = cast_scratch_bytes(max_out, max_tri);
     if (cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess ||
         cudaMalloc(&sl.build_scratch, sl.build_bytes) != cudaSuccess ||
         cudaMalloc(&sl.cast_scratch, sl.cast_bytes) != cudaSuccess ||
         cudaMalloc(reinterpret_cast<void**>(&sl.d_transform), 64) != cudaSuccess ||
@@ -435,6 +469,7 @@ int dm_server_create(int device, size_t budget_bytes, int num_slots, uint32_t ma
     return set_error(DM_ERR_INVALID_ARGUMENT, "budget smaller than the slots' own memory");
   }
   S->dispatcher = std::thread(dispatch_loop, S);
+  S->completer = std::thread(complete_loop, S);
   *out = S;
   return DM_OK;
 }
@@ -556,6 +591,12 @@ int dm_server_destroy(dm_server* S) {
     S->cv.notify_all();
   }
   if (S->dispatcher.joinable()) S->dispatcher.join();
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop_completer = true;
+    S->cv.notify_all();
+  }
+  if (S->completer.joinable()) S->completer.join();
   cudaSetDevice(S->device);
   for (auto& sl : S->slots)
     if (sl.stream) cudaStreamSynchronize(sl.stream);
@@ -570,6 +611,7 @@ int dm_server_destroy(dm_server* S) {
     cudaFree(sl.d_rays);
     cudaFree(sl.d_hit);
     cudaFree(sl.d_t);
+    if (sl.done) cudaEventDestroy(sl.done);
     if (sl.stream) cudaStreamDestroy(sl.stream);
   }
   for (auto& kv : S->host) {

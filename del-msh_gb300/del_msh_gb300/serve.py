@@ -124,14 +124,26 @@ class Server:
         self.close()
 
 
-def latency_stats(results, t_scale=1e-6):
-    """p50 / p99 / mean latency in ms (done - scheduled arrival) and the span."""
+def latency_stats(results, t_scale=1e-6, kinds=None):
+    """p50 / p99 / mean latency in ms (done - scheduled arrival) and the span;
+    with `kinds` (the request kind of each result) also, per kind, the count,
+    p50 / p99 latency and the mean wait before admission."""
     lat = np.array([(r.t_done_ns - r.t_submit_ns) for r in results], np.float64) * t_scale
+    wait = np.array([(r.t_admit_ns - r.t_submit_ns) for r in results], np.float64) * t_scale
     t0 = min(r.t_submit_ns for r in results)
     t1 = max(r.t_done_ns for r in results)
     ok = all(r.status == 0 for r in results)
-    return {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "mean_ms": float(lat.mean()), "span_s": (t1 - t0) * 1e-9, "all_ok": ok}
+    out = {"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+           "mean_ms": float(lat.mean()), "span_s": (t1 - t0) * 1e-9, "all_ok": ok}
+    if kinds is not None:
+        kinds = np.asarray(kinds)
+        out["by_kind"] = {name: {"n": int((kinds == k).sum()),
+                                 "p50_ms": float(np.percentile(lat[kinds == k], 50)),
+                                 "p99_ms": float(np.percentile(lat[kinds == k], 99)),
+                                 "mean_wait_ms": float(wait[kinds == k].mean())}
+                          for k, name in ((BUILD_CAST, "build_cast"), (REFIT_CAST, "refit_cast"),
+                                          (CAST_RAYS, "cast_rays")) if (kinds == k).any()}
+    return out
 
 
 class ServedWorkload:
