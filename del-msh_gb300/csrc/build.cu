@@ -197,12 +197,19 @@ __global__ void __launch_bounds__(kThreads) k_morton_tri(uint32_t num_tri, const
                                                         uint32_t* status) {
   __shared__ float m[16];
   __shared__ uint32_t sh[kHist ? 4 * kRadix : 1];
+  // The mesh is an input of the whole build, so the first centroid's gathers
+  // need not wait for the kernel that computes the transform.
+  const uint32_t i0 = blockIdx.x * kThreads + threadIdx.x;
+  float3 c0 = make_float3(0.f, 0.f, 0.f);
+  if (i0 < num_tri) c0 = tri_centroid(tri2vtx, num_vtx, vtx2xyz, i0, status);
+  pdl_wait();
+  pdl_launch_dependents();
   if (threadIdx.x < 16) m[threadIdx.x] = transform[threadIdx.x];
   if (kHist)
     for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads) sh[i] = 0;
   __syncthreads();
-  for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < num_tri; i += gridDim.x * kThreads) {
-    const float3 c = tri_centroid(tri2vtx, num_vtx, vtx2xyz, i, status);
+  for (uint32_t i = i0; i < num_tri; i += gridDim.x * kThreads) {
+    const float3 c = i == i0 ? c0 : tri_centroid(tri2vtx, num_vtx, vtx2xyz, i, status);
     const float3 q = transform_homogeneous(m, c.x, c.y, c.z);
     const uint32_t code = morton_code3(q.x, q.y, q.z);
     codes[i] = code;
@@ -243,6 +250,8 @@ __global__ void __launch_bounds__(kThreads) k_vtx2morton(uint32_t n, uint32_t nu
 __global__ void __launch_bounds__(kThreads) k_topology(uint32_t n, const uint32_t* __restrict__ c,
                                                       const uint32_t* __restrict__ idx2obj, uint32_t* bvhnodes,
                                                       uint32_t* other_end) {
+  pdl_wait();
+  pdl_launch_dependents();
   const uint32_t ib = blockIdx.x * kThreads + threadIdx.x;
   if (ib >= n - 1) return;
   topology_node(n, Codes32{c}, Objs32{idx2obj}, bvhnodes, ib, other_end);
@@ -420,6 +429,8 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, S
                                                           const float* __restrict__ vtx1_all, float* aabb_all,
                                                           uint32_t* gflags_all, uint32_t* queue, uint32_t capacity,
                                                           uint32_t* height_out, uint32_t* status) {
+  pdl_wait();
+  pdl_launch_dependents();
   // runs only when the range-query refit handed over (NaN) or heights are wanted
   if (*reinterpret_cast<volatile uint32_t*>(queue + 1) == 0u) return;
   extern __shared__ __align__(16) unsigned char win_raw[];
@@ -586,6 +597,8 @@ __global__ void __launch_bounds__(128) k_refit_top(uint32_t total_tri, Segments 
                                                    const uint32_t* __restrict__ bvhnodes_all, float* aabb_all,
                                                    uint32_t* gflags_all, const uint32_t* queue, uint32_t capacity,
                                                    uint32_t* height_out, uint32_t* status) {
+  pdl_wait();
+  pdl_launch_dependents();
   const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t count = __ldcg(queue);
   if (e >= count || e >= capacity) return;
@@ -849,6 +862,8 @@ __global__ void __launch_bounds__(256) k_refit_seg_super(uint32_t total_tri, uin
   __shared__ Box t[2 * kRefitSuper];
   __shared__ Box ttop[2 * kTopSmem];  // the top heap, when it fits
   __shared__ bool s_last;
+  pdl_wait();
+  pdl_launch_dependents();
   if (*reinterpret_cast<volatile uint32_t*>(hdr + 1) != 0u) return;
   const uint32_t sb = blockIdx.x;
   const uint64_t sb_start = static_cast<uint64_t>(sb) << kRefitSuperLog;
@@ -999,6 +1014,8 @@ __global__ void __launch_bounds__(256) k_refit_seg_cross(uint32_t total_tri, Seg
                                                          const uint32_t* __restrict__ other_all, float* aabb_all,
                                                          const uint32_t* hdr, uint32_t* cross_list, SegView v,
                                                          uint32_t* status) {
+  pdl_wait();
+  pdl_launch_dependents();
   const bool climb = *reinterpret_cast<const volatile uint32_t*>(hdr + 1) != 0u;
   uint32_t count = *reinterpret_cast<const volatile uint32_t*>(hdr + 3);
   if (count > total_tri) count = total_tri;
@@ -1032,7 +1049,8 @@ void launch_morton_tri(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx
                        uint32_t* status) {
   const int grid = grid_for(num_tri, kThreads * 8, 152 * 16);
   if (hist)
-    k_morton_tri<true><<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status);
+    launch_pdl(k_morton_tri<true>, dim3(grid), dim3(kThreads), 0, s, num_tri, tri2vtx, num_vtx, vtx2xyz, transform,
+               codes, hist, status);
   else
     k_morton_tri<false><<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, transform, codes, nullptr,
                                                   status);
@@ -1051,9 +1069,14 @@ void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, con
     return;
   }
   const uint32_t grid = (n - 1 + kThreads - 1) / kThreads;
-  k_topology<<<grid, kThreads, 0, s>>>(n, idx2morton, idx2obj, bvhnodes, other_end);
+  launch_pdl(k_topology, dim3(grid), dim3(kThreads), 0, s, n, idx2morton, idx2obj, bvhnodes, other_end);
 }
 
+// The kernels after the first of this sequence are launched with launch_pdl
+// and wait (pdl_wait) before touching their predecessor's data, so each is
+// resident when its predecessor ends.  The first kernel triggers nothing
+// early: measured on GB300, letting the range-query kernels' successors in
+// while its last wave runs made the refit slower (2M triangles: 92 -> 115 us).
 void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
                            const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
                            const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
@@ -1092,24 +1115,24 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   if (seg.tri_off) {
     k_refit_seg_win<true><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
                                                           vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg, status);
-    k_refit_seg_super<<<supers, 256, 0, s>>>(total_tri, queue, wseg, sseg, tseg, top_log);
-    k_refit_seg_cross<true><<<cross_grid, 256, 0, s>>>(total_tri, seg, other_end, aabb, queue, flags, v, status);
-    k_refit_win<true><<<climb_grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
-                                                         vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out,
-                                                         status);
-    k_refit_top<true><<<top_grid, 128, 0, s>>>(total_tri, seg, bvhnodes, aabb, flags, queue, capacity, height_out,
-                                               status);
+    launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
+    launch_pdl(k_refit_seg_cross<true>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb, queue,
+               flags, v, status);
+    launch_pdl(k_refit_win<true>, dim3(climb_grid), dim3(kWinThreads), smem, s, total_tri, seg, num_vtx_single,
+               bvhnodes, other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out, status);
+    launch_pdl(k_refit_top<true>, dim3(top_grid), dim3(128), 0, s, total_tri, seg, bvhnodes, aabb, flags, queue,
+               capacity, height_out, status);
   } else {
     k_refit_seg_win<false><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end,
                                                            tri2vtx, vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg,
                                                            status);
-    k_refit_seg_super<<<supers, 256, 0, s>>>(total_tri, queue, wseg, sseg, tseg, top_log);
-    k_refit_seg_cross<false><<<cross_grid, 256, 0, s>>>(total_tri, seg, other_end, aabb, queue, flags, v, status);
-    k_refit_win<false><<<climb_grid, kWinThreads, smem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
-                                                          vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out,
-                                                          status);
-    k_refit_top<false><<<top_grid, 128, 0, s>>>(total_tri, seg, bvhnodes, aabb, flags, queue, capacity, height_out,
-                                                status);
+    launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
+    launch_pdl(k_refit_seg_cross<false>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb, queue,
+               flags, v, status);
+    launch_pdl(k_refit_win<false>, dim3(climb_grid), dim3(kWinThreads), smem, s, total_tri, seg, num_vtx_single,
+               bvhnodes, other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out, status);
+    launch_pdl(k_refit_top<false>, dim3(top_grid), dim3(128), 0, s, total_tri, seg, bvhnodes, aabb, flags, queue,
+               capacity, height_out, status);
   }
 }
 

@@ -152,10 +152,10 @@ int check_mesh(uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx, cons
 void sort4(cudaStream_t s, uint32_t n, const uint32_t* k0, uint32_t* ak, uint32_t* av, uint32_t* bk, uint32_t* bv,
            uint32_t* ok, uint32_t* ov, uint32_t* hist, uint32_t* counters, uint32_t* lookback, uint32_t* status) {
   const size_t lbw = dm::sort_lookback_words(n, 1);
-  dm::launch_onesweep_u32(s, n, 0, k0, nullptr, ak, av, hist, lookback, counters, status);
-  dm::launch_onesweep_u32(s, n, 8, ak, av, bk, bv, hist + 256, lookback + lbw, counters + 1, status);
-  dm::launch_onesweep_u32(s, n, 16, bk, bv, ak, av, hist + 512, lookback + 2 * lbw, counters + 2, status);
-  dm::launch_onesweep_u32(s, n, 24, ak, av, ok, ov, hist + 768, lookback + 3 * lbw, counters + 3, status);
+  dm::launch_onesweep_u32(s, n, 0, k0, nullptr, ak, av, hist, lookback, counters, status, true);
+  dm::launch_onesweep_u32(s, n, 8, ak, av, bk, bv, hist + 256, lookback + lbw, counters + 1, status, true);
+  dm::launch_onesweep_u32(s, n, 16, bk, bv, ak, av, hist + 512, lookback + 2 * lbw, counters + 2, status, true);
+  dm::launch_onesweep_u32(s, n, 24, ak, av, ok, ov, hist + 768, lookback + 3 * lbw, counters + 3, status, true);
 }
 
 // ev (optional, 5 events): recorded before the first stage and after each of

@@ -21,6 +21,17 @@ enum DeviceStatusBits : uint32_t {
   kStatusSingular = 8u,  // a matrix to invert was singular (the result is NaN)
 };
 
+// Programmatic dependent launch.  A kernel launched with
+// launch_pdl (dm_internal.h) may start while its predecessor in the stream
+// is still running; pdl_wait() returns once the predecessor has completed
+// and its writes are visible (at once for a normal launch).  Each such
+// kernel calls pdl_launch_dependents() only after pdl_wait(), so when the
+// next kernel starts early every kernel before this one has completed: code
+// before pdl_wait() may read results of those, but nothing this kernel's
+// predecessor writes, and may write nothing that it reads.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ void raise_status(uint32_t* status, uint32_t bits) {
   if (status) atomicOr(status, bits);
 }

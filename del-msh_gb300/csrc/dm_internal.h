@@ -118,10 +118,12 @@ void launch_digit_hist_u64(cudaStream_t s, uint32_t n, const uint64_t* keys, int
 
 // One stable onesweep pass (digit at `shift`).  vals_in == nullptr means the
 // values are the input positions (iota).  lookback: sort_num_tiles(n)*256
-// words and tile_counter: 1 word, both zero on entry.
+// words and tile_counter: 1 word, both zero on entry.  With `pdl` the pass
+// may start while the previous kernel runs (launch_pdl): the tile counter and
+// lookback words must have been zeroed before that kernel.
 void launch_onesweep_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in,
                          const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
-                         uint32_t* lookback, uint32_t* tile_counter, uint32_t* status);
+                         uint32_t* lookback, uint32_t* tile_counter, uint32_t* status, bool pdl = false);
 void launch_onesweep_u64(cudaStream_t s, uint32_t n, uint32_t shift, const uint64_t* keys_in,
                          const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
                          uint32_t* lookback, uint32_t* tile_counter, uint32_t* status);
@@ -161,6 +163,25 @@ constexpr uint32_t kCastVariants[][2] = {{128, 64}, {64, 64}, {256, 64}, {128, 3
 Tuning get_tuning();
 bool set_tuning(const Tuning& t);  // false (and nothing changed) for an unsupported choice
 constexpr size_t kFrameBytes = 16;
+
+// Launches `kernel` so that it may start before the previous kernel in the
+// stream has finished (programmatic dependent launch); the kernel must call
+// pdl_wait() (dm_device.cuh) before it touches that kernel's data.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args... args) {
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
 
 struct MeshView {
   uint32_t num_tri;

@@ -417,6 +417,8 @@ __global__ void __launch_bounds__(kCastThreads) k_cast_deep(Job job, const uint3
                                                            uint32_t max_tri, uint32_t* status) {
   __shared__ float smem[64];
   job.prepare(smem);
+  pdl_wait();
+  pdl_launch_dependents();
   __syncthreads();
   const uint32_t num = *count_in;
   if (num == 0) return;
@@ -504,11 +506,12 @@ inline void cast_job(cudaStream_t s, const Job& job, const CastScratch& sc, uint
   const uint64_t pool_frames = sc.pool_bytes / kFrameBytes;
   uint4* pool = static_cast<uint4*>(sc.pool);
   const uint32_t deep_grid = 152 * 4;
-  k_cast_deep<Job><<<deep_grid, kCastThreads, 0, s>>>(job, sc.list1, sc.counters + 1, sc.list2, sc.counters + 2,
-                                                      pool, pool_frames, 0u, max_tri, status);
+  launch_pdl(k_cast_deep<Job>, dim3(deep_grid), dim3(kCastThreads), 0, s, job, sc.list1, sc.counters + 1, sc.list2,
+             sc.counters + 2, pool, pool_frames, 0u, max_tri, status);
   const uint32_t cap3 = max_tri < 2 ? 2u : max_tri;
-  k_cast_deep<Job><<<deep_grid, kCastThreads, 0, s>>>(job, sc.list2, sc.counters + 2, nullptr, nullptr, pool,
-                                                      pool_frames, cap3, max_tri, status);
+  launch_pdl(k_cast_deep<Job>, dim3(deep_grid), dim3(kCastThreads), 0, s, job, sc.list2, sc.counters + 2,
+             static_cast<uint32_t*>(nullptr), static_cast<uint32_t*>(nullptr), pool, pool_frames, cap3, max_tri,
+             status);
 }
 
 }  // namespace dm

@@ -97,7 +97,11 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 
   for (int i = tid; i < kWarps * kRadix; i += kThreads) (&S.whist[0][0])[i] = 0u;
+  // This pass's tile counter is zeroed before the sort starts and touched by
+  // no other pass, so the ticket may be taken before the previous pass ends.
   if (tid == 0) S.tile = atomicAdd(tile_counter, 1u);
+  pdl_wait();
+  pdl_launch_dependents();
   const uint32_t gb = block_exclusive_scan(__ldg(hist + tid), S.scan);  // has __syncthreads
   S.gbase[tid] = gb;
   const uint32_t tile = S.tile;
@@ -244,7 +248,7 @@ __global__ void __launch_bounds__(kThreads) k_digit_hist(uint32_t n, const KeyT*
 template <typename KeyT, int kWindow>
 void onesweep_w(cudaStream_t s, uint32_t n, uint32_t shift, const KeyT* keys_in, const uint32_t* vals_in,
                 KeyT* keys_out, uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback, uint32_t* tile_counter,
-                uint32_t* status) {
+                uint32_t* status, bool pdl) {
   const size_t smem = sizeof(SortSmem<KeyT>);
   static bool configured[64] = {false};  // the attribute is per device and function
   int dev = 0;
@@ -257,23 +261,24 @@ void onesweep_w(cudaStream_t s, uint32_t n, uint32_t shift, const KeyT* keys_in,
     configured[dev] = true;
   }
   const uint32_t grid = sort_num_tiles(n);
-  if (vals_in == nullptr)
-    k_onesweep<KeyT, true, kWindow><<<grid, kThreads, smem, s>>>(keys_in, nullptr, keys_out, vals_out, n, shift, hist,
-                                                                 lookback, tile_counter, status);
+  auto* kernel = vals_in == nullptr ? k_onesweep<KeyT, true, kWindow> : k_onesweep<KeyT, false, kWindow>;
+  if (pdl)
+    launch_pdl(kernel, dim3(grid), dim3(kThreads), smem, s, keys_in, vals_in, keys_out, vals_out, n, shift, hist,
+               lookback, tile_counter, status);
   else
-    k_onesweep<KeyT, false, kWindow><<<grid, kThreads, smem, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift,
-                                                                  hist, lookback, tile_counter, status);
+    kernel<<<grid, kThreads, smem, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, hist, lookback, tile_counter,
+                                        status);
 }
 
 template <typename KeyT>
 void onesweep(cudaStream_t s, uint32_t n, uint32_t shift, const KeyT* keys_in, const uint32_t* vals_in,
               KeyT* keys_out, uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback, uint32_t* tile_counter,
-              uint32_t* status) {
+              uint32_t* status, bool pdl) {
   if (n == 0) return;
   if (get_tuning().sort_window == 8)
-    onesweep_w<KeyT, 8>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
+    onesweep_w<KeyT, 8>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status, pdl);
   else
-    onesweep_w<KeyT, 4>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
+    onesweep_w<KeyT, 4>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status, pdl);
 }
 
 }  // namespace
@@ -294,14 +299,14 @@ void launch_digit_hist_u64(cudaStream_t s, uint32_t n, const uint64_t* keys, int
 
 void launch_onesweep_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in,
                          const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
-                         uint32_t* lookback, uint32_t* tile_counter, uint32_t* status) {
-  onesweep<uint32_t>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
+                         uint32_t* lookback, uint32_t* tile_counter, uint32_t* status, bool pdl) {
+  onesweep<uint32_t>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status, pdl);
 }
 
 void launch_onesweep_u64(cudaStream_t s, uint32_t n, uint32_t shift, const uint64_t* keys_in,
                          const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
                          uint32_t* lookback, uint32_t* tile_counter, uint32_t* status) {
-  onesweep<uint64_t>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
+  onesweep<uint64_t>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status, false);
 }
 
 }  // namespace dm
