@@ -933,10 +933,43 @@ __global__ void __launch_bounds__(256) k_refit_seg_super(uint32_t total_tri, uin
 
 // One crossing branch (global position g of its index): the segment-tree
 // query over its leaf range.
+__device__ __forceinline__ Box box_shfl_down(const Box& b, uint32_t delta, uint32_t mask) {
+  Box o;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    o.lo[d] = __shfl_down_sync(mask, b.lo[d], delta, 8);
+    o.hi[d] = __shfl_down_sync(mask, b.hi[d], delta, 8);
+  }
+  return o;
+}
+
+// Ordered union over the 8 lanes of a group, lane order ascending (kAsc) or
+// descending; lane 0 of the group gets the result.  box_union keeps its left
+// operand on ties, so the order of the operands is that of the leaves.
+template <bool kAsc>
+__device__ __forceinline__ Box group_union(Box x, uint32_t sub, uint32_t mask) {
+#pragma unroll
+  for (uint32_t off = 1; off < 8; off <<= 1) {
+    const Box y = box_shfl_down(x, off, mask);
+    if ((sub & (2 * off - 1)) == 0) x = kAsc ? box_union(x, y) : box_union(y, x);
+  }
+  return x;
+}
+
+// Box of branch g (global leaf position of its Karras index) whose range
+// crosses a window edge, by 8 lanes: the range [l, r) of leaves is the
+// ragged leaves at both ends (up to 7 each) plus, per level k >= 3 of the
+// segment tree, at most one node on each side.  With L = the first and R =
+// the last-plus-one level-3 index, the iterative walk (if l odd take l++; if
+// r odd take --r; halve) is at level 3+j at l_j = ceil(L / 2^j) and
+// r_j = floor(R / 2^j) while l_j < r_j, so every lane finds its own levels
+// (4 consecutive ones) without walking the others.  In leaf order the pieces
+// are: left ragged leaves, left nodes by ascending level, right nodes by
+// descending level, right ragged leaves.
 template <bool kBatch>
-__device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, const Segments& seg,
-                                                const uint32_t* __restrict__ other_all, float* aabb_all,
-                                                const SegView& v, uint32_t* status) {
+__device__ __forceinline__ void refit_cross_group(uint32_t g, uint32_t sub, uint32_t mask, uint32_t total_tri,
+                                                  const Segments& seg, const uint32_t* __restrict__ other_all,
+                                                  float* aabb_all, const SegView& v, uint32_t* status) {
   uint32_t m = 0, t0 = 0, T = total_tri;
   if (kBatch) {
     m = mesh_of_leaf(seg, g);
@@ -945,89 +978,79 @@ __device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, 
   }
   const uint32_t n = g - t0;
   if (g < t0 || n + 1 >= T) {
-    raise_status(status, kStatusBadIndex);
+    if (sub == 0) raise_status(status, kStatusBadIndex);
     return;
   }
   const uint32_t oth = __ldg(other_all + (static_cast<size_t>(t0) - m) + n);
   const uint32_t lo = n < oth ? n : oth, hi = n < oth ? oth : n;
   if (hi >= T) {
-    raise_status(status, kStatusBadIndex);
+    if (sub == 0) raise_status(status, kStatusBadIndex);
     return;
   }
-  uint32_t l = t0 + lo, r = t0 + hi + 1;
+  const uint32_t l = t0 + lo, r = t0 + hi + 1;
   const float* leaf0 = aabb_all + 6 * (2ull * t0 - m + T - 1) - 6ull * t0;  // + 6*p: leaf of global position p
-  const float* dummy = leaf0 + 6ull * l;
-  Box L = box_identity(), R = box_identity();
-  {  // ragged ends: up to 7 leaves on each side
-    const uint32_t nl = (8u - (l & 7u)) & 7u, nr = r & 7u;
-    Box bl[7], br[7];
+  const uint32_t nl = (8u - (l & 7u)) & 7u, nr = r & 7u;
+  const uint32_t L = (l + nl) >> 3, R = (r - nr) >> 3;
+  const float* pa = sub < nl ? leaf0 + 6ull * (l + sub) : nullptr;
+  const float* pb = sub < nr ? leaf0 + 6ull * (r - nr + sub) : nullptr;
+  const float* pl[4];
+  const float* pr[4];
 #pragma unroll
-    for (int q = 0; q < 7; ++q) {
-      bl[q] = box_load_cg(static_cast<uint32_t>(q) < nl ? leaf0 + 6ull * (l + q) : dummy);
-      br[q] = box_load_cg(static_cast<uint32_t>(q) < nr ? leaf0 + 6ull * (r - 1 - q) : dummy);
-    }
-#pragma unroll
-    for (int q = 0; q < 7; ++q) {
-      if (static_cast<uint32_t>(q) < nl) L = box_union(L, bl[q]);
-      if (static_cast<uint32_t>(q) < nr) R = box_union(br[q], R);
-    }
-    l = (l + nl) >> 3;
-    r = (r - nr) >> 3;
+  for (uint32_t q = 0; q < 4; ++q) {
+    const uint32_t j = 4 * sub + q;
+    const uint32_t lj = static_cast<uint32_t>((static_cast<uint64_t>(L) + (1ull << j) - 1) >> j);
+    const uint32_t rj = static_cast<uint32_t>(static_cast<uint64_t>(R) >> j);
+    const bool act = lj < rj;
+    pl[q] = (act && (lj & 1u)) ? seg_node(v, 3 + j, lj) : nullptr;
+    pr[q] = (act && (rj & 1u)) ? seg_node(v, 3 + j, rj - 1) : nullptr;
   }
-  uint32_t lvl = 3;
-  while (l < r) {
-    const float* pl[4];
-    const float* pr[4];
-    bool tl[4], tr[4];
+  const Box id = box_identity();
+  Box A = pa ? box_load_cg(pa) : id, B = pb ? box_load_cg(pb) : id;
+  Box bl[4], br[4];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      tl[q] = (l < r) && (l & 1u);
-      pl[q] = tl[q] ? seg_node(v, lvl, l) : dummy;
-      if (tl[q]) ++l;
-      tr[q] = (l < r) && (r & 1u);
-      if (tr[q]) --r;
-      pr[q] = tr[q] ? seg_node(v, lvl, r) : dummy;
-      l >>= 1;
-      r >>= 1;
-      ++lvl;
-    }
-    Box bl[4], br[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      bl[q] = box_load_cg(pl[q]);
-      br[q] = box_load_cg(pr[q]);
-    }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (tl[q]) L = box_union(L, bl[q]);
-      if (tr[q]) R = box_union(br[q], R);
-    }
+  for (int q = 0; q < 4; ++q) {
+    bl[q] = pl[q] ? box_load_cg(pl[q]) : id;
+    br[q] = pr[q] ? box_load_cg(pr[q]) : id;
   }
-  box_store(aabb_all + 6 * (2ull * t0 - m + n), box_union(L, R));
+  Box Lp = bl[0], Rp = br[3];
+#pragma unroll
+  for (int q = 1; q < 4; ++q) {
+    Lp = box_union(Lp, bl[q]);      // ascending levels
+    Rp = box_union(Rp, br[3 - q]);  // descending levels
+  }
+  A = group_union<true>(A, sub, mask);
+  Lp = group_union<true>(Lp, sub, mask);
+  Rp = group_union<false>(Rp, sub, mask);
+  B = group_union<true>(B, sub, mask);
+  if (sub == 0) box_store(aabb_all + 6 * (2ull * t0 - m + n), box_union(box_union(A, Lp), box_union(Rp, B)));
 }
 
 // Branches whose range crosses a window edge, from the list the window kernel
-// appended: a global segment-tree query, its loads issued four levels at a
-// time.  Every list entry read is cleared, also when the climb took over.
+// appended, one group of 8 lanes per branch (refit_cross_group).  Every list
+// entry read is cleared, also when the climb took over.
 template <bool kBatch>
-__global__ void __launch_bounds__(256) k_refit_seg_cross(uint32_t total_tri, Segments seg,
-                                                         const uint32_t* __restrict__ other_all, float* aabb_all,
-                                                         const uint32_t* hdr, uint32_t* cross_list, SegView v,
-                                                         uint32_t* status) {
+__global__ void __launch_bounds__(256, 4) k_refit_seg_cross(uint32_t total_tri, Segments seg,
+                                                            const uint32_t* __restrict__ other_all, float* aabb_all,
+                                                            const uint32_t* hdr, uint32_t* cross_list, SegView v,
+                                                            uint32_t* status) {
   pdl_wait();
   pdl_launch_dependents();
   const bool climb = *reinterpret_cast<const volatile uint32_t*>(hdr + 1) != 0u;
   uint32_t count = *reinterpret_cast<const volatile uint32_t*>(hdr + 3);
   if (count > total_tri) count = total_tri;
-  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+  const uint32_t sub = threadIdx.x & 7u;
+  const uint32_t mask = 0xffu << (threadIdx.x & 24u);  // the group's lanes in the warp
+  const uint32_t groups = (gridDim.x * blockDim.x) >> 3;
+  for (uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; e < count; e += groups) {
     const uint32_t entry = cross_list[e];
-    cross_list[e] = 0u;
+    __syncwarp(mask);
+    if (sub == 0) cross_list[e] = 0u;
     if (climb) continue;
     if (entry == 0u || entry > total_tri) {
-      raise_status(status, kStatusBadIndex);
+      if (sub == 0) raise_status(status, kStatusBadIndex);
       continue;
     }
-    refit_cross_one<kBatch>(entry - 1, total_tri, seg, other_all, aabb_all, v, status);
+    refit_cross_group<kBatch>(entry - 1, sub, mask, total_tri, seg, other_all, aabb_all, v, status);
   }
 }
 
@@ -1107,7 +1130,7 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   if (height_out) cudaMemsetAsync(queue + 1, 1, sizeof(uint32_t), s);  // heights come from the climb
   const uint32_t top_grid = (capacity + 127) / 128;
   // persistent grids: the crossing list is short, and the climb usually exits at once
-  const uint32_t cross_grid = std::min<uint32_t>((total_tri + 255) / 256, sms * 2);
+  const uint32_t cross_grid = std::min<uint32_t>((total_tri + 31) / 32, sms * 8);  // 32 branches per block
   const uint32_t climb_grid = std::min<uint32_t>(windows, sms * 6);
   float* wseg = const_cast<float*>(v.wseg);
   float* sseg = const_cast<float*>(v.sseg);
