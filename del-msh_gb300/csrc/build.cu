@@ -99,7 +99,8 @@ __device__ __forceinline__ MinMax block_reduce_mm(MinMax v, MinMax* sh /* [kThre
 __global__ void __launch_bounds__(kThreads) k_centroid_aabb(uint32_t num_tri, const uint32_t* __restrict__ tri2vtx,
                                                            uint32_t num_vtx, const float* __restrict__ vtx2xyz,
                                                            float* partials, uint32_t* ticket, float* aabb_out,
-                                                           float* transform_out, uint32_t* status) {
+                                                           float* transform_out, uint32_t* status, float* cent,
+                                                           size_t stride) {
   __shared__ MinMax sh[kThreads / 32];
   __shared__ bool s_last;
   MinMax v;
@@ -110,6 +111,11 @@ __global__ void __launch_bounds__(kThreads) k_centroid_aabb(uint32_t num_tri, co
   }
   for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < num_tri; i += gridDim.x * kThreads) {
     const float3 c = tri_centroid(tri2vtx, num_vtx, vtx2xyz, i, status);
+    if (cent) {
+      cent[i] = c.x;
+      cent[stride + i] = c.y;
+      cent[2 * stride + i] = c.z;
+    }
     const float cc[3] = {c.x, c.y, c.z};
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -194,14 +200,15 @@ __global__ void __launch_bounds__(kThreads) k_morton_tri(uint32_t num_tri, const
                                                         uint32_t num_vtx, const float* __restrict__ vtx2xyz,
                                                         const float* __restrict__ transform,
                                                         uint32_t* __restrict__ codes, uint32_t* __restrict__ hist,
-                                                        uint32_t* status) {
+                                                        uint32_t* status, const float* cent, size_t stride) {
   __shared__ float m[16];
   __shared__ uint32_t sh[kHist ? 4 * kRadix : 1];
-  // The mesh is an input of the whole build, so the first centroid's gathers
-  // need not wait for the kernel that computes the transform.
+  // The mesh is an input of the whole build, so without stored centroids the
+  // first centroid's gathers need not wait for the kernel that computes the
+  // transform.
   const uint32_t i0 = blockIdx.x * kThreads + threadIdx.x;
   float3 c0 = make_float3(0.f, 0.f, 0.f);
-  if (i0 < num_tri) c0 = tri_centroid(tri2vtx, num_vtx, vtx2xyz, i0, status);
+  if (!cent && i0 < num_tri) c0 = tri_centroid(tri2vtx, num_vtx, vtx2xyz, i0, status);
   pdl_wait();
   pdl_launch_dependents();
   if (threadIdx.x < 16) m[threadIdx.x] = transform[threadIdx.x];
@@ -209,7 +216,8 @@ __global__ void __launch_bounds__(kThreads) k_morton_tri(uint32_t num_tri, const
     for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads) sh[i] = 0;
   __syncthreads();
   for (uint32_t i = i0; i < num_tri; i += gridDim.x * kThreads) {
-    const float3 c = i == i0 ? c0 : tri_centroid(tri2vtx, num_vtx, vtx2xyz, i, status);
+    const float3 c = cent ? make_float3(cent[i], cent[stride + i], cent[2 * stride + i])
+                          : (i == i0 ? c0 : tri_centroid(tri2vtx, num_vtx, vtx2xyz, i, status));
     const float3 q = transform_homogeneous(m, c.x, c.y, c.z);
     const uint32_t code = morton_code3(q.x, q.y, q.z);
     codes[i] = code;
@@ -1061,22 +1069,22 @@ __global__ void __launch_bounds__(256, 4) k_refit_seg_cross(uint32_t total_tri, 
 
 void launch_centroid_aabb(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
                           const float* vtx2xyz, float* partials, uint32_t* ticket, float* aabb_out,
-                          float* transform_out, uint32_t* status) {
+                          float* transform_out, uint32_t* status, float* cent, size_t stride) {
   const int grid = grid_for(num_tri, kThreads * 8, kAabbBlocks);
   k_centroid_aabb<<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, partials, ticket, aabb_out,
-                                            transform_out, status);
+                                            transform_out, status, cent, stride);
 }
 
 void launch_morton_tri(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
                        const float* vtx2xyz, const float* transform, uint32_t* codes, uint32_t* hist,
-                       uint32_t* status) {
+                       uint32_t* status, const float* cent, size_t stride) {
   const int grid = grid_for(num_tri, kThreads * 8, 152 * 16);
   if (hist)
     launch_pdl(k_morton_tri<true>, dim3(grid), dim3(kThreads), 0, s, num_tri, tri2vtx, num_vtx, vtx2xyz, transform,
-               codes, hist, status);
+               codes, hist, status, cent, stride);
   else
     k_morton_tri<false><<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, transform, codes, nullptr,
-                                                  status);
+                                                  status, cent, stride);
 }
 
 void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float* vtx2co, const float* transform,

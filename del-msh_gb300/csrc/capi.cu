@@ -186,9 +186,14 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   uint32_t* height = at<uint32_t>(base, L.height);
 
   if (ev) DM_CUDA(cudaEventRecord(ev[0], s));
+  // the centroids are kept (x, y, z in the sort's A keys / A values / B
+  // values, idle until the sort) so that the Morton pass does not gather the
+  // vertices again
+  float* cent = at<float>(base, L.akeys);
+  const size_t cstride = (L.avals - L.akeys) / 4;
   dm::launch_centroid_aabb(s, T, tri2vtx, num_vtx, vtx2xyz, at<float>(base, L.partials),
-                           at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status);
-  dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status);
+                           at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status, cent, cstride);
+  dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status, cent, cstride);
   if (tri2morton_out) DM_CUDA(cudaMemcpyAsync(tri2morton_out, codes, size_t{4} * T, cudaMemcpyDeviceToDevice, s));
   // codes -> (ak, av) -> (codes, bv) -> (ak, av) -> (ok, ov): the codes are
   // dead after pass 0, so they hold the pass-1 keys and, by default, the final

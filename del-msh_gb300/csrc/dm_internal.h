@@ -23,16 +23,20 @@ constexpr int kAabbBlocks = 1024;  // upper bound on centroid-AABB reduction blo
 
 // Centroid AABB (vtx2xyz.rs:19-37 over elem2center) and the fit transform
 // (16 floats, column-major).  partials: kAabbBlocks*6 floats; ticket: one u32
-// that is zero on entry and left zero.
+// that is zero on entry and left zero.  With cent != nullptr the centroids
+// are also stored, x, y and z each as num_tri floats (cent, cent + stride,
+// cent + 2 * stride).
 void launch_centroid_aabb(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
                           const float* vtx2xyz, float* partials, uint32_t* ticket, float* aabb_out,
-                          float* transform_out, uint32_t* status);
+                          float* transform_out, uint32_t* status, float* cent = nullptr, size_t stride = 0);
 
 // Triangle-centroid Morton codes; when hist != nullptr also accumulates the
-// four 8-bit digit histograms (u32[4][256], zeroed by the caller).
+// four 8-bit digit histograms (u32[4][256], zeroed by the caller).  With
+// cent != nullptr the centroids are read from there (launch_centroid_aabb's
+// layout) instead of being recomputed.
 void launch_morton_tri(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
                        const float* vtx2xyz, const float* transform, uint32_t* codes, uint32_t* hist,
-                       uint32_t* status);
+                       uint32_t* status, const float* cent = nullptr, size_t stride = 0);
 
 // mortons.cu:8-37 semantics with the CPU's clamping (num_dim 2 or 3).
 void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float* vtx2co, const float* transform,
