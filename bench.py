@@ -344,10 +344,59 @@ def run_ours(args):
         e2e_step()
         e_ev[k][1].record(stream)
     barrier()
-    e2e_ms = statistics.mean(a.elapsed_time(b) for a, b in e_ev)
+    e2e_serial_ms = statistics.mean(a.elapsed_time(b) for a, b in e_ev)
     ok = bool(np.array_equal(h_p2t.numpy(), pix2tri.cpu().numpy()))
 
-    step_ms, e2e_ms, build_mean, cast_mean = reduce_max_over_ranks(pg, [step_ms, e2e_ms, build_mean, cast_mean], dev)
+    # The same calls as a serving loop runs them back to back: step k+1's
+    # upload (copy stream) overlaps step k's build + cast (compute stream),
+    # and step k's download (a second copy stream) overlaps step k+1.  Device
+    # inputs and pinned outputs are double-buffered; every step still copies
+    # its whole mesh in and its whole image out inside the timed region.
+    s_in, s_out = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+    p_tri = [e_tri, torch.empty_like(e_tri)]
+    p_vtx = [e_vtx, torch.empty_like(e_vtx)]
+    p_hp = [h_p2t, torch.empty_like(h_p2t).pin_memory()]
+    p_ht = [h_tt, torch.empty_like(h_tt).pin_memory()]
+    consumed = [torch.cuda.Event(), torch.cuda.Event()]  # compute finished with input buffer b
+
+    def pipelined(steps):
+        ev_start, ev_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev_start.record(stream)
+        s_in.wait_event(ev_start)
+        for k in range(steps):
+            b = k & 1
+            with torch.cuda.stream(s_in):
+                if k >= 2:
+                    s_in.wait_event(consumed[b])
+                p_tri[b].copy_(h_tri, non_blocking=True)
+                p_vtx[b].copy_(h_vtx, non_blocking=True)
+                uploaded = torch.cuda.Event()
+                uploaded.record(s_in)
+            stream.wait_event(uploaded)
+            t_tri = p_tri[b].view(torch.uint32)
+            b2, a2 = TriMesh3.make_bvhnodes_bvhnode2aabb(t_tri, p_vtx[b])
+            p2, t2 = Pix2Tri.by_raycasting(t_tri, p_vtx[b], b2, a2, m_row, (IMG_W, IMG_H), return_depth=True)
+            consumed[b].record(stream)
+            computed = torch.cuda.Event()
+            computed.record(stream)
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(computed)
+                p_hp[b].copy_(p2.view(torch.int32), non_blocking=True)
+                p_ht[b].copy_(t2, non_blocking=True)
+                p2.record_stream(s_out)
+                t2.record_stream(s_out)
+        ev_end.record(s_out)
+        ev_end.synchronize()
+        return ev_start.elapsed_time(ev_end) / steps
+
+    pipelined(3)
+    barrier()
+    e2e_ms = pipelined(args.steps)
+    barrier()
+    ok = ok and bool(np.array_equal(p_hp[(args.steps - 1) & 1].numpy(), pix2tri.cpu().numpy()))
+
+    step_ms, e2e_ms, e2e_serial_ms, build_mean, cast_mean = reduce_max_over_ranks(
+        pg, [step_ms, e2e_ms, e2e_serial_ms, build_mean, cast_mean], dev)
     if rank != 0:
         if pg is not None:
             pg.destroy_process_group()
@@ -375,7 +424,12 @@ def run_ours(args):
                            "algorithmic_bytes": nbytes["build"]},
         "e2e": {"value": job_throughput(world, R, e2e_ms), "unit": UNIT,
                 "h2d_bytes_per_step": int(tri.nbytes + vtx.nbytes), "d2h_bytes_per_step": int(8 * R),
-                "ms_per_step": e2e_ms, "api": "TriMesh3.torch + Pix2Tri.torch", "matches_device_run": ok},
+                "ms_per_step": e2e_ms, "api": "TriMesh3.torch + Pix2Tri.torch", "matches_device_run": ok,
+                "schedule": "pipelined: step k+1's upload and step k's download (two copy streams) overlap the "
+                            "build + cast (compute stream); inputs and outputs double-buffered; no L2 flush "
+                            "between steps (each step touches ~220 MB, more than the 129 MB L2)",
+                "serial": {"value": job_throughput(world, R, e2e_serial_ms), "ms_per_step": e2e_serial_ms,
+                           "schedule": "upload, build, cast, download on one stream; L2 flushed between steps"}},
         "gpu_launches": args.steps * KERNELS_PER_STEP,
         "tuning": _native.get_tuning(),
         "clocks": clocks,
