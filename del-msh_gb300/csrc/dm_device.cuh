@@ -165,6 +165,25 @@ __device__ __forceinline__ bool slab(const float* __restrict__ box, float3 org, 
   return true;
 }
 
+// slab() for a direction with no zero component: the same operations in the
+// same order, without the per-axis test.
+__device__ __forceinline__ bool slab_nz(const float* __restrict__ box, float3 org, float3 inv, float& te, float& tx) {
+  const float2 a = __ldg(reinterpret_cast<const float2*>(box));
+  const float2 b = __ldg(reinterpret_cast<const float2*>(box) + 1);
+  const float2 c = __ldg(reinterpret_cast<const float2*>(box) + 2);
+  const float x0 = __fmul_rn(__fsub_rn(a.x, org.x), inv.x), x1 = __fmul_rn(__fsub_rn(b.y, org.x), inv.x);
+  const float y0 = __fmul_rn(__fsub_rn(a.y, org.y), inv.y), y1 = __fmul_rn(__fsub_rn(c.x, org.y), inv.y);
+  const float z0 = __fmul_rn(__fsub_rn(b.x, org.z), inv.z), z1 = __fmul_rn(__fsub_rn(c.y, org.z), inv.z);
+  float tmin = fmaxf(-INFINITY, fminf(x0, x1)), tmax = fminf(INFINITY, fmaxf(x0, x1));
+  tmin = fmaxf(tmin, fminf(y0, y1));
+  tmax = fminf(tmax, fmaxf(y0, y1));
+  tmin = fmaxf(tmin, fminf(z0, z1));
+  tmax = fminf(tmax, fmaxf(z0, z1));
+  te = tmin;
+  tx = tmax;
+  return tmin <= tmax && !(tmax < 0.0f);
+}
+
 // Rust's lexicographic `<` on (f32, f32) tuples.
 __device__ __forceinline__ bool tuple_lt(float a0, float a1, float b0, float b1) {
   return (a0 == b0) ? (a1 < b1) : (a0 < b0);

@@ -63,6 +63,7 @@ __device__ __forceinline__ Hit pick(Hit a, Hit b) {
 
 struct Ray {
   float3 org, dir, inv;
+  bool nz;  // no zero direction component: box tests take slab_nz
 };
 
 __device__ __forceinline__ Ray make_ray(float3 o, float3 d) {
@@ -70,6 +71,7 @@ __device__ __forceinline__ Ray make_ray(float3 o, float3 d) {
   r.org = o;
   r.dir = d;
   r.inv = make_float3(__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z));
+  r.nz = d.x != 0.0f && d.y != 0.0f && d.z != 0.0f;
   return r;
 }
 
@@ -94,7 +96,8 @@ __device__ __forceinline__ bool leaf_hit(const MeshView& m, const Ray& r, uint32
 }
 
 __device__ __forceinline__ bool node_slab(const MeshView& m, const Ray& r, uint32_t n, float& te, float& tx) {
-  return slab(m.aabb + static_cast<size_t>(n) * 6, r.org, r.inv, r.dir, te, tx);
+  const float* box = m.aabb + static_cast<size_t>(n) * 6;
+  return r.nz ? slab_nz(box, r.org, r.inv, te, tx) : slab(box, r.org, r.inv, r.dir, te, tx);
 }
 
 struct LocalStack {
