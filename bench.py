@@ -47,7 +47,7 @@ IMG_W, IMG_H = 1920, 1080
 # Morton, 4 sort passes, topology, 5 refit kernels (window, superblock,
 # crossing, and the tree-order climb's two, which exit at once without NaN);
 # cast = persistent traversal + 2 overflow tiers (exit at once when empty)
-KERNELS_PER_STEP = 15
+KERNELS_PER_STEP = 16
 NDIV = 1024
 SEED = 0
 L2_FLUSH_BYTES = 256 << 20

@@ -1033,23 +1033,105 @@ __device__ __forceinline__ void refit_cross_group(uint32_t g, uint32_t sub, uint
   if (sub == 0) box_store(aabb_all + 6 * (2ull * t0 - m + n), box_union(box_union(A, Lp), box_union(Rp, B)));
 }
 
-// Branches whose range crosses a window edge, from the list the window kernel
-// appended, one group of 8 lanes per branch (refit_cross_group).  Every list
-// entry read is cleared, also when the climb took over.
+// One thread per branch: the same query walked level by level, its loads
+// issued four levels at a time.
 template <bool kBatch>
-__global__ void __launch_bounds__(256, 4) k_refit_seg_cross(uint32_t total_tri, Segments seg,
-                                                            const uint32_t* __restrict__ other_all, float* aabb_all,
-                                                            const uint32_t* hdr, uint32_t* cross_list, SegView v,
-                                                            uint32_t* status) {
+__device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, const Segments& seg,
+                                                const uint32_t* __restrict__ other_all, float* aabb_all,
+                                                const SegView& v, uint32_t* status) {
+  uint32_t m = 0, t0 = 0, T = total_tri;
+  if (kBatch) {
+    m = mesh_of_leaf(seg, g);
+    t0 = __ldg(seg.tri_off + m);
+    T = __ldg(seg.tri_off + m + 1) - t0;
+  }
+  const uint32_t n = g - t0;
+  if (g < t0 || n + 1 >= T) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  const uint32_t oth = __ldg(other_all + (static_cast<size_t>(t0) - m) + n);
+  const uint32_t lo = n < oth ? n : oth, hi = n < oth ? oth : n;
+  if (hi >= T) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  uint32_t l = t0 + lo, r = t0 + hi + 1;
+  const float* leaf0 = aabb_all + 6 * (2ull * t0 - m + T - 1) - 6ull * t0;  // + 6*p: leaf of global position p
+  const float* dummy = leaf0 + 6ull * l;
+  Box L = box_identity(), R = box_identity();
+  {  // ragged ends: up to 7 leaves on each side
+    const uint32_t nl = (8u - (l & 7u)) & 7u, nr = r & 7u;
+    Box bl[7], br[7];
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+      bl[q] = box_load_cg(static_cast<uint32_t>(q) < nl ? leaf0 + 6ull * (l + q) : dummy);
+      br[q] = box_load_cg(static_cast<uint32_t>(q) < nr ? leaf0 + 6ull * (r - 1 - q) : dummy);
+    }
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+      if (static_cast<uint32_t>(q) < nl) L = box_union(L, bl[q]);
+      if (static_cast<uint32_t>(q) < nr) R = box_union(br[q], R);
+    }
+    l = (l + nl) >> 3;
+    r = (r - nr) >> 3;
+  }
+  uint32_t lvl = 3;
+  while (l < r) {
+    const float* pl[4];
+    const float* pr[4];
+    bool tl[4], tr[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      tl[q] = (l < r) && (l & 1u);
+      pl[q] = tl[q] ? seg_node(v, lvl, l) : dummy;
+      if (tl[q]) ++l;
+      tr[q] = (l < r) && (r & 1u);
+      if (tr[q]) --r;
+      pr[q] = tr[q] ? seg_node(v, lvl, r) : dummy;
+      l >>= 1;
+      r >>= 1;
+      ++lvl;
+    }
+    Box bl[4], br[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      bl[q] = box_load_cg(pl[q]);
+      br[q] = box_load_cg(pr[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      if (tl[q]) L = box_union(L, bl[q]);
+      if (tr[q]) R = box_union(br[q], R);
+    }
+  }
+  box_store(aabb_all + 6 * (2ull * t0 - m + n), box_union(L, R));
+}
+
+// Branches whose range crosses a window edge, from the list the window kernel
+// appended, in one of two kernels chosen on the device by the list's length.
+// A short list (at most `groups` branches) gets a group of 8 lanes per branch
+// (k_refit_seg_cross_groups, refit_cross_group), which cuts the latency of
+// each query; a long one (runs of equal codes across many windows) one
+// thread per branch (k_refit_seg_cross_threads, refit_cross_one), which costs
+// fewer instructions in all.  Every list entry read is cleared, also when the
+// climb took over.
+template <bool kBatch>
+__global__ void __launch_bounds__(256, 4) k_refit_seg_cross_groups(uint32_t total_tri, Segments seg,
+                                                                   const uint32_t* __restrict__ other_all,
+                                                                   float* aabb_all, const uint32_t* hdr,
+                                                                   uint32_t* cross_list, SegView v, uint32_t groups,
+                                                                   uint32_t* status) {
   pdl_wait();
   pdl_launch_dependents();
   const bool climb = *reinterpret_cast<const volatile uint32_t*>(hdr + 1) != 0u;
   uint32_t count = *reinterpret_cast<const volatile uint32_t*>(hdr + 3);
   if (count > total_tri) count = total_tri;
+  if (count > groups) return;  // the one-thread kernel takes it
   const uint32_t sub = threadIdx.x & 7u;
   const uint32_t mask = 0xffu << (threadIdx.x & 24u);  // the group's lanes in the warp
-  const uint32_t groups = (gridDim.x * blockDim.x) >> 3;
-  for (uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; e < count; e += groups) {
+  const uint32_t stride = (gridDim.x * blockDim.x) >> 3;
+  for (uint32_t e = (blockIdx.x * blockDim.x + threadIdx.x) >> 3; e < count; e += stride) {
     const uint32_t entry = cross_list[e];
     __syncwarp(mask);
     if (sub == 0) cross_list[e] = 0u;
@@ -1059,6 +1141,30 @@ __global__ void __launch_bounds__(256, 4) k_refit_seg_cross(uint32_t total_tri, 
       continue;
     }
     refit_cross_group<kBatch>(entry - 1, sub, mask, total_tri, seg, other_all, aabb_all, v, status);
+  }
+}
+
+template <bool kBatch>
+__global__ void __launch_bounds__(256) k_refit_seg_cross_threads(uint32_t total_tri, Segments seg,
+                                                                 const uint32_t* __restrict__ other_all,
+                                                                 float* aabb_all, const uint32_t* hdr,
+                                                                 uint32_t* cross_list, SegView v, uint32_t groups,
+                                                                 uint32_t* status) {
+  pdl_wait();
+  pdl_launch_dependents();
+  const bool climb = *reinterpret_cast<const volatile uint32_t*>(hdr + 1) != 0u;
+  uint32_t count = *reinterpret_cast<const volatile uint32_t*>(hdr + 3);
+  if (count > total_tri) count = total_tri;
+  if (count <= groups) return;  // the 8-lane kernel took it
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
+    const uint32_t entry = cross_list[e];
+    cross_list[e] = 0u;
+    if (climb) continue;
+    if (entry == 0u || entry > total_tri) {
+      raise_status(status, kStatusBadIndex);
+      continue;
+    }
+    refit_cross_one<kBatch>(entry - 1, total_tri, seg, other_all, aabb_all, v, status);
   }
 }
 
@@ -1139,6 +1245,8 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   const uint32_t top_grid = (capacity + 127) / 128;
   // persistent grids: the crossing list is short, and the climb usually exits at once
   const uint32_t cross_grid = std::min<uint32_t>((total_tri + 31) / 32, sms * 8);  // 32 branches per block
+  const uint32_t cross_groups = cross_grid * 32;
+  const uint32_t cross_grid1 = std::min<uint32_t>((total_tri + 255) / 256, sms * 2);
   const uint32_t climb_grid = std::min<uint32_t>(windows, sms * 6);
   float* wseg = const_cast<float*>(v.wseg);
   float* sseg = const_cast<float*>(v.sseg);
@@ -1147,8 +1255,10 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
     k_refit_seg_win<true><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
                                                           vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg, status);
     launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
-    launch_pdl(k_refit_seg_cross<true>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb, queue,
-               flags, v, status);
+    launch_pdl(k_refit_seg_cross_groups<true>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb,
+               queue, flags, v, cross_groups, status);
+    launch_pdl(k_refit_seg_cross_threads<true>, dim3(cross_grid1), dim3(256), 0, s, total_tri, seg, other_end, aabb,
+               queue, flags, v, cross_groups, status);
     launch_pdl(k_refit_win<true>, dim3(climb_grid), dim3(kWinThreads), smem, s, total_tri, seg, num_vtx_single,
                bvhnodes, other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out, status);
     launch_pdl(k_refit_top<true>, dim3(top_grid), dim3(128), 0, s, total_tri, seg, bvhnodes, aabb, flags, queue,
@@ -1158,8 +1268,10 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
                                                            tri2vtx, vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg,
                                                            status);
     launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
-    launch_pdl(k_refit_seg_cross<false>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb, queue,
-               flags, v, status);
+    launch_pdl(k_refit_seg_cross_groups<false>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb,
+               queue, flags, v, cross_groups, status);
+    launch_pdl(k_refit_seg_cross_threads<false>, dim3(cross_grid1), dim3(256), 0, s, total_tri, seg, other_end, aabb,
+               queue, flags, v, cross_groups, status);
     launch_pdl(k_refit_win<false>, dim3(climb_grid), dim3(kWinThreads), smem, s, total_tri, seg, num_vtx_single,
                bvhnodes, other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out, status);
     launch_pdl(k_refit_top<false>, dim3(top_grid), dim3(128), 0, s, total_tri, seg, bvhnodes, aabb, flags, queue,
