@@ -79,11 +79,12 @@ def peaks():
 def algorithmic_bytes(T: int, V: int, R: int):
     """Compulsory DRAM bytes per launch of each stage (u32/f32 = 4 B)."""
     return {
-        "morton": (12 * T + 12 * V) + (12 * T + 12 * V + 8 * T),  # centroid AABB pass + Morton pass
+        # centroid AABB pass (stores the centroids) + Morton pass (reads them; codes and histograms)
+        "morton": (12 * T + 12 * V + 12 * T) + (12 * T + 8 * T),
         "sort": 68 * T,  # 4T histogram + 4 passes x (8T read + 8T write)
         "topology": 8 * T + 24 * T,
         "refit": 24 * T + 12 * T + 12 * V + 48 * T + 8 * T,
-        "build": 224 * T + 36 * V,
+        "build": 236 * T + 24 * V,
         "cast": 8 * R + 72 * T + 12 * T + 12 * V,  # outputs + one read of tree and mesh
     }
 
