@@ -1245,7 +1245,9 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   const uint32_t top_grid = (capacity + 127) / 128;
   // persistent grids: the crossing list is short, and the climb usually exits at once
   const uint32_t cross_grid = std::min<uint32_t>((total_tri + 31) / 32, sms * 8);  // 32 branches per block
-  const uint32_t cross_groups = cross_grid * 32;
+  // the 8-lane kernel loops over up to 4 rounds of its grid; longer lists
+  // (the 4M soup has 3.2M crossing branches, the 2M torus 41k) take a thread each
+  const uint32_t cross_groups = cross_grid * 32 * 4;
   const uint32_t cross_grid1 = std::min<uint32_t>((total_tri + 255) / 256, sms * 2);
   const uint32_t climb_grid = std::min<uint32_t>(windows, sms * 6);
   float* wseg = const_cast<float*>(v.wseg);
