@@ -822,11 +822,21 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
     if (threadIdx.x == 0) atomicOr(hdr + 1, 1u);  // hand the whole call to the climb
     return;
   }
+  // heap levels of 64..256 nodes by the block, the 5 top levels (32..1
+  // nodes) by warp 0 alone
 #pragma unroll 1
-  for (uint32_t half = kRefitWindow / 2; half >= 1; half >>= 1) {
+  for (uint32_t half = kRefitWindow / 2; half > 32; half >>= 1) {
     for (uint32_t h = half + threadIdx.x; h < 2 * half; h += kWinThreads) tree[h] = box_union(tree[2 * h], tree[2 * h + 1]);
     __syncthreads();
   }
+  if (threadIdx.x < 32) {
+#pragma unroll
+    for (uint32_t half = 32; half >= 1; half >>= 1) {
+      if (threadIdx.x < half) tree[half + threadIdx.x] = box_union(tree[2 * (half + threadIdx.x)], tree[2 * (half + threadIdx.x) + 1]);
+      __syncwarp();
+    }
+  }
+  __syncthreads();
   // heap nodes of 8..512 leaves for the crossing queries
   if (threadIdx.x >= 1 && threadIdx.x < 128) {
     uint32_t lvl, j;
