@@ -193,16 +193,19 @@ __global__ void __launch_bounds__(kThreads) k_centroid_aabb(uint32_t num_tri, co
 }
 
 // Centroid -> transform_homogeneous -> morton_code3 per triangle
-// (bvhnodes_morton.rs:151-159 -> mortons.rs:115-138).  With kHist the four
-// 8-bit digit histograms of the codes are accumulated for the radix sort.
+// (bvhnodes_morton.rs:151-159 -> mortons.rs:115-138).  With kHist the digit
+// histograms of the radix sort are accumulated: three of 10 bits (hist10) or
+// four of 8 bits.
 template <bool kHist>
 __global__ void __launch_bounds__(kThreads) k_morton_tri(uint32_t num_tri, const uint32_t* __restrict__ tri2vtx,
                                                         uint32_t num_vtx, const float* __restrict__ vtx2xyz,
                                                         const float* __restrict__ transform,
                                                         uint32_t* __restrict__ codes, uint32_t* __restrict__ hist,
-                                                        uint32_t* status, const float* cent, size_t stride) {
+                                                        uint32_t* status, const float* cent, size_t stride,
+                                                        bool hist10) {
   __shared__ float m[16];
-  __shared__ uint32_t sh[kHist ? 4 * kRadix : 1];
+  __shared__ uint32_t sh[kHist ? 3 * kRadix10 : 1];
+  const int hist_words = hist10 ? 3 * kRadix10 : 4 * kRadix;
   // The mesh is an input of the whole build, so without stored centroids the
   // first centroid's gathers need not wait for the kernel that computes the
   // transform.
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(kThreads) k_morton_tri(uint32_t num_tri, const
   pdl_launch_dependents();
   if (threadIdx.x < 16) m[threadIdx.x] = transform[threadIdx.x];
   if (kHist)
-    for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads) sh[i] = 0;
+    for (int i = threadIdx.x; i < hist_words; i += kThreads) sh[i] = 0;
   __syncthreads();
   for (uint32_t i = i0; i < num_tri; i += gridDim.x * kThreads) {
     const float3 c = cent ? make_float3(cent[i], cent[stride + i], cent[2 * stride + i])
@@ -223,12 +226,16 @@ __global__ void __launch_bounds__(kThreads) k_morton_tri(uint32_t num_tri, const
     codes[i] = code;
     if (kHist) {
 #pragma unroll
-      for (int p = 0; p < 4; ++p) atomicAdd(&sh[p * kRadix + ((code >> (8 * p)) & 0xFFu)], 1u);
+      if (hist10) {
+        for (int p = 0; p < 3; ++p) atomicAdd(&sh[p * kRadix10 + ((code >> (10 * p)) & 0x3FFu)], 1u);
+      } else {
+        for (int p = 0; p < 4; ++p) atomicAdd(&sh[p * kRadix + ((code >> (8 * p)) & 0xFFu)], 1u);
+      }
     }
   }
   if (kHist) {
     __syncthreads();
-    for (int i = threadIdx.x; i < 4 * kRadix; i += kThreads)
+    for (int i = threadIdx.x; i < hist_words; i += kThreads)
       if (sh[i]) atomicAdd(hist + i, sh[i]);
   }
 }
@@ -1193,14 +1200,14 @@ void launch_centroid_aabb(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2
 
 void launch_morton_tri(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
                        const float* vtx2xyz, const float* transform, uint32_t* codes, uint32_t* hist,
-                       uint32_t* status, const float* cent, size_t stride) {
+                       uint32_t* status, const float* cent, size_t stride, bool hist10) {
   const int grid = grid_for(num_tri, kThreads * 8, 152 * 16);
   if (hist)
     launch_pdl(k_morton_tri<true>, dim3(grid), dim3(kThreads), 0, s, num_tri, tri2vtx, num_vtx, vtx2xyz, transform,
-               codes, hist, status, cent, stride);
+               codes, hist, status, cent, stride, hist10);
   else
     k_morton_tri<false><<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, transform, codes, nullptr,
-                                                  status, cent, stride);
+                                                  status, cent, stride, false);
 }
 
 void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float* vtx2co, const float* transform,

@@ -96,12 +96,12 @@ struct SortLayout {
   size_t hist = 0, counters = 0, lookback = 0, keys = 0, vals = 0, zero_bytes = 0, total = 0;
 };
 
-SortLayout sort_layout(uint32_t n, int num_pass, size_t key_bytes) {
+SortLayout sort_layout(uint32_t n, int num_pass, size_t key_bytes, int radix = dm::kRadix) {
   SortLayout L;
   L.hist = 0;
-  L.counters = 8 * 256 * 4;
+  L.counters = std::max<size_t>(8 * 256, static_cast<size_t>(num_pass) * radix) * 4;
   L.lookback = align256(L.counters + 16 * 4);
-  L.zero_bytes = L.lookback + align256(dm::sort_lookback_words(n, num_pass) * 4);
+  L.zero_bytes = L.lookback + align256(dm::sort_lookback_words(n, num_pass, radix) * 4);
   L.keys = L.zero_bytes;
   L.vals = L.keys + align256(static_cast<size_t>(n) * key_bytes);
   L.total = L.vals + align256(static_cast<size_t>(n) * 4);
@@ -112,6 +112,7 @@ SortLayout sort_layout(uint32_t n, int num_pass, size_t key_bytes) {
 struct BuildLayout {
   size_t transform, aabb, ticket, height, sort_hdr, partials, codes, akeys, avals, bvals, flags, total, zero_bytes,
       sort_bytes;
+  bool radix10;  // three 10-bit passes (dm::kRadix10MaxKeys), else four 8-bit ones
   SortLayout sort;
 };
 
@@ -122,7 +123,8 @@ BuildLayout build_layout(uint32_t T) {
   L.ticket = 96;
   L.height = 100;
   L.sort_hdr = 256;
-  L.sort = sort_layout(T, 4, 4);
+  L.radix10 = T <= dm::kRadix10MaxKeys;
+  L.sort = L.radix10 ? sort_layout(T, 3, 4, dm::kRadix10) : sort_layout(T, 4, 4);
   L.sort_bytes = L.sort.zero_bytes;  // header + lookback (the tmp arrays are carved separately)
   L.zero_bytes = L.sort_hdr + L.sort_bytes;
   L.partials = align256(L.zero_bytes);
@@ -146,6 +148,16 @@ int check_mesh(uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx, cons
   DM_REQUIRE(num_vtx >= 1, "num_vtx must be >= 1");
   DM_REQUIRE(tri2vtx && vtx2xyz, "tri2vtx / vtx2xyz must not be NULL");
   return DM_OK;
+}
+
+// Three 10-bit onesweep passes over 30-bit keys: (k0, iota) -> A -> B -> out.
+void sort3(cudaStream_t s, uint32_t n, const uint32_t* k0, uint32_t* ak, uint32_t* av, uint32_t* bk, uint32_t* bv,
+           uint32_t* ok, uint32_t* ov, uint32_t* hist, uint32_t* counters, uint32_t* lookback, uint32_t* status) {
+  const size_t lbw = dm::sort_lookback_words(n, 1, dm::kRadix10);
+  dm::launch_onesweep10_u32(s, n, 0, k0, nullptr, ak, av, hist, lookback, counters, status);
+  dm::launch_onesweep10_u32(s, n, 10, ak, av, bk, bv, hist + dm::kRadix10, lookback + lbw, counters + 1, status);
+  dm::launch_onesweep10_u32(s, n, 20, bk, bv, ok, ov, hist + 2 * dm::kRadix10, lookback + 2 * lbw, counters + 2,
+                            status);
 }
 
 // The four onesweep passes over 30- or 32-bit keys: (k0, iota) -> A -> B -> A -> out.
@@ -193,17 +205,19 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   const size_t cstride = (L.avals - L.akeys) / 4;
   dm::launch_centroid_aabb(s, T, tri2vtx, num_vtx, vtx2xyz, at<float>(base, L.partials),
                            at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status, cent, cstride);
-  dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status, cent, cstride);
+  dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status, cent, cstride, L.radix10);
   if (tri2morton_out) DM_CUDA(cudaMemcpyAsync(tri2morton_out, codes, size_t{4} * T, cudaMemcpyDeviceToDevice, s));
-  // codes -> (ak, av) -> (codes, bv) -> (ak, av) -> (ok, ov): the codes are
-  // dead after pass 0, so they hold the pass-1 keys and, by default, the final
-  // sorted keys; pass 3 only reads (ak, av).
-  uint32_t* ok = idx2morton_out ? idx2morton_out : codes;
-  uint32_t* ov = idx2tri_out ? idx2tri_out : bv;
+  // 3 passes: codes -> (ak, av) -> (codes, bv) -> (ok, ov), by default the A
+  //   buffers (dead after pass 2); other_end then takes bv.
+  // 4 passes: codes -> (ak, av) -> (codes, bv) -> (ak, av) -> (ok, ov), by
+  //   default (codes, bv) (dead after pass 2); other_end then takes ak.
+  uint32_t* ok = idx2morton_out ? idx2morton_out : (L.radix10 ? ak : codes);
+  uint32_t* ov = idx2tri_out ? idx2tri_out : (L.radix10 ? av : bv);
   if (ev) DM_CUDA(cudaEventRecord(ev[1], s));
-  sort4(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
+  if (L.radix10) sort3(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
+  else sort4(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
   if (ev) DM_CUDA(cudaEventRecord(ev[2], s));
-  uint32_t* other_end = other_end_out ? other_end_out : ak;  // the sort's A buffers are dead after pass 3
+  uint32_t* other_end = other_end_out ? other_end_out : (L.radix10 ? bv : ak);
   dm::launch_topology(s, T, ok, ov, bvhnodes, other_end);
   if (ev) DM_CUDA(cudaEventRecord(ev[3], s));
   // the height is only computed on request: it needs the tree-order climb

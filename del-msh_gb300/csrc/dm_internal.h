@@ -31,12 +31,13 @@ void launch_centroid_aabb(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2
                           float* transform_out, uint32_t* status, float* cent = nullptr, size_t stride = 0);
 
 // Triangle-centroid Morton codes; when hist != nullptr also accumulates the
-// four 8-bit digit histograms (u32[4][256], zeroed by the caller).  With
-// cent != nullptr the centroids are read from there (launch_centroid_aabb's
-// layout) instead of being recomputed.
+// digit histograms of the radix sort (hist10: u32[3][1024] for three 10-bit
+// passes, else u32[4][256]; zeroed by the caller).  With cent != nullptr the
+// centroids are read from there (launch_centroid_aabb's layout) instead of
+// being recomputed.
 void launch_morton_tri(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
                        const float* vtx2xyz, const float* transform, uint32_t* codes, uint32_t* hist,
-                       uint32_t* status, const float* cent = nullptr, size_t stride = 0);
+                       uint32_t* status, const float* cent = nullptr, size_t stride = 0, bool hist10 = false);
 
 // mortons.cu:8-37 semantics with the CPU's clamping (num_dim 2 or 3).
 void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float* vtx2co, const float* transform,
@@ -112,8 +113,8 @@ constexpr int kSortTile = 3840;  // keys per onesweep tile
 constexpr int kRadix = 256;
 
 inline uint32_t sort_num_tiles(uint32_t n) { return (n + kSortTile - 1) / kSortTile; }
-inline size_t sort_lookback_words(uint32_t n, int num_pass) {
-  return static_cast<size_t>(sort_num_tiles(n)) * kRadix * num_pass;
+inline size_t sort_lookback_words(uint32_t n, int num_pass, int radix = kRadix) {
+  return static_cast<size_t>(sort_num_tiles(n)) * radix * num_pass;
 }
 
 // Histogram of num_pass 8-bit digits of 32-bit keys (hist zeroed by caller).
@@ -128,6 +129,18 @@ void launch_digit_hist_u64(cudaStream_t s, uint32_t n, const uint64_t* keys, int
 void launch_onesweep_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in,
                          const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
                          uint32_t* lookback, uint32_t* tile_counter, uint32_t* status, bool pdl = false);
+// A stable pass over a 10-bit digit of u32 keys (1024 digits; hist: 1024
+// words, lookback: sort_lookback_words(n, 1, 1024) words); otherwise as
+// launch_onesweep_u32 with pdl.  Three of them sort 30-bit Morton codes.
+constexpr int kRadix10 = 1024;
+// Builds of up to this many triangles sort in three 10-bit passes: fewer,
+// heavier passes win while a tile's 1024 digit runs are the cost; above it
+// (short runs, scattered writes) four 8-bit passes are faster (measured on
+// GB300: 327k keys 44 vs 61 us, 1.3M keys 107 vs 83 us).
+constexpr uint32_t kRadix10MaxKeys = 1u << 19;
+void launch_onesweep10_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in,
+                           const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
+                           uint32_t* lookback, uint32_t* tile_counter, uint32_t* status);
 void launch_onesweep_u64(cudaStream_t s, uint32_t n, uint32_t shift, const uint64_t* keys_in,
                          const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
                          uint32_t* lookback, uint32_t* tile_counter, uint32_t* status);

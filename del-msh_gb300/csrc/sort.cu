@@ -230,6 +230,232 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
   }
 }
 
+// ---------------------------------------------------------------- 10-bit
+// The same pass over a 10-bit digit of u32 keys (1024 digits), so that three
+// passes sort 30-bit Morton codes.  Each thread owns 4 consecutive digits in
+// the per-digit steps; the per-warp counts are 16-bit (a warp ranks at most
+// 32 * kKpt = 480 keys) and the look-back result is folded with the global
+// base into one offset per digit, which keeps a tile at ~54 KB of shared
+// memory (four tiles per SM, as the 8-bit pass).
+constexpr int kDpt10 = kRadix10 / kThreads;  // digits per thread: 4
+static_assert(kDpt10 == 4, "four digits per thread");
+
+struct SortSmem10 {
+  uint16_t whist[kWarps][kRadix10];  // per-warp digit counts, then per-warp exclusive offsets
+  uint32_t tstart[kRadix10];         // start of each digit inside the tile
+  uint32_t offs[kRadix10];           // global base, then output position minus tile slot
+  uint32_t scan[kWarps];
+  uint32_t tile;
+  uint32_t keys[kSortTile];
+  uint32_t vals[kSortTile];
+};
+
+__device__ __forceinline__ uint32_t digit10(uint32_t k, uint32_t shift) { return (k >> shift) & (kRadix10 - 1); }
+
+__device__ __forceinline__ uint32_t warp_peers10(uint32_t d, bool valid) {
+  uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+  for (int b = 0; b < 10; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const uint32_t bb = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? bb : ~bb;
+  }
+  return peers;
+}
+
+template <bool kIota, int kWindow>
+__global__ void __launch_bounds__(kThreads, 4) k_onesweep10(const uint32_t* __restrict__ keys_in,
+                                                          const uint32_t* __restrict__ vals_in,
+                                                          uint32_t* __restrict__ keys_out,
+                                                          uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift,
+                                                          const uint32_t* __restrict__ hist, uint32_t* lookback,
+                                                          uint32_t* tile_counter, uint32_t* status) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SortSmem10& S = *reinterpret_cast<SortSmem10*>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+
+  {
+    uint32_t* w = reinterpret_cast<uint32_t*>(&S.whist[0][0]);
+    for (int i = tid; i < kWarps * kRadix10 / 2; i += kThreads) w[i] = 0u;
+  }
+  // This pass's tile counter is zeroed before the sort starts and touched by
+  // no other pass, so the ticket may be taken before the previous pass ends.
+  if (tid == 0) S.tile = atomicAdd(tile_counter, 1u);
+  pdl_wait();
+  pdl_launch_dependents();
+  // global start of digits 4*tid .. 4*tid+3 (scan of the upfront histogram)
+  const uint4 h4 = __ldg(reinterpret_cast<const uint4*>(hist) + tid);
+  const uint32_t hsum = h4.x + h4.y + h4.z + h4.w;
+  {
+    const uint32_t base = block_exclusive_scan(hsum, S.scan);  // has __syncthreads
+    S.offs[4 * tid] = base;
+    S.offs[4 * tid + 1] = base + h4.x;
+    S.offs[4 * tid + 2] = base + h4.x + h4.y;
+    S.offs[4 * tid + 3] = base + h4.x + h4.y + h4.z;
+  }
+  const uint32_t tile = S.tile;
+  const uint32_t tile_base = tile * kSortTile;
+  const uint32_t wbase = tile_base + static_cast<uint32_t>(warp) * 32u * kKpt;
+
+  uint32_t keys[kKpt];
+  uint32_t ranks[kKpt];
+#pragma unroll
+  for (int j = 0; j < kKpt; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    keys[j] = idx < n ? keys_in[idx] : 0u;
+  }
+  // Rank inside the warp in (j, lane) order, i.e. input order.
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint16_t* my_hist = S.whist[warp];
+#pragma unroll
+  for (int j = 0; j < kKpt; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    const bool valid = idx < n;
+    const uint32_t d = digit10(keys[j], shift);
+    const uint32_t peers = warp_peers10(d, valid);
+    const uint32_t before = valid ? my_hist[d] : 0u;
+    __syncwarp();
+    if (valid && lane == __ffs(peers) - 1) my_hist[d] = static_cast<uint16_t>(before + __popc(peers));
+    __syncwarp();
+    ranks[j] = before + __popc(peers & lt_mask);
+  }
+  __syncthreads();
+
+  // Digits 4*tid+q: per-warp exclusive offsets and the tile counts.
+  uint32_t cnt[kDpt10];
+#pragma unroll
+  for (int q = 0; q < kDpt10; ++q) {
+    const uint32_t d = 4 * tid + q;
+    uint32_t c = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) {
+      const uint32_t x = S.whist[w][d];
+      S.whist[w][d] = static_cast<uint16_t>(c);
+      c += x;
+    }
+    cnt[q] = c;
+  }
+  // Publish this tile's counts at once, so that successors looking back find them.
+  volatile uint32_t* lb = lookback + static_cast<size_t>(tile) * kRadix10 + 4 * tid;
+  const uint32_t pflag = tile == 0 ? kFlagInc : kFlagAgg;
+#pragma unroll
+  for (int q = 0; q < kDpt10; ++q) lb[q] = pflag | cnt[q];
+
+  // Tile-local layout, then the scatter into shared memory (as the 8-bit pass).
+  {
+    const uint32_t csum = cnt[0] + cnt[1] + cnt[2] + cnt[3];
+    const uint32_t ts = block_exclusive_scan(csum, S.scan);  // has __syncthreads
+    S.tstart[4 * tid] = ts;
+    S.tstart[4 * tid + 1] = ts + cnt[0];
+    S.tstart[4 * tid + 2] = ts + cnt[0] + cnt[1];
+    S.tstart[4 * tid + 3] = ts + cnt[0] + cnt[1] + cnt[2];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kKpt; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    if (idx < n) {
+      const uint32_t dg = digit10(keys[j], shift);
+      const uint32_t pos = S.tstart[dg] + S.whist[warp][dg] + ranks[j];
+      S.keys[pos] = keys[j];
+      S.vals[pos] = kIota ? idx : vals_in[idx];
+    }
+  }
+
+  // Decoupled look-back for the thread's 4 digits together: predecessor k's 4
+  // words are read as one uint4; a round reads kWindow predecessors and
+  // consumes them in order until every digit has met an inclusive prefix.
+  uint32_t excl[kDpt10] = {0u, 0u, 0u, 0u};
+  if (tile != 0) {
+    bool done[kDpt10] = {false, false, false, false};
+    int64_t k = static_cast<int64_t>(tile) - 1;
+    uint32_t spins = 0;
+    const volatile uint4* lb4 = reinterpret_cast<const volatile uint4*>(lookback) + tid;  // + kRadix10/4 per tile
+    bool all_done = false;
+    while (!all_done && k >= 0) {
+      uint4 v[kWindow];
+#pragma unroll
+      for (int j = 0; j < kWindow; ++j) {
+        if (k - j >= 0) {
+          const volatile uint4* p = lb4 + static_cast<size_t>(k - j) * (kRadix10 / 4);
+          v[j] = make_uint4(p->x, p->y, p->z, p->w);
+        } else {
+          v[j] = make_uint4(kFlagInc, kFlagInc, kFlagInc, kFlagInc);  // below tile 0: never consumed
+        }
+      }
+      bool stalled = false;
+#pragma unroll
+      for (int j = 0; j < kWindow; ++j) {
+        if (all_done || stalled || k < 0) continue;
+        const uint32_t w4[4] = {v[j].x, v[j].y, v[j].z, v[j].w};
+        bool ready = true;
+#pragma unroll
+        for (int q = 0; q < kDpt10; ++q) ready = ready && (done[q] || (w4[q] & ~kValueMask) != 0u);
+        if (!ready) {
+          stalled = true;  // predecessor k not fully published yet: re-read from k
+          continue;
+        }
+        all_done = true;
+#pragma unroll
+        for (int q = 0; q < kDpt10; ++q) {
+          if (done[q]) continue;
+          excl[q] += w4[q] & kValueMask;
+          if ((w4[q] & ~kValueMask) == kFlagInc) done[q] = true;
+          all_done = all_done && done[q];
+        }
+        --k;
+      }
+      if (stalled) {
+        if (++spins > kSpinLimit) {
+          raise_status(status, kStatusSpinTimeout);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kDpt10; ++q) lb[q] = kFlagInc | ((excl[q] + cnt[q]) & kValueMask);
+  }
+  // output position of tile slot i of digit d: base + excl + (i - tstart),
+  // kept as one word (mod 2^32, so the subtraction may wrap)
+#pragma unroll
+  for (int q = 0; q < kDpt10; ++q) {
+    const uint32_t d = 4 * tid + q;
+    S.offs[d] = S.offs[d] + excl[q] - S.tstart[d];
+  }
+  __syncthreads();
+
+  const uint32_t tile_n = (n - tile_base) < static_cast<uint32_t>(kSortTile) ? (n - tile_base) : kSortTile;
+  for (uint32_t i = tid; i < tile_n; i += kThreads) {
+    const uint32_t key = S.keys[i];
+    const uint32_t g = S.offs[digit10(key, shift)] + i;
+    if (g < n) {  // always true unless a look-back wait gave up (status already raised)
+      keys_out[g] = key;
+      vals_out[g] = S.vals[i];
+    }
+  }
+}
+
+template <int kWindow>
+void onesweep10_w(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in, const uint32_t* vals_in,
+                  uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback,
+                  uint32_t* tile_counter, uint32_t* status) {
+  const size_t smem = sizeof(SortSmem10);
+  static bool configured[64] = {false};  // the attribute is per device and function
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !configured[dev]) {
+    cudaFuncSetAttribute(k_onesweep10<true, kWindow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
+    cudaFuncSetAttribute(k_onesweep10<false, kWindow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
+    configured[dev] = true;
+  }
+  auto* kernel = vals_in == nullptr ? k_onesweep10<true, kWindow> : k_onesweep10<false, kWindow>;
+  launch_pdl(kernel, dim3(sort_num_tiles(n)), dim3(kThreads), smem, s, keys_in, vals_in, keys_out, vals_out, n, shift,
+             hist, lookback, tile_counter, status);
+}
+
 template <typename KeyT>
 __global__ void __launch_bounds__(kThreads) k_digit_hist(uint32_t n, const KeyT* __restrict__ keys, int num_pass,
                                                         uint32_t* __restrict__ hist) {
@@ -301,6 +527,16 @@ void launch_onesweep_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint3
                          const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
                          uint32_t* lookback, uint32_t* tile_counter, uint32_t* status, bool pdl) {
   onesweep<uint32_t>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status, pdl);
+}
+
+void launch_onesweep10_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in,
+                           const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
+                           uint32_t* lookback, uint32_t* tile_counter, uint32_t* status) {
+  if (n == 0) return;
+  if (get_tuning().sort_window == 8)
+    onesweep10_w<8>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
+  else
+    onesweep10_w<4>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status);
 }
 
 void launch_onesweep_u64(cudaStream_t s, uint32_t n, uint32_t shift, const uint64_t* keys_in,
