@@ -40,7 +40,9 @@
 // an overflow list and re-cast from scratch by a second kernel whose per-ray
 // stacks are carved from a global pool (capacity chosen on the device from
 // the overflow count), and anything still deeper by a third kernel with
-// capacity num_tri, which no tree can exceed.  Duplicate Morton codes produce
+// capacity num_tri, which no tree can exceed.  Those two keep the top 64
+// frames of each stack in an on-chip ring (RingStack) and only its bottom in
+// the pool.  Duplicate Morton codes produce
 // long chains (a run of k equal codes is a chain of height k), which is where
 // the deeper tiers are used.
 #pragma once
@@ -106,10 +108,33 @@ struct LocalStack {
   __device__ __forceinline__ uint4 load(uint32_t i) const { return p[i]; }
 };
 
-struct GlobalStack {
-  uint4* p;
-  __device__ __forceinline__ void store(uint32_t i, uint4 v) const { __stcg(p + i, v); }
-  __device__ __forceinline__ uint4 load(uint32_t i) const { return __ldcg(p + i); }
+// A ray's stack for the overflow tiers: frames [*lo, sp) live in an on-chip
+// ring of kRing frames, the frames below *lo in the ray's global area.  The
+// traversal only ever reads the top frame and writes the top or the next
+// slot, so a push past the ring spills the ring's oldest frame, and reading a
+// top that has left the ring (the ring is then empty) brings it back.  Deep
+// chains thus push and pop at on-chip latency; only their bottoms go to L2.
+template <int kRing>
+struct RingStack {
+  static_assert((kRing & (kRing - 1)) == 0, "ring size is a power of two");
+  uint4* ring;   // kRing on-chip frames
+  uint4* glob;   // the ray's global frames (capacity: the tier's cap)
+  uint32_t* lo;  // first frame held by the ring
+  __device__ __forceinline__ void store(uint32_t i, uint4 v) const {
+    if (i >= *lo + kRing) {  // a push past the ring: spill its oldest frame
+      __stcg(glob + *lo, ring[*lo & (kRing - 1)]);
+      ++*lo;
+    }
+    if (i >= *lo) ring[i & (kRing - 1)] = v;
+    else __stcg(glob + i, v);
+  }
+  __device__ __forceinline__ uint4 load(uint32_t i) const {
+    if (i >= *lo) return ring[i & (kRing - 1)];
+    const uint4 v = __ldcg(glob + i);
+    ring[i & (kRing - 1)] = v;  // i is the top and the ring is empty: i becomes its only frame
+    *lo = i;
+    return v;
+  }
 };
 
 constexpr uint32_t kChainBit = 0x80000000u;  // frame.x flag of a chain frame (node ids are < 2^31)
@@ -319,6 +344,7 @@ __device__ __forceinline__ void hit_bc(const MeshView& m, const Ray& r, const Hi
 }
 
 constexpr int kCastThreads = 128;
+constexpr int kDeepRing = 64;  // on-chip frames per ray of the overflow tiers
 
 // A Job maps a work index to (mesh, ray, output slot):
 //   uint32_t num_work;                              work indices are 0..num_work-1
@@ -438,9 +464,12 @@ __global__ void __launch_bounds__(kCastThreads) k_cast_deep(Job job, const uint3
   if (slots > threads) slots = threads;
   const uint64_t slot = static_cast<uint64_t>(threadIdx.x) * gridDim.x + blockIdx.x;  // spread over blocks
   if (slot >= slots) return;
-  GlobalStack st{pool + slot * cap};
+  uint4 ring[kDeepRing];
+  uint32_t lo = 0;
+  const RingStack<kDeepRing> st{ring, pool + slot * cap, &lo};
   bool bad = false;
   for (uint64_t k = slot; k < num; k += slots) {
+    lo = 0;
     const uint32_t w = list_in[k];
     MeshView m{};
     Ray r{};
