@@ -105,9 +105,44 @@ def test_build_cfg1_matches_golden(cuda, golden_dir):
     assert _status_clear() == 0
 
 
+def signed_zero_mesh(runs: bool):
+    """Boxes whose extremes tie between -0.0 and +0.0: a box keeps the
+    leftmost extreme (the first vertex of a triangle, the leftmost leaf of a
+    branch), so the bits of every refit path must follow that order.
+    Grid: 262k triangles on the plane z = ±0 with a column at x = ±0 (window
+    heaps, superblocks, 8-lane crossing queries).  Runs: 64 clusters of 10k
+    triangles on the plane x = ±0 whose centroids share Morton codes, so the
+    runs cross many windows (more crossing branches than 8-lane groups: the
+    one-thread crossing kernel)."""
+    if not runs:
+        rng = np.random.default_rng(9)
+        nx, ny = 513, 257
+        gx, gy = np.meshgrid(np.linspace(-1, 1, nx), np.linspace(0, 1, ny), indexing="ij")
+        vtx = np.stack([gx, gy, np.zeros_like(gx)], -1).reshape(-1, 3).astype(np.float32)
+        zero = np.where(rng.random(vtx.shape) < 0.5, np.float32(-0.0), np.float32(0.0)).astype(np.float32)
+        vtx = np.where(vtx == 0, zero, vtx).astype(np.float32)
+        i, j = np.meshgrid(np.arange(nx - 1), np.arange(ny - 1), indexing="ij")
+        v00 = (i * ny + j).ravel()
+        v10, v01, v11 = v00 + ny, v00 + 1, v00 + ny + 1
+        tri = np.stack([np.stack([v00, v10, v11], 1), np.stack([v00, v11, v01], 1)], 1).reshape(-1, 3)
+        return tri.astype(np.uint32), vtx
+    rng = np.random.default_rng(10)
+    k, m = 64, 10_000
+    c = rng.random((k, 1, 2)).astype(np.float32)
+    e = (rng.random((k, m, 1)) * 1e-3).astype(np.float32)
+    y, z = c[..., 0:1], c[..., 1:2]
+    p0 = np.concatenate([np.zeros_like(e), y + e, z + 0 * e], -1)
+    p1 = np.concatenate([np.zeros_like(e), y - e, z + 0 * e], -1)
+    p2 = np.concatenate([np.zeros_like(e), y + 0 * e, z + e], -1)
+    vtx = np.stack([p0, p1, p2], 2).reshape(-1, 3).astype(np.float32)
+    vtx[:, 0] = np.where(rng.random(vtx.shape[0]) < 0.5, np.float32(-0.0), np.float32(0.0))
+    tri = np.arange(vtx.shape[0], dtype=np.uint32).reshape(-1, 3)
+    return tri, vtx
+
+
 @pytest.mark.parametrize("want_height", [True, False])
 @pytest.mark.parametrize("case", ["torus", "soup", "ico", "tiny2", "tiny3", "same_tris", "flat", "nan_vertex",
-                                  "big_window_span"])
+                                  "big_window_span", "signed_zero_grid", "signed_zero_runs"])
 def test_build_matches_oracle(cuda, oracle, case, want_height):
     """Both refits: the tree-order climb (asked for the height) and the range
     queries (no height; NaN in a leaf box hands the call to the climb)."""
@@ -134,6 +169,8 @@ def test_build_matches_oracle(cuda, oracle, case, want_height):
     elif case == "big_window_span":  # > 2^15 leaves: superblock and top heaps, ragged last window
         tri, vtx = W.displaced_torus(190, seed=7)
         tri = tri[:-37]
+    elif case.startswith("signed_zero"):
+        tri, vtx = signed_zero_mesh(case == "signed_zero_runs")
     else:  # all vertices on the plane z = 0
         rng = np.random.default_rng(8)
         vtx = np.concatenate([rng.random((3000, 2)), np.zeros((3000, 1))], 1).astype(np.float32)
