@@ -651,19 +651,33 @@ size_t dm_batch_build_scratch_bytes(uint32_t num_mesh, uint32_t total_tri) {
 
 int dm_batch_trimesh3_build(uint64_t stream_ptr, uint32_t num_mesh, const uint32_t* mesh2tri,
                             const uint32_t* mesh2vtx, uint32_t total_tri, uint32_t total_vtx,
-                            const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t* bvhnodes, float* bvhnode2aabb,
-                            uint32_t* heights, void* scratch, size_t scratch_bytes) {
+                            uint32_t max_tri_per_mesh, const uint32_t* tri2vtx, const float* vtx2xyz,
+                            uint32_t* bvhnodes, float* bvhnode2aabb, uint32_t* heights, void* scratch,
+                            size_t scratch_bytes) {
   if (int e = check_batch(num_mesh, mesh2tri, mesh2vtx, total_tri, total_vtx, tri2vtx, vtx2xyz)) return e;
   DM_REQUIRE(bvhnodes && bvhnode2aabb, "NULL argument");
+  DM_REQUIRE(max_tri_per_mesh >= 1 && max_tri_per_mesh <= total_tri, "max_tri_per_mesh must be in 1..total_tri");
   cudaStream_t s = as_stream(stream_ptr);
   const BatchLayout L = batch_layout(num_mesh, total_tri);
   Scratch sc;
   if (int e = sc.acquire(scratch, scratch_bytes, L.total, s, nullptr)) return e;
   void* base = sc.ptr;
   uint32_t* status = status_ptr();
-  DM_CUDA(cudaMemsetAsync(base, 0, L.zero_bytes, s));
-  DM_CUDA(cudaMemsetAsync(at<char>(base, L.flags), 0, size_t{4} * total_tri, s));
   const dm::Segments seg{num_mesh, mesh2tri, mesh2vtx};
+  DM_CUDA(cudaMemsetAsync(at<char>(base, L.flags), 0, size_t{4} * total_tri, s));
+  if (max_tri_per_mesh <= dm::kSegMaxTri) {
+    // every mesh sorted and linked on chip (the lists reuse the key buffer)
+    uint32_t* seg_counters = at<uint32_t>(base, L.counters) + 8;
+    DM_CUDA(cudaMemsetAsync(seg_counters, 0, 4 * sizeof(uint32_t), s));
+    if (dm::launch_batch_seg_build(s, seg, max_tri_per_mesh, tri2vtx, vtx2xyz, bvhnodes, at<uint32_t>(base, L.other),
+                                   at<uint32_t>(base, L.keys_a), seg_counters, status) != 0)
+      return fail(DM_ERR_CUDA, "fused batch build launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    dm::launch_refit_windowed(s, total_tri, seg, 0, bvhnodes, at<uint32_t>(base, L.other), tri2vtx, vtx2xyz, nullptr,
+                              bvhnode2aabb, at<uint32_t>(base, L.flags), heights, status);
+    DM_CUDA(cudaGetLastError());
+    return DM_OK;
+  }
+  DM_CUDA(cudaMemsetAsync(base, 0, L.zero_bytes, s));
   float* transforms = at<float>(base, L.transforms);
   uint32_t* hist = at<uint32_t>(base, L.hist);
   uint32_t* counters = at<uint32_t>(base, L.counters);

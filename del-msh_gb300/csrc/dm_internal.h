@@ -155,6 +155,16 @@ void launch_batch_morton(cudaStream_t s, uint32_t total_tri, const Segments& seg
                          uint32_t* status);
 void launch_batch_topology(cudaStream_t s, uint32_t total_tri, const Segments& seg, const uint64_t* keys,
                            const uint32_t* vals, uint32_t* bvhnodes, uint32_t* other_end);
+// Batches whose largest mesh has at most this many triangles replace
+// launch_batch_fit .. launch_batch_topology with launch_batch_seg_build: each
+// mesh sorted and linked in on-chip memory by one block or one cluster.
+constexpr uint32_t kSegMaxTri = 65536;
+// lists: num_mesh words; counters: 4 words, zero on entry.  Returns non-zero
+// (nothing launched after the failing launch) if the kernel cannot be
+// launched on this device.
+int launch_batch_seg_build(cudaStream_t s, const Segments& seg, uint32_t max_tri, const uint32_t* tri2vtx,
+                           const float* vtx2xyz, uint32_t* bvhnodes, uint32_t* other, uint32_t* lists,
+                           uint32_t* counters, uint32_t* status);
 
 // ----------------------------------------------------------------- cast.cu
 constexpr int kCastStack = 64;  // default frames of the on-chip (local) traversal stack

@@ -33,20 +33,6 @@ __device__ __forceinline__ uint32_t digit_of(KeyT k, uint32_t shift) {
   return static_cast<uint32_t>(k >> shift) & (kRadix - 1);
 }
 
-// Lanes of the warp holding the same 8-bit digit, among the valid lanes: one
-// ballot per digit bit.  Measured on GB300, this is several times faster than
-// __match_any_sync, which made ranking the longest phase of a pass.
-__device__ __forceinline__ uint32_t warp_peers(uint32_t d, bool valid) {
-  uint32_t peers = __ballot_sync(0xffffffffu, valid);
-#pragma unroll
-  for (int b = 0; b < 8; ++b) {
-    const bool bit = (d >> b) & 1u;
-    const uint32_t bb = __ballot_sync(0xffffffffu, bit);
-    peers &= bit ? bb : ~bb;
-  }
-  return peers;
-}
-
 // Exclusive scan of one value per thread over the 256-thread block.
 __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* s_warp /* kWarps */) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

@@ -46,7 +46,7 @@ _SIGNATURES = {
     "dm_pix2tri_by_raycast": (i32, [u64, u32, u32, vp, vp, u32, vp, u32, vp, vp, vp, vp, vp, sz]),
     "dm_search_bvh3_first_intersection_ray": (i32, [u64, u32, vp, vp, vp, vp, vp, u32, vp, u32, vp, vp, vp, vp, sz]),
     "dm_cast_scratch_bytes": (sz, [u32, u32]),
-    "dm_batch_trimesh3_build": (i32, [u64, u32, vp, vp, u32, u32, vp, vp, vp, vp, vp, vp, sz]),
+    "dm_batch_trimesh3_build": (i32, [u64, u32, vp, vp, u32, u32, u32, vp, vp, vp, vp, vp, vp, sz]),
     "dm_batch_build_scratch_bytes": (sz, [u32, u32]),
     "dm_batch_pix2tri_by_raycast": (i32, [u64, u32, vp, vp, u32, u32, u32, vp, vp, vp, vp, u32, u32, vp, vp, vp, vp,
                                           sz]),

@@ -65,7 +65,7 @@ class MeshBatch:
     def build(self):
         """Builds every mesh's LBVH (asynchronous on the current stream)."""
         _native.call("dm_batch_trimesh3_build", self._stream(), self.num_mesh, self.d_tri_off.data_ptr(),
-                     self.d_vtx_off.data_ptr(), self.total_tri, self.total_vtx, self.tri2vtx.data_ptr(),
+                     self.d_vtx_off.data_ptr(), self.total_tri, self.total_vtx, self.max_tri, self.tri2vtx.data_ptr(),
                      self.vtx2xyz.data_ptr(), self.bvhnodes.data_ptr(), self.bvhnode2aabb.data_ptr(),
                      self.heights.data_ptr() if self.heights is not None else None, self._build_scratch.data_ptr(),
                      self._build_bytes)

@@ -312,11 +312,17 @@ int dm_quad_oct_tree_aggregate(uint64_t stream_ptr, uint32_t num_idx, uint32_t n
  * and casts one mesh per call (TriMesh3/torch.py:233-285, Pix2Tri/torch.py:8-61). */
 
 /* Builds every mesh's LBVH.  heights (optional, device u32[num_mesh]) gets
- * each tree's height. */
+ * each tree's height.  max_tri_per_mesh bounds the largest mesh.  Up to
+ * 65536, each mesh is sorted and linked in on-chip memory by one block or one
+ * cluster of blocks, and a mesh with more triangles than max_tri_per_mesh
+ * raises device status bit 4 and gets a placeholder tree (branch i: leaf i
+ * and branch i+1).  Above 65536, all meshes go through one global sort of
+ * (mesh, code) keys, which has no per-mesh bound. */
 int dm_batch_trimesh3_build(uint64_t stream_ptr, uint32_t num_mesh, const uint32_t* mesh2tri,
                             const uint32_t* mesh2vtx, uint32_t total_tri, uint32_t total_vtx,
-                            const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t* bvhnodes, float* bvhnode2aabb,
-                            uint32_t* heights, void* scratch, size_t scratch_bytes);
+                            uint32_t max_tri_per_mesh, const uint32_t* tri2vtx, const float* vtx2xyz,
+                            uint32_t* bvhnodes, float* bvhnode2aabb, uint32_t* heights, void* scratch,
+                            size_t scratch_bytes);
 size_t dm_batch_build_scratch_bytes(uint32_t num_mesh, uint32_t total_tri);
 
 /* Casts an img_w x img_h image per mesh through that mesh's column-major

@@ -78,3 +78,88 @@ def test_batch_graph_replay_follows_vertex_updates(cuda, oracle):
             r_p2t, _ = oracle.pix2tri(tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"],
                                       ortho_transforms([meshes[m]], margin=0.3)[0], 16, 16)
             assert np.array_equal(got[m], r_p2t), (frame, m)
+
+
+def _soup(n, seed):
+    return W.clustered_soup(n, num_cluster=4, seed=seed)
+
+
+def _torus(nmajor, nminor, seed):
+    tri, vtx = W.torus_zup(1.0, 0.35, nmajor, nminor)
+    rng = np.random.default_rng(seed)
+    return tri, (vtx.astype(np.float64) + rng.uniform(-0.01, 0.01, vtx.shape)).astype(np.float32)
+
+
+def _check_trees(torch, oracle, b, meshes):
+    for m, (tri, vtx) in enumerate(meshes):
+        bvh, aabb = b.mesh_tree(m)
+        ref = oracle.build(tri, vtx)
+        assert np.array_equal(to_np(bvh, torch), ref["bvhnodes"]), m
+        assert np.array_equal(bits(to_np(aabb, torch)), bits(ref["bvhnode2aabb"])), m
+
+
+@pytest.mark.parametrize("sizes", [
+    # largest mesh in (16384, 32768]: clusters of two blocks
+    "pairs",
+    # largest mesh in (32768, 65536]: clusters of four blocks
+    "quads",
+    # largest mesh above 65536: the global (mesh, code) sort
+    "global",
+])
+def test_batch_build_large_meshes_match_oracle(cuda, oracle, sizes):
+    """Meshes at and around the block (16384) and cluster capacities, clustered
+    soups whose runs of equal codes cross block boundaries, and small meshes
+    built by single blocks in the same launch."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.batch import MeshBatch
+    meshes = [W.icosphere(1), _soup(700, 1), _soup(16384, 2), _soup(16385, 3), _torus(128, 64, 4)]
+    if sizes == "pairs":
+        meshes += [_soup(32768, 5), _torus(128, 128, 6), _soup(20000, 7)]
+    elif sizes == "quads":
+        meshes += [_soup(32769, 8), _torus(256, 128, 9), _soup(65536, 10), _soup(50001, 11)]
+    else:
+        meshes += [_soup(70000, 12), _torus(256, 128, 13)]
+    meshes.append((np.array([[0, 1, 2]], np.uint32), np.array([[0, 0, 0], [1, 0, 0], [0, 1, 1]], np.float32)))
+    b = MeshBatch(meshes)
+    b.build()
+    torch.cuda.synchronize()
+    _check_trees(torch, oracle, b, meshes)
+    assert _native.device_status(clear=True) == 0
+
+
+def test_batch_build_understated_max_tri(cuda, oracle):
+    """A mesh above the max_tri_per_mesh the call was given raises status bit 4
+    and gets the documented placeholder tree (branch i: leaf i, branch i + 1),
+    with the boxes of that tree; the other meshes are unaffected."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.batch import MeshBatch
+    meshes = [_soup(3000, 1), _soup(9000, 2), W.icosphere(2)]
+    b = MeshBatch(meshes)
+    b.max_tri = 5000  # understated: mesh 1 has 9000 triangles
+    _native.device_status(clear=True)
+    b.build()
+    torch.cuda.synchronize()
+    assert _native.device_status(clear=True) == 4
+    for m in (0, 2):
+        tri, vtx = meshes[m]
+        bvh, aabb = b.mesh_tree(m)
+        ref = oracle.build(tri, vtx)
+        assert np.array_equal(to_np(bvh, torch), ref["bvhnodes"]), m
+        assert np.array_equal(bits(to_np(aabb, torch)), bits(ref["bvhnode2aabb"])), m
+    T = 9000
+    bvh, aabb = b.mesh_tree(1)
+    bvh, aabb = to_np(bvh, torch).astype(np.int64), to_np(aabb, torch)
+    nb = T - 1
+    i = np.arange(nb)
+    assert np.array_equal(bvh[:nb, 0], np.where(i == 0, 0xFFFFFFFF, i - 1))
+    assert np.array_equal(bvh[:nb, 1], nb + i)
+    assert np.array_equal(bvh[:nb, 2], np.where(i + 1 < nb, i + 1, nb + i + 1))
+    j = np.arange(T)
+    assert np.array_equal(bvh[nb:, 0], np.minimum(j, nb - 1))
+    assert np.array_equal(bvh[nb:, 1], j)
+    assert (bvh[nb:, 2] == 0xFFFFFFFF).all()
+    # the root box is the box of every triangle, whatever the tree
+    root = oracle.build(*meshes[1])["bvhnode2aabb"][0]
+    assert np.array_equal(bits(aabb[0]), bits(root))
