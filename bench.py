@@ -487,8 +487,12 @@ def run_batched(args):
         plain.cast_pixels(tf)
 
     def batch_step():
+        # an NVTX range, so that a profiler can keep this step's launches
+        # apart from the plain path's (ncu --nvtx --nvtx-include "batched step/")
+        torch.cuda.nvtx.range_push("batched step")
         b.build()
         b.cast_pixels(tf)
+        torch.cuda.nvtx.range_pop()
 
     for _ in range(max(1, args.warmup // 2)):
         plain_step()
