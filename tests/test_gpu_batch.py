@@ -163,3 +163,32 @@ def test_batch_build_understated_max_tri(cuda, oracle):
     # the root box is the box of every triangle, whatever the tree
     root = oracle.build(*meshes[1])["bvhnode2aabb"][0]
     assert np.array_equal(bits(aabb[0]), bits(root))
+
+
+def test_full_config4_batched(cuda, oracle):
+    """The full ragged batch: 4096 meshes (about 33M triangles, the largest
+    65536, so clusters of four blocks), each with its 64x64 orthographic
+    image.  Every mesh's tree, boxes and image equal the oracle's bit for bit."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.batch import MeshBatch, ortho_transforms
+    meshes = W.ragged_batch(num_mesh=4096, tmin=64, tmax=65536, seed=0)
+    b = MeshBatch(meshes)
+    assert b.max_tri > 32768
+    tf = ortho_transforms(meshes)
+    b.build()
+    b.alloc_cast(64, 64)
+    p2t, tt = b.cast_pixels(torch.from_numpy(tf).to("cuda:0"))
+    torch.cuda.synchronize()
+    bvh_all, aabb_all = to_np(b.bvhnodes, torch), bits(to_np(b.bvhnode2aabb, torch))
+    p2t, tt = to_np(p2t, torch), bits(to_np(tt, torch))
+    for m, (tri, vtx) in enumerate(meshes):
+        ref = oracle.build(tri, vtx)
+        a = int(b.node_off[m])
+        n = 2 * tri.shape[0] - 1
+        assert np.array_equal(bvh_all[a:a + n], ref["bvhnodes"]), m
+        assert np.array_equal(aabb_all[a:a + n], bits(ref["bvhnode2aabb"])), m
+        r_p2t, r_tt = oracle.pix2tri(tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"], tf[m], 64, 64)
+        assert np.array_equal(p2t[m], r_p2t), m
+        assert np.array_equal(tt[m], bits(r_tt)), m
+    assert _native.device_status(clear=True) == 0
