@@ -308,6 +308,7 @@ bool set_tuning(const Tuning& t) {
   const auto phase_ok = [](uint32_t v) { return v >= 1 && v <= 32; };
   if (!cast_ok || !tile_ok || !sort_ok) return false;
   if (!phase_ok(t.cast_refill_min) || !phase_ok(t.cast_leaf_min) || !phase_ok(t.cast_ascend_min)) return false;
+  if (t.cast_long_steps < 1 || t.cast_long_steps > (1u << 30)) return false;
   std::lock_guard<std::mutex> lk(g_tuning_mutex);
   g_tuning = t;
   return true;
@@ -335,8 +336,8 @@ int dm_device_status(uint32_t* bits, int clear) {
 int dm_tuning_get(dm_tuning* out) {
   DM_REQUIRE(out, "NULL argument");
   const dm::Tuning t = dm::get_tuning();
-  *out = dm_tuning{t.cast_threads, t.cast_stack,     t.tile_w,        t.sort_window,
-                   t.cast_refill_min, t.cast_leaf_min, t.cast_ascend_min, 0};
+  *out = dm_tuning{t.cast_threads,    t.cast_stack,    t.tile_w,          t.sort_window,
+                   t.cast_refill_min, t.cast_leaf_min, t.cast_ascend_min, t.cast_long_steps};
   return DM_OK;
 }
 
@@ -351,10 +352,12 @@ int dm_tuning_set(const dm_tuning* in) {
   t.cast_refill_min = phase(in->cast_refill_min);
   t.cast_leaf_min = phase(in->cast_leaf_min);
   t.cast_ascend_min = phase(in->cast_ascend_min);
+  t.cast_long_steps = in->cast_long_steps == 0 ? dm::kDefaultLongSteps : in->cast_long_steps;
   DM_REQUIRE(dm::set_tuning(t),
-             "unsupported tuning (cast %u threads x %u frames, tile_w %u, sort window %u, phase minima %u/%u/%u)",
+             "unsupported tuning (cast %u threads x %u frames, tile_w %u, sort window %u, phase minima %u/%u/%u, "
+             "long-ray steps %u)",
              in->cast_threads, in->cast_stack, in->tile_w, in->sort_window, t.cast_refill_min, t.cast_leaf_min,
-             t.cast_ascend_min);
+             t.cast_ascend_min, t.cast_long_steps);
   return DM_OK;
 }
 

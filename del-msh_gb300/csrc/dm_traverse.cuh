@@ -197,10 +197,13 @@ __device__ __forceinline__ bool trav_begin(const MeshView& m, const Ray& r, Trav
 // tree has nodes) finishes the ray and sets `bad`.
 template <typename StackT>
 __device__ __forceinline__ int phase_inner(const MeshView& m, const Ray& r, StackT stack, uint32_t cap, Trav& s,
-                                           bool& bad) {
+                                           bool& bad, uint32_t long_steps = kUMax) {
   const uint32_t* __restrict__ bn = m.bvhnodes;
   const uint32_t num_node = 2 * m.num_tri - 1;
-  if (++s.steps > num_node + 1) {
+  // one test for both bounds: more entries than the tree has nodes (a
+  // malformed tree), or than the caller's budget (the ray is handed over)
+  if (++s.steps > min(num_node + 1, long_steps)) {
+    if (s.steps <= num_node + 1) return kLaneOverflow;
     bad = true;
     return kLaneDone;
   }
@@ -268,14 +271,27 @@ __device__ __forceinline__ int phase_leaf(const MeshView& m, const Ray& r, Trav&
   return kLaneInner;
 }
 
+// A frame kind that only the warp tier pushes (see ChainFold); elsewhere none.
+struct NoFold {
+  __device__ __forceinline__ int operator()(const uint4&, Trav&) const { return 0; }
+};
+
 // Pops frames until a far child is to be searched (kLaneInner) or the stack
-// is empty (kLaneDone).
-template <typename StackT>
-__device__ __forceinline__ int phase_ascend(const MeshView& m, const Ray& r, StackT stack, Trav& s, bool& bad) {
+// is empty (kLaneDone).  `fold` consumes the frames of its own kind (1), or
+// reports a malformed one (2).
+template <typename StackT, typename Fold = NoFold>
+__device__ __forceinline__ int phase_ascend(const MeshView& m, const Ray& r, StackT stack, Trav& s, bool& bad,
+                                            const Fold& fold = Fold{}) {
   const uint32_t num_node = 2 * m.num_tri - 1;
   s.chain_next = kUMax;
   while (s.sp > 0) {
     const uint4 f = stack.load(s.sp - 1);
+    const int folded = fold(f, s);
+    if (folded == 1) continue;
+    if (folded == 2) {
+      bad = true;
+      return kLaneDone;
+    }
     const Hit saved{__uint_as_float(f.z), f.w};
     uint32_t far;
     float far_enter;
@@ -361,6 +377,7 @@ constexpr int kDeepRing = 64;  // on-chip frames per ray of the overflow tiers
 // of the warp wait for it, or when nothing else can run.
 struct PhaseMins {
   uint32_t refill, leaf, ascend;
+  uint32_t long_steps;  // node entries after which a ray is handed to the warp tier
 };
 
 // Persistent warps with per-lane ray refill, run in phases.  Each lane holds
@@ -374,8 +391,9 @@ struct PhaseMins {
 // refill finds no more work, a waiting lane would only lengthen the warp's
 // longest ray, so from then on every phase runs whenever a lane needs it.
 // Every lane still makes the same decisions in the same order, so results do
-// not depend on the thresholds.  Rays overflowing the on-chip stack go to ovf_list (their
-// work index).  kThreads threads per block and kStack on-chip frames per ray
+// not depend on the thresholds.  Rays overflowing the on-chip stack, or
+// taking more than mins.long_steps node entries, go to ovf_list (their work
+// index) for the warp tier.  kThreads threads per block and kStack on-chip frames per ray
 // are tuning choices (Tuning); the register bound (64 registers) keeps 2048
 // resident threads per SM.
 template <typename Job, int kThreads, int kStack>
@@ -424,7 +442,7 @@ __global__ void __launch_bounds__(kThreads, 65536 / (64 * kThreads)) k_cast_pers
     // leaves the inner phase early waits for the others' entries.
 #pragma unroll
     for (int k = 0; k < kInnerSteps; ++k)
-      if (state == kLaneInner) state = phase_inner(m, r, stack, kStack, s, bad);
+      if (state == kLaneInner) state = phase_inner(m, r, stack, kStack, s, bad, mins.long_steps);
     uint32_t inner = __ballot_sync(kAll, state == kLaneInner);
     const uint32_t leaf = __ballot_sync(kAll, state == kLaneLeaf);
     if (leaf != 0u && (inner == 0u || static_cast<uint32_t>(__popc(leaf)) >= leaf_min)) {
@@ -503,6 +521,190 @@ __global__ void __launch_bounds__(kCastThreads) k_cast_deep(Job job, const uint3
   if (bad) raise_status(status, kStatusBadIndex);
 }
 
+// ------------------------------------------------------------ warp tier
+// Rays that overflowed the persistent cast's stack or ran past its step
+// budget, one warp each.  Every lane runs the same serial traversal on the
+// same state (the same loads, the same decisions), except at a chain: a run
+// of links, branches j whose left child is leaf j and right child branch
+// j + 1 (runs of equal Morton codes build them).  The recursion's result over
+// a chain c0..c1 is a fold from its far end: with x = F(c1 + 1), for j = c1
+// down to c0
+//   x <- g_j(x):  neither child box hit: none;  only leaf j's box: h_j (its hit);
+//                 only branch j+1's box: x;  both, the leaf nearer: h_j if h_j
+//                 is a hit before branch j+1's entry, else pick(h_j, x);  both,
+//                 the branch nearer: x if x is a hit before leaf j's entry,
+//                 else pick(x, h_j)
+// (the rules of phase_inner / phase_leaf / phase_ascend).  So the warp pushes
+// a fold frame, searches the tail c1 + 1 on its own, and on popping the frame
+// tests 32 links per round (a lane per link) and folds them with shuffles.
+// On the duplicate-heavy soup 96% of the long rays' node entries are links.
+constexpr uint32_t kFoldMin = 8;  // shorter chains are walked link by link
+constexpr uint32_t kWarpAll = 0xffffffffu;
+
+__device__ __forceinline__ bool is_link(const MeshView& m, uint32_t node, uint32_t left, uint32_t right) {
+  return left == m.num_tri - 1 + node && right == node + 1;
+}
+
+// The last link of the chain starting at link c0 (the same in every lane).
+__device__ __forceinline__ uint32_t chain_last(const MeshView& m, uint32_t c0, uint32_t lane) {
+  const uint32_t num_branch = m.num_tri - 1;
+  uint32_t last = c0;
+  for (;;) {
+    const uint32_t j = last + 1 + lane;
+    bool ok = false;
+    if (j < num_branch) {
+      uint32_t l, r;
+      load_record(m.bvhnodes, j, l, r);
+      ok = is_link(m, j, l, r);
+    }
+    const uint32_t fail = __ballot_sync(kWarpAll, !ok);
+    if (fail != 0u) return last + static_cast<uint32_t>(__ffs(fail)) - 1u;
+    last += 32;
+  }
+}
+
+// Folds links hi, hi - 1, .., lo (at most 32) into x; lane k tests link hi - k.
+__device__ __forceinline__ Hit fold_links(const MeshView& m, const Ray& r, uint32_t lo, uint32_t hi, Hit x,
+                                          uint32_t lane, bool& bad) {
+  const uint32_t n = hi - lo + 1;
+  bool ha = false, hb = false;
+  float a0 = 0.f, a1 = 0.f, b0 = 0.f, b1 = 0.f;
+  Hit h{INFINITY, kUMax};
+  if (lane < n) {
+    const uint32_t j = hi - lane, leaf = m.num_tri - 1 + j;
+    ha = node_slab(m, r, leaf, a0, a1);
+    hb = node_slab(m, r, j + 1, b0, b1);
+    if (ha) {
+      const uint32_t tri = __ldg(m.bvhnodes + static_cast<size_t>(leaf) * 3 + 1);
+      float t, u, v;
+      if (leaf_hit(m, r, tri, t, u, v, bad)) h = Hit{t, tri};
+    }
+  }
+  for (uint32_t k = 0; k < n; ++k) {
+    const bool kha = __shfl_sync(kWarpAll, ha, k), khb = __shfl_sync(kWarpAll, hb, k);
+    const float ka0 = __shfl_sync(kWarpAll, a0, k), ka1 = __shfl_sync(kWarpAll, a1, k);
+    const float kb0 = __shfl_sync(kWarpAll, b0, k), kb1 = __shfl_sync(kWarpAll, b1, k);
+    const Hit kh{__shfl_sync(kWarpAll, h.t, k), __shfl_sync(kWarpAll, h.id, k)};
+    if (!kha && !khb) {
+      x = Hit{INFINITY, kUMax};
+    } else if (!khb) {
+      x = kh;
+    } else if (kha) {
+      if (tuple_lt(ka0, ka1, kb0, kb1)) x = (kh.id != kUMax && kb0 > kh.t) ? kh : pick(kh, x);
+      else x = (x.id != kUMax && ka0 > x.t) ? x : pick(x, kh);
+    }
+  }
+  return x;
+}
+
+// phase_inner, except that a branch starting a chain of at least kFoldMin
+// links pushes a fold frame {c0 | bit, c1 | bit, saved} and searches the
+// chain's tail (if its box is hit) with a fresh result.
+template <typename StackT>
+__device__ __forceinline__ int phase_inner_warp(const MeshView& m, const Ray& r, StackT stack, uint32_t cap, Trav& s,
+                                                bool& bad, uint32_t lane) {
+  if (s.right != kUMax && is_link(m, s.node, s.left, s.right)) {
+    const uint32_t c0 = s.node, c1 = chain_last(m, c0, lane);
+    if (c1 - c0 + 1 >= kFoldMin) {
+      s.steps += 2 * (c1 - c0 + 1);  // its branches and leaves
+      if (s.steps > 2 * m.num_tri) {
+        bad = true;
+        return kLaneDone;
+      }
+      if (s.sp >= cap) return kLaneOverflow;
+      stack.store(s.sp++, make_uint4(kChainBit | c0, kChainBit | c1, __float_as_uint(s.best.t), s.best.id));
+      s.best = Hit{INFINITY, kUMax};
+      s.chain_next = kUMax;
+      const uint32_t tail = c1 + 1;
+      float te, tx;
+      if (!node_slab(m, r, tail, te, tx)) return kLaneAscend;  // the fold ignores the tail
+      s.node = tail;
+      load_record(m.bvhnodes, tail, s.left, s.right);
+      return kLaneInner;
+    }
+  }
+  return phase_inner(m, r, stack, cap, s, bad);
+}
+
+// Fold frames {c0 | bit, c1 | bit, saved}: the tail's result (the current
+// one) is folded through the chain, and the chain's result into `saved`.
+struct ChainFold {
+  const MeshView& m;
+  const Ray& r;
+  uint32_t lane;
+  bool* bad;
+  __device__ __forceinline__ int operator()(const uint4& f, Trav& s) const {
+    if (!((f.x & kChainBit) && (f.y & kChainBit))) return 0;
+    const uint32_t c0 = f.x & ~kChainBit, c1 = f.y & ~kChainBit;
+    if (c0 > c1 || c1 + 1 >= 2 * m.num_tri - 1) return 2;
+    Hit x = s.best;
+    for (uint32_t hi = c1;;) {
+      const uint32_t lo = hi - c0 >= 31 ? hi - 31 : c0;
+      x = fold_links(m, r, lo, hi, x, lane, *bad);
+      if (lo == c0) break;
+      hi = lo - 1;
+    }
+    --s.sp;
+    s.best = pick(Hit{__uint_as_float(f.z), f.w}, x);
+    return 1;
+  }
+};
+
+template <typename StackT>
+__device__ __forceinline__ int trav_step_warp(const MeshView& m, const Ray& r, StackT stack, uint32_t cap, Trav& s,
+                                              bool& bad, uint32_t lane) {
+  int st = phase_inner_warp(m, r, stack, cap, s, bad, lane);
+  if (st == kLaneLeaf) st = phase_leaf(m, r, s, bad);
+  if (st == kLaneAscend) st = phase_ascend(m, r, stack, s, bad, ChainFold{m, r, lane, &bad});
+  return st == kLaneInner ? kStepContinue : (st == kLaneOverflow ? kStepOverflow : kStepDone);
+}
+
+// One warp per ray of list_in; a ray whose frames outgrow the warp's slice of
+// the pool goes to list_out.  Every lane keeps the same stack (the ring in its
+// own local memory, the spilled frames at the same addresses of the slice).
+template <typename Job>
+__global__ void __launch_bounds__(kCastThreads) k_cast_warp(Job job, const uint32_t* list_in, const uint32_t* count_in,
+                                                           uint32_t* list_out, uint32_t* count_out, uint4* pool,
+                                                           uint64_t pool_frames, uint32_t max_tri, uint32_t* status) {
+  __shared__ float smem[64];
+  job.prepare(smem);
+  pdl_wait();
+  pdl_launch_dependents();
+  __syncthreads();
+  const uint32_t num = *count_in;
+  if (num == 0) return;
+  constexpr uint32_t kWarps = kCastThreads / 32;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t warps = static_cast<uint64_t>(gridDim.x) * kWarps;
+  const uint64_t wid = static_cast<uint64_t>(blockIdx.x) * kWarps + threadIdx.x / 32;
+  uint64_t cap = pool_frames / warps;
+  if (cap > 2ull * max_tri) cap = 2ull * max_tri;
+  uint4 ring[kDeepRing];
+  uint32_t lo = 0;
+  const RingStack<kDeepRing> st{ring, pool + wid * cap, &lo};
+  bool bad = false;
+  for (uint64_t k = wid; k < num; k += warps) {
+    lo = 0;
+    const uint32_t w = list_in[k];
+    MeshView m{};
+    Ray r{};
+    uint32_t out = 0;
+    if (!job.fetch(w, smem, m, r, out)) continue;
+    Trav s{};
+    int rc = kStepDone;
+    if (trav_begin(m, r, s)) {
+      do {
+        rc = trav_step_warp(m, r, st, static_cast<uint32_t>(cap), s, bad, lane);
+      } while (rc == kStepContinue);
+    }
+    if (lane == 0) {
+      if (rc == kStepDone) job.write(out, m, r, s.best);
+      else list_out[atomicAdd(count_out, 1u)] = w;
+    }
+  }
+  if (bad) raise_status(status, kStatusBadIndex);
+}
+
 // Number of resident blocks of a persistent kernel instantiation on the
 // current device.
 template <typename Job, int kThreads, int kStack>
@@ -526,15 +728,18 @@ inline void launch_persistent(cudaStream_t s, const Job& job, const CastScratch&
   const uint32_t needed = (job.num_work + kThreads - 1) / kThreads;
   if (static_cast<uint32_t>(grid) > needed) grid = static_cast<int>(needed);
   const Tuning t = get_tuning();
-  const PhaseMins mins{t.cast_refill_min, t.cast_leaf_min, t.cast_ascend_min};
+  const PhaseMins mins{t.cast_refill_min, t.cast_leaf_min, t.cast_ascend_min, t.cast_long_steps};
   k_cast_persistent<Job, kThreads, kStack><<<grid, kThreads, 0, s>>>(job, sc.counters, sc.list1, sc.counters + 1,
                                                                      status, mins);
 }
 
-// The three-tier cast of every work index of `job`.  sc.counters (4 words)
-// must be zero on entry: [0] work counter, [1] tier-1 overflow count, [2]
-// tier-2 overflow count.  The first tier's block size and on-chip stack
-// depth come from the current Tuning (kCastVariants lists the choices).
+// The tiered cast of every work index of `job`: the persistent cast; the
+// warp tier for the rays it hands over; for the rare ray whose frames outgrow
+// a warp's slice, the serial tier with the pool split over those rays, then
+// with unbounded frames.  sc.counters (4 words) must be zero on entry: [0]
+// work counter, [1..3] the hand-over counts of tiers 1..3 (lists list1,
+// list2, list1 again).  The first tier's block size and on-chip stack depth
+// come from the current Tuning (kCastVariants lists the choices).
 template <typename Job>
 inline void cast_job(cudaStream_t s, const Job& job, const CastScratch& sc, uint32_t max_tri, uint32_t* status) {
   if (job.num_work == 0) return;
@@ -547,10 +752,12 @@ inline void cast_job(cudaStream_t s, const Job& job, const CastScratch& sc, uint
   const uint64_t pool_frames = sc.pool_bytes / kFrameBytes;
   uint4* pool = static_cast<uint4*>(sc.pool);
   const uint32_t deep_grid = 152 * 4;
-  launch_pdl(k_cast_deep<Job>, dim3(deep_grid), dim3(kCastThreads), 0, s, job, sc.list1, sc.counters + 1, sc.list2,
-             sc.counters + 2, pool, pool_frames, 0u, max_tri, status);
+  launch_pdl(k_cast_warp<Job>, dim3(deep_grid), dim3(kCastThreads), 0, s, job, sc.list1, sc.counters + 1, sc.list2,
+             sc.counters + 2, pool, pool_frames, max_tri, status);
+  launch_pdl(k_cast_deep<Job>, dim3(deep_grid), dim3(kCastThreads), 0, s, job, sc.list2, sc.counters + 2, sc.list1,
+             sc.counters + 3, pool, pool_frames, 0u, max_tri, status);
   const uint32_t cap3 = max_tri < 2 ? 2u : max_tri;
-  launch_pdl(k_cast_deep<Job>, dim3(deep_grid), dim3(kCastThreads), 0, s, job, sc.list2, sc.counters + 2,
+  launch_pdl(k_cast_deep<Job>, dim3(deep_grid), dim3(kCastThreads), 0, s, job, sc.list1, sc.counters + 3,
              static_cast<uint32_t*>(nullptr), static_cast<uint32_t*>(nullptr), pool, pool_frames, cap3, max_tri,
              status);
 }

@@ -66,9 +66,9 @@ class Tuning(C.Structure):
     """dm_tuning of include/delmsh_gb300.h."""
     _fields_ = [("cast_threads", C.c_uint32), ("cast_stack", C.c_uint32), ("tile_w", C.c_uint32),
                 ("sort_window", C.c_uint32), ("cast_refill_min", C.c_uint32), ("cast_leaf_min", C.c_uint32),
-                ("cast_ascend_min", C.c_uint32), ("reserved", C.c_uint32)]
+                ("cast_ascend_min", C.c_uint32), ("cast_long_steps", C.c_uint32)]
     KEYS = ("cast_threads", "cast_stack", "tile_w", "sort_window", "cast_refill_min", "cast_leaf_min",
-            "cast_ascend_min")
+            "cast_ascend_min", "cast_long_steps")
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k in self.KEYS}
@@ -81,9 +81,10 @@ def get_tuning() -> dict:
 
 
 def set_tuning(cast_threads: int, cast_stack: int, tile_w: int, sort_window: int, cast_refill_min: int = 0,
-               cast_leaf_min: int = 0, cast_ascend_min: int = 0) -> None:
-    """Sets dm_tuning; a phase minimum of 0 selects the library default."""
-    t = Tuning(cast_threads, cast_stack, tile_w, sort_window, cast_refill_min, cast_leaf_min, cast_ascend_min)
+               cast_leaf_min: int = 0, cast_ascend_min: int = 0, cast_long_steps: int = 0) -> None:
+    """Sets dm_tuning; a phase minimum or step budget of 0 selects the library default."""
+    t = Tuning(cast_threads, cast_stack, tile_w, sort_window, cast_refill_min, cast_leaf_min, cast_ascend_min,
+               cast_long_steps)
     call("dm_tuning_set", C.addressof(t))
 
 

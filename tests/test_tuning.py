@@ -19,14 +19,15 @@ def test_tuning_roundtrip_and_validation():
                     _native.set_tuning(threads, frames, tile_w, window)  # phase minima 0: the default, 6
                     assert _native.get_tuning() == dict(cast_threads=threads, cast_stack=frames, tile_w=tile_w,
                                                         sort_window=window, cast_refill_min=6, cast_leaf_min=6,
-                                                        cast_ascend_min=6)
+                                                        cast_ascend_min=6, cast_long_steps=256)
         for mins in PHASE_CHOICES + [(1, 32, 32), (32, 1, 32), (32, 32, 1)]:
             _native.set_tuning(128, 64, 8, 4, *mins)
             assert tuple(_native.get_tuning()[k] for k in ("cast_refill_min", "cast_leaf_min",
                                                            "cast_ascend_min")) == mins
         _native.set_tuning(**DEFAULT)
         for bad in [(96, 64, 8, 4), (128, 48, 8, 4), (128, 64, 3, 4), (128, 64, 64, 4), (128, 64, 8, 5),
-                    (128, 64, 8, 4, 33, 6, 6), (128, 64, 8, 4, 6, 40, 6), (128, 64, 8, 4, 6, 6, 33)]:
+                    (128, 64, 8, 4, 33, 6, 6), (128, 64, 8, 4, 6, 40, 6), (128, 64, 8, 4, 6, 6, 33),
+                    (128, 64, 8, 4, 6, 6, 6, (1 << 30) + 1)]:
             with pytest.raises(_native.DelMshError):
                 _native.set_tuning(*bad)
             assert _native.get_tuning() == DEFAULT  # a rejected choice changes nothing
@@ -101,6 +102,52 @@ def test_shallow_stack_overflows_to_deeper_tiers(cuda, oracle):
         d_tri, d_vtx = to_dev(tri, torch), to_dev(vtx, torch)
         bvh, aabb = TriMesh3.make_bvhnodes_bvhnode2aabb(d_tri, d_vtx)
         hit, t = SearchBvh3.first_intersection_ray(to_dev(org, torch), to_dev(d, torch), d_tri, d_vtx, bvh, aabb)
+        assert np.array_equal(to_np(hit, torch), r_hit)
+        assert np.array_equal(bits(to_np(t, torch)), bits(r_t))
+    finally:
+        _native.set_tuning(**before)
+    assert _native.device_status(clear=True) == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("long_steps", [1, 16])
+def test_warp_tier_matches_oracle(cuda, oracle, long_steps):
+    """With a tiny step budget the persistent cast hands (nearly) every ray to
+    the warp tier, which runs each ray with a whole warp and folds chains of
+    links 32 at a time; the hits equal the oracle's bit for bit, on a smooth
+    mesh and on the duplicate-heavy soup (long chains)."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.Pix2Tri import torch as Pix2Tri
+    from del_msh_gb300.SearchBvh3 import torch as SearchBvh3
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    tri, vtx = W.displaced_torus(96, seed=11)
+    ref = oracle.build(tri, vtx)
+    m = W.pinhole_ndc2world(W.random_viewpoint(3.0, seed=2), aspect=120 / 90)
+    r_p2t, r_tt = oracle.pix2tri(tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"], m, 120, 90)
+    stri, svtx = W.clustered_soup(200_000, num_cluster=4, seed=9)
+    # rays from the cube boundary aimed at triangles, so that they cross the
+    # clusters' runs of equal codes (the tree's long chains)
+    org, _ = W.cube_boundary_rays(4_000, seed=9)
+    rng = np.random.default_rng(9)
+    target = svtx[stri[rng.integers(0, stri.shape[0], org.shape[0])]].mean(axis=1)
+    target = target + rng.uniform(-2e-4, 2e-4, target.shape)
+    d = (target - org).astype(np.float32)
+    sref = oracle.build(stri, svtx)
+    r_hit, r_t = oracle.cast_rays(org, d, stri, svtx, sref["bvhnodes"], sref["bvhnode2aabb"])
+    assert (r_hit != 0xFFFFFFFF).sum() > 1000
+    before = _native.get_tuning()
+    try:
+        _native.set_tuning(**dict(before, cast_long_steps=long_steps))
+        d_tri, d_vtx = to_dev(tri, torch), to_dev(vtx, torch)
+        bvh, aabb = TriMesh3.make_bvhnodes_bvhnode2aabb(d_tri, d_vtx)
+        m_row = torch.from_numpy(np.ascontiguousarray(m.reshape(4, 4).T)).to("cuda:0")
+        p2t, tt = Pix2Tri.by_raycasting(d_tri, d_vtx, bvh, aabb, m_row, (120, 90), return_depth=True)
+        assert np.array_equal(to_np(p2t, torch), r_p2t)
+        assert np.array_equal(bits(to_np(tt, torch)), bits(r_tt))
+        s_tri, s_vtx = to_dev(stri, torch), to_dev(svtx, torch)
+        sbvh, saabb = TriMesh3.make_bvhnodes_bvhnode2aabb(s_tri, s_vtx)
+        hit, t = SearchBvh3.first_intersection_ray(to_dev(org, torch), to_dev(d, torch), s_tri, s_vtx, sbvh, saabb)
         assert np.array_equal(to_np(hit, torch), r_hit)
         assert np.array_equal(bits(to_np(t, torch)), bits(r_t))
     finally:
