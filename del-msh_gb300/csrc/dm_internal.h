@@ -173,7 +173,7 @@ constexpr int kCastStack = 64;  // default frames of the on-chip (local) travers
 // set through dm_tuning_set.  Every choice gives the same results; only the
 // speed differs.  Read at each launch.
 constexpr uint32_t kDefaultPhaseMin = 6;
-constexpr uint32_t kDefaultLongSteps = 256;
+constexpr uint32_t kDefaultLongSteps = 64;
 struct Tuning {
   uint32_t cast_threads = 128;  // threads per block of the persistent cast
   uint32_t cast_stack = 64;     // on-chip frames per ray
@@ -185,9 +185,8 @@ struct Tuning {
   uint32_t cast_refill_min = kDefaultPhaseMin;
   uint32_t cast_leaf_min = kDefaultPhaseMin;
   uint32_t cast_ascend_min = kDefaultPhaseMin;
-  // node entries after which the persistent cast hands a ray to the warp
-  // tier (measured on GB300: 256 leaves the config-2 cast as it is and takes
-  // the soup's cast from 15.3 to 2.6 ms; 128 slows config 2 by 27%)
+  // node entries after which the persistent cast, once a warp has no more
+  // rays to take, hands a ray entering a long chain to the warp tier
   uint32_t cast_long_steps = kDefaultLongSteps;
 };
 // (threads, stack) pairs compiled for the persistent cast

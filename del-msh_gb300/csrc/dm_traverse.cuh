@@ -173,6 +173,29 @@ enum LaneState : int {
   kLaneDone = 5,      // s.best is the ray's result
 };
 
+// Chain links: branch j whose left child is leaf j and right child branch
+// j + 1 (runs of equal Morton codes build long runs of them).  The warp tier
+// folds runs of at least kFoldMin links instead of walking them.
+constexpr uint32_t kFoldMin = 8;
+
+__device__ __forceinline__ bool is_link(const MeshView& m, uint32_t node, uint32_t left, uint32_t right) {
+  return left == m.num_tri - 1 + node && right == node + 1;
+}
+
+// Whether a run of at least kFoldMin links starts at branch `node` (its
+// record: left, right); the other records are loaded together.
+__device__ __forceinline__ bool long_chain_at(const MeshView& m, uint32_t node, uint32_t left, uint32_t right) {
+  if (!is_link(m, node, left, right) || node + kFoldMin > m.num_tri - 1) return false;
+  bool all = true;
+#pragma unroll
+  for (uint32_t k = 1; k < kFoldMin; ++k) {
+    uint32_t l, r;
+    load_record(m.bvhnodes, node + k, l, r);
+    all = all && is_link(m, node + k, l, r);
+  }
+  return all;
+}
+
 // Starts a ray: a miss of the root box finishes it immediately.
 __device__ __forceinline__ bool trav_begin(const MeshView& m, const Ray& r, Trav& s) {
   s.node = 0;
@@ -197,13 +220,10 @@ __device__ __forceinline__ bool trav_begin(const MeshView& m, const Ray& r, Trav
 // tree has nodes) finishes the ray and sets `bad`.
 template <typename StackT>
 __device__ __forceinline__ int phase_inner(const MeshView& m, const Ray& r, StackT stack, uint32_t cap, Trav& s,
-                                           bool& bad, uint32_t long_steps = kUMax) {
+                                           bool& bad) {
   const uint32_t* __restrict__ bn = m.bvhnodes;
   const uint32_t num_node = 2 * m.num_tri - 1;
-  // one test for both bounds: more entries than the tree has nodes (a
-  // malformed tree), or than the caller's budget (the ray is handed over)
-  if (++s.steps > min(num_node + 1, long_steps)) {
-    if (s.steps <= num_node + 1) return kLaneOverflow;
+  if (++s.steps > num_node + 1) {
     bad = true;
     return kLaneDone;
   }
@@ -391,9 +411,9 @@ struct PhaseMins {
 // refill finds no more work, a waiting lane would only lengthen the warp's
 // longest ray, so from then on every phase runs whenever a lane needs it.
 // Every lane still makes the same decisions in the same order, so results do
-// not depend on the thresholds.  Rays overflowing the on-chip stack, or
-// taking more than mins.long_steps node entries, go to ovf_list (their work
-// index) for the warp tier.  kThreads threads per block and kStack on-chip frames per ray
+// not depend on the thresholds.  Rays overflowing the on-chip stack, and
+// rays past mins.long_steps node entries at a long chain once the warp's
+// work is exhausted, go to ovf_list (their work index) for the warp tier.  kThreads threads per block and kStack on-chip frames per ray
 // are tuning choices (Tuning); the register bound (64 registers) keeps 2048
 // resident threads per SM.
 template <typename Job, int kThreads, int kStack>
@@ -442,7 +462,7 @@ __global__ void __launch_bounds__(kThreads, 65536 / (64 * kThreads)) k_cast_pers
     // leaves the inner phase early waits for the others' entries.
 #pragma unroll
     for (int k = 0; k < kInnerSteps; ++k)
-      if (state == kLaneInner) state = phase_inner(m, r, stack, kStack, s, bad, mins.long_steps);
+      if (state == kLaneInner) state = phase_inner(m, r, stack, kStack, s, bad);
     uint32_t inner = __ballot_sync(kAll, state == kLaneInner);
     const uint32_t leaf = __ballot_sync(kAll, state == kLaneLeaf);
     if (leaf != 0u && (inner == 0u || static_cast<uint32_t>(__popc(leaf)) >= leaf_min)) {
@@ -453,6 +473,11 @@ __global__ void __launch_bounds__(kThreads, 65536 / (64 * kThreads)) k_cast_pers
     if (asc != 0u && (inner == 0u || static_cast<uint32_t>(__popc(asc)) >= ascend_min)) {
       if (state == kLaneAscend) state = phase_ascend(m, r, stack, s, bad);
     }
+    // Once the warp has no more rays to take, a ray past the step budget
+    // that is about to enter a long chain would hold the kernel's end: it is
+    // handed to the warp tier, which folds chains 32 links at a time.
+    if (exhausted && state == kLaneInner && s.steps > mins.long_steps && long_chain_at(m, s.node, s.left, s.right))
+      state = kLaneOverflow;
     if (state == kLaneDone) {
       job.write(out, m, r, s.best);
       state = kLaneIdle;
@@ -538,12 +563,7 @@ __global__ void __launch_bounds__(kCastThreads) k_cast_deep(Job job, const uint3
 // a fold frame, searches the tail c1 + 1 on its own, and on popping the frame
 // tests 32 links per round (a lane per link) and folds them with shuffles.
 // On the duplicate-heavy soup 96% of the long rays' node entries are links.
-constexpr uint32_t kFoldMin = 8;  // shorter chains are walked link by link
 constexpr uint32_t kWarpAll = 0xffffffffu;
-
-__device__ __forceinline__ bool is_link(const MeshView& m, uint32_t node, uint32_t left, uint32_t right) {
-  return left == m.num_tri - 1 + node && right == node + 1;
-}
 
 // The last link of the chain starting at link c0 (the same in every lane).
 __device__ __forceinline__ uint32_t chain_last(const MeshView& m, uint32_t c0, uint32_t lane) {

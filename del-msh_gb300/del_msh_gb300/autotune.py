@@ -42,7 +42,7 @@ SORT_WINDOWS = [4, 8]
 PHASE_CHOICES = [(1, 1, 1), (4, 4, 4), (6, 6, 6), (8, 8, 8), (8, 6, 6), (12, 8, 8), (16, 8, 8), (12, 12, 12),
                  (16, 12, 12), (24, 8, 8), (20, 10, 10), (8, 4, 4), (12, 4, 4), (12, 6, 6), (16, 6, 6), (6, 2, 2)]
 DEFAULT = dict(cast_threads=128, cast_stack=64, tile_w=8, sort_window=4, cast_refill_min=6, cast_leaf_min=6,
-               cast_ascend_min=6, cast_long_steps=256)
+               cast_ascend_min=6, cast_long_steps=64)
 _PHASE_KEYS = ("cast_refill_min", "cast_leaf_min", "cast_ascend_min")
 
 

@@ -78,9 +78,10 @@ typedef struct dm_tuning {
   uint32_t cast_refill_min;
   uint32_t cast_leaf_min;
   uint32_t cast_ascend_min;
-  /* Node entries after which the persistent cast hands a ray to the warp
-     tier, where one warp runs it and folds runs of chain links 32 at a time:
-     1..2^30, 0 = the default (256).  Results do not depend on it. */
+  /* Node entries after which the persistent cast, once a warp has no more
+     rays to take, hands a ray entering a long run of chain links to the warp
+     tier, where one warp runs it and folds the links 32 at a time: 1..2^30,
+     0 = the default (64).  Results do not depend on it. */
   uint32_t cast_long_steps;
 } dm_tuning;
 

@@ -19,7 +19,7 @@ def test_tuning_roundtrip_and_validation():
                     _native.set_tuning(threads, frames, tile_w, window)  # phase minima 0: the default, 6
                     assert _native.get_tuning() == dict(cast_threads=threads, cast_stack=frames, tile_w=tile_w,
                                                         sort_window=window, cast_refill_min=6, cast_leaf_min=6,
-                                                        cast_ascend_min=6, cast_long_steps=256)
+                                                        cast_ascend_min=6, cast_long_steps=64)
         for mins in PHASE_CHOICES + [(1, 32, 32), (32, 1, 32), (32, 32, 1)]:
             _native.set_tuning(128, 64, 8, 4, *mins)
             assert tuple(_native.get_tuning()[k] for k in ("cast_refill_min", "cast_leaf_min",
@@ -112,14 +112,15 @@ def test_shallow_stack_overflows_to_deeper_tiers(cuda, oracle):
 @pytest.mark.gpu
 @pytest.mark.parametrize("long_steps", [1, 16])
 def test_warp_tier_matches_oracle(cuda, oracle, long_steps):
-    """With a tiny step budget the persistent cast hands (nearly) every ray to
-    the warp tier, which runs each ray with a whole warp and folds chains of
-    links 32 at a time; the hits equal the oracle's bit for bit, on a smooth
-    mesh and on the duplicate-heavy soup (long chains)."""
+    """With a tiny step budget the persistent cast hands every ray that
+    reaches a long run of chain links (once its warp has no more rays to
+    take) to the warp tier, which folds the links 32 at a time; on a soup with
+    rays aimed at its clusters (runs of equal codes) hundreds of rays go
+    there, and the hits equal the oracle's bit for bit.  A smooth mesh, with
+    no long chains, keeps the oracle's bits under the same budget."""
     torch = cuda
     from del_msh_gb300 import _native
     from del_msh_gb300.Pix2Tri import torch as Pix2Tri
-    from del_msh_gb300.SearchBvh3 import torch as SearchBvh3
     from del_msh_gb300.TriMesh3 import torch as TriMesh3
     tri, vtx = W.displaced_torus(96, seed=11)
     ref = oracle.build(tri, vtx)
@@ -136,6 +137,7 @@ def test_warp_tier_matches_oracle(cuda, oracle, long_steps):
     sref = oracle.build(stri, svtx)
     r_hit, r_t = oracle.cast_rays(org, d, stri, svtx, sref["bvhnodes"], sref["bvhnode2aabb"])
     assert (r_hit != 0xFFFFFFFF).sum() > 1000
+    L = _native.load()
     before = _native.get_tuning()
     try:
         _native.set_tuning(**dict(before, cast_long_steps=long_steps))
@@ -147,8 +149,18 @@ def test_warp_tier_matches_oracle(cuda, oracle, long_steps):
         assert np.array_equal(bits(to_np(tt, torch)), bits(r_tt))
         s_tri, s_vtx = to_dev(stri, torch), to_dev(svtx, torch)
         sbvh, saabb = TriMesh3.make_bvhnodes_bvhnode2aabb(s_tri, s_vtx)
-        hit, t = SearchBvh3.first_intersection_ray(to_dev(org, torch), to_dev(d, torch), s_tri, s_vtx, sbvh, saabb)
-        assert np.array_equal(to_np(hit, torch), r_hit)
+        n, T, V = org.shape[0], stri.shape[0], svtx.shape[0]
+        hit = torch.empty((n,), dtype=torch.int32, device="cuda:0")
+        t = torch.empty((n,), dtype=torch.float32, device="cuda:0")
+        cs = L.dm_cast_scratch_bytes(n, T)
+        scr = torch.empty((cs,), dtype=torch.uint8, device="cuda:0")
+        o_dev, d_dev = to_dev(org, torch), to_dev(d, torch)
+        _native.call("dm_search_bvh3_first_intersection_ray", torch.cuda.current_stream().cuda_stream, n,
+                     o_dev.data_ptr(), d_dev.data_ptr(), hit.data_ptr(), t.data_ptr(), None, T, s_tri.data_ptr(), V,
+                     s_vtx.data_ptr(), sbvh.data_ptr(), saabb.data_ptr(), scr.data_ptr(), cs)
+        handed = int(scr[4:8].view(torch.int32).item())  # rays handed to the warp tier
+        assert handed > 100
+        assert np.array_equal(to_np(hit, torch).view(np.uint32), r_hit)
         assert np.array_equal(bits(to_np(t, torch)), bits(r_t))
     finally:
         _native.set_tuning(**before)
