@@ -566,21 +566,36 @@ __global__ void __launch_bounds__(kCastThreads) k_cast_deep(Job job, const uint3
 // On the duplicate-heavy soup 96% of the long rays' node entries are links.
 constexpr uint32_t kWarpAll = 0xffffffffu;
 
-// The last link of the chain starting at link c0 (the same in every lane).
+// The last link of the chain starting at link c0 (the same in every lane),
+// 256 records per round (8 per lane: 2.19 ms soup cast, 4 per lane 2.22,
+// 1 per lane 2.45).
 __device__ __forceinline__ uint32_t chain_last(const MeshView& m, uint32_t c0, uint32_t lane) {
   const uint32_t num_branch = m.num_tri - 1;
   uint32_t last = c0;
   for (;;) {
-    const uint32_t j = last + 1 + lane;
-    bool ok = false;
-    if (j < num_branch) {
-      uint32_t l, r;
-      load_record(m.bvhnodes, j, l, r);
-      ok = is_link(m, j, l, r);
+    // lane l checks links last + 1 + 8 l .. last + 8 l + 8
+    bool ok[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const uint32_t j = last + 1 + 8 * lane + q;
+      ok[q] = false;
+      if (j < num_branch) {
+        uint32_t l, r;
+        load_record(m.bvhnodes, j, l, r);
+        ok[q] = is_link(m, j, l, r);
+      }
     }
-    const uint32_t fail = __ballot_sync(kWarpAll, !ok);
-    if (fail != 0u) return last + static_cast<uint32_t>(__ffs(fail)) - 1u;
-    last += 32;
+    uint32_t first_bad = 8;
+#pragma unroll
+    for (int q = 7; q >= 0; --q)
+      if (!ok[q]) first_bad = q;
+    const uint32_t fail = __ballot_sync(kWarpAll, first_bad < 8);
+    if (fail != 0u) {
+      const uint32_t l0 = static_cast<uint32_t>(__ffs(fail)) - 1u;
+      const uint32_t fb = __shfl_sync(kWarpAll, first_bad, l0);
+      return last + 8 * l0 + fb;
+    }
+    last += 256;
   }
 }
 
