@@ -654,16 +654,19 @@ struct BatchJob {
   const uint32_t* bvhnodes;
   const float* aabb;
   uint32_t img_w, img_h, tiles_x, tile_w, tile_h, work_per_mesh;
+  uint32_t tile_w_log;  // tile_w is a power of two
+  Divider by_work_per_mesh, by_tiles_x;
   const float* transforms;  // num_mesh x 16, column-major ndc -> world
   CastOut o;
 
   __device__ __forceinline__ void prepare(float*) const {}
 
   __device__ __forceinline__ bool fetch(uint32_t w, const float*, MeshView& mv, Ray& r, uint32_t& out) const {
-    const uint32_t m = w / work_per_mesh, lw = w - m * work_per_mesh;
+    const uint32_t m = by_work_per_mesh.div(w), lw = w - m * work_per_mesh;
     const uint32_t tile = lw >> 5, j = lw & 31u;
-    const uint32_t px = (tile % tiles_x) * tile_w + (j % tile_w);
-    const uint32_t py = (tile / tiles_x) * tile_h + (j / tile_w);
+    const uint32_t ty = by_tiles_x.div(tile);
+    const uint32_t px = (tile - ty * tiles_x) * tile_w + (j & (tile_w - 1u));
+    const uint32_t py = ty * tile_h + (j >> tile_w_log);
     if (px >= img_w || py >= img_h) return false;
     const uint32_t t0 = __ldg(seg.tri_off + m), T = __ldg(seg.tri_off + m + 1) - t0;
     const uint32_t v0 = __ldg(seg.vtx_off + m), V = __ldg(seg.vtx_off + m + 1) - v0;
@@ -686,7 +689,7 @@ struct BatchJob {
     for (int k = 0; k < 16; ++k) mm[k] = __ldg(mt + k);
     const uint32_t pix = py * img_w + px;
     float3 o3, d3;
-    ray_for_pixel(pix, img_w, img_h, mm, o3, d3);
+    ray_for_pixel_xy(px, py, img_w, img_h, mm, o3, d3);
     r = make_ray(o3, d3);
     out = m * (img_w * img_h) + pix;
     return true;
@@ -806,8 +809,11 @@ void launch_batch_cast_pixels(cudaStream_t s, const Segments& seg, uint32_t max_
   const Tuning t = get_tuning();
   job.tile_w = t.tile_w;
   job.tile_h = 32u / t.tile_w;
+  job.tile_w_log = static_cast<uint32_t>(__builtin_ctz(t.tile_w));
   job.tiles_x = (img_w + job.tile_w - 1) / job.tile_w;
   job.work_per_mesh = job.tiles_x * ((img_h + job.tile_h - 1) / job.tile_h) * 32u;
+  job.by_work_per_mesh = Divider::make(job.work_per_mesh);
+  job.by_tiles_x = Divider::make(job.tiles_x);
   job.num_work = job.work_per_mesh * seg.num_mesh;
   job.transforms = transforms;
   job.o = o;

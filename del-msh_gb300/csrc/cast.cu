@@ -14,6 +14,8 @@ struct SingleJob {
   uint32_t num_work;
   MeshView m;
   uint32_t img_w, img_h, tiles_x, tile_w, tile_h;  // pixel mode
+  uint32_t tile_w_log;                              // tile_w is a power of two
+  Divider by_tiles_x;
   const float* t_ndc2world;
   const float* ray_org;  // ray mode when non-null
   const float* ray_dir;
@@ -34,12 +36,13 @@ struct SingleJob {
       return true;
     }
     const uint32_t tile = w >> 5, j = w & 31u;
-    const uint32_t px = (tile % tiles_x) * tile_w + (j % tile_w);
-    const uint32_t py = (tile / tiles_x) * tile_h + (j / tile_w);
+    const uint32_t ty = by_tiles_x.div(tile);
+    const uint32_t px = (tile - ty * tiles_x) * tile_w + (j & (tile_w - 1u));
+    const uint32_t py = ty * tile_h + (j >> tile_w_log);
     if (px >= img_w || py >= img_h) return false;
     out = py * img_w + px;
     float3 o3, d3;
-    ray_for_pixel(out, img_w, img_h, smem, o3, d3);
+    ray_for_pixel_xy(px, py, img_w, img_h, smem, o3, d3);
     r = make_ray(o3, d3);
     return true;
   }
@@ -91,7 +94,9 @@ void launch_cast_pixels(cudaStream_t s, uint32_t img_w, uint32_t img_h, const fl
   const Tuning t = get_tuning();
   job.tile_w = t.tile_w;
   job.tile_h = 32u / t.tile_w;
+  job.tile_w_log = static_cast<uint32_t>(__builtin_ctz(t.tile_w));
   job.tiles_x = (img_w + job.tile_w - 1) / job.tile_w;
+  job.by_tiles_x = Divider::make(job.tiles_x);
   const uint32_t tiles_y = (img_h + job.tile_h - 1) / job.tile_h;
   job.num_work = job.tiles_x * tiles_y * 32u;
   job.t_ndc2world = t_ndc2world;

@@ -203,11 +203,9 @@ __device__ __forceinline__ bool tuple_lt(float a0, float a1, float b0, float b1)
   return (a0 == b0) ? (a1 < b1) : (a0 < b0);
 }
 
-// ray_for_pixel.h:3-19
-__device__ __forceinline__ void ray_for_pixel(uint32_t i_pix, uint32_t img_w, uint32_t img_h, const float* m,
-                                              float3& org, float3& dir) {
-  const uint32_t ih = i_pix / img_w;
-  const uint32_t iw = i_pix - ih * img_w;
+// ray_for_pixel.h:3-19 for the pixel in column iw, row ih.
+__device__ __forceinline__ void ray_for_pixel_xy(uint32_t iw, uint32_t ih, uint32_t img_w, uint32_t img_h,
+                                                 const float* m, float3& org, float3& dir) {
   const float x0 = __fsub_rn(__fdiv_rn(__fmul_rn(2.0f, __fadd_rn(static_cast<float>(iw), 0.5f)),
                                        static_cast<float>(img_w)),
                              1.0f);
@@ -218,6 +216,27 @@ __device__ __forceinline__ void ray_for_pixel(uint32_t i_pix, uint32_t img_w, ui
   org = q0;
   dir = sub3(q1, q0);
 }
+
+// ray_for_pixel.h:3-19 for pixel i_pix (row-major).
+__device__ __forceinline__ void ray_for_pixel(uint32_t i_pix, uint32_t img_w, uint32_t img_h, const float* m,
+                                              float3& org, float3& dir) {
+  const uint32_t ih = i_pix / img_w;
+  ray_for_pixel_xy(i_pix - ih * img_w, ih, img_w, img_h, m, org, dir);
+}
+
+// n / d for any 32-bit n by a 64-bit multiply-high with magic = ceil(2^64 / d):
+// n * magic / 2^64 exceeds n / d by less than n / 2^64 < 2^-32 < 1 / d, so the
+// floor is exact.  For the per-ray index arithmetic of the casts.
+struct Divider {
+  uint32_t d;
+  unsigned long long magic;  // 0 for d == 1
+  __host__ static Divider make(uint32_t d) {
+    return Divider{d, d <= 1 ? 0ull : ~0ull / d + 1ull};
+  }
+  __device__ __forceinline__ uint32_t div(uint32_t n) const {
+    return d <= 1 ? n : static_cast<uint32_t>(__umul64hi(static_cast<unsigned long long>(n), magic));
+  }
+};
 
 // ---------------------------------------------------------------- AABBs
 
