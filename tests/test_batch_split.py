@@ -17,3 +17,20 @@ def test_multiply_high_owner_is_exact():
             magic = np.uint64(0xFFFFFFFF // per + 1)
             own = (i * magic) >> np.uint64(32)
             assert np.array_equal(own, i // np.uint64(per)), (kc, per)
+
+
+def test_divider_multiply_high_is_exact():
+    """The casts' per-ray index arithmetic (Divider in csrc/dm_device.cuh)
+    divides a 32-bit index n by d as the high 64 bits of n * ceil(2^64 / d):
+    the product exceeds n / d by less than n / 2^64 < 1 / d, so the floor is
+    exact.  Checked here on the edges and on random operands."""
+    rng = np.random.default_rng(7)
+    ds = [2, 3, 5, 7, 16, 30, 60, 64, 120, 480, 481, 1919, 4096, 65535, 65537, 2**31 - 1, 2**32 - 1]
+    ds += [int(x) for x in rng.integers(2, 2**32, 300)]
+    for d in ds:
+        magic = (2**64 - 1) // d + 1
+        ns = [0, 1, d - 1, d, d + 1, 2**32 - 1, 2**32 - 2, (2**32 - 1) // d * d, (2**32 - 1) // d * d - 1]
+        ns += [int(x) for x in rng.integers(0, 2**32, 200)]
+        for n in ns:
+            if 0 <= n < 2**32:
+                assert (n * magic) >> 64 == n // d, (n, d)
