@@ -36,6 +36,36 @@ __device__ __forceinline__ float3 tri_centroid(const uint32_t* __restrict__ tri2
   return make_float3(centroid1(p0.x, p1.x, p2.x), centroid1(p0.y, p1.y, p2.y), centroid1(p0.z, p1.z, p2.z));
 }
 
+// tri_centroid, and the triangle's box exactly as leaf_box computes it (the
+// same vertex loads, eps 0) into *box.
+__device__ __forceinline__ float3 tri_centroid_box(const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
+                                                   const float* __restrict__ vtx2xyz, uint32_t it, uint32_t* status,
+                                                   Box* box) {
+  const uint32_t* t = tri2vtx + static_cast<size_t>(it) * 3;
+  const float3 p0 = load_vtx(vtx2xyz, vtx_index(t, num_vtx, status));
+  const float3 p1 = load_vtx(vtx2xyz, vtx_index(t + 1, num_vtx, status));
+  const float3 p2 = load_vtx(vtx2xyz, vtx_index(t + 2, num_vtx, status));
+  box_set(*box, p0, 0.0f);
+  box_add(*box, p1, 0.0f);
+  box_add(*box, p2, 0.0f);
+  return make_float3(centroid1(p0.x, p1.x, p2.x), centroid1(p0.y, p1.y, p2.y), centroid1(p0.z, p1.z, p2.z));
+}
+
+// A box stored by box_store, read through the read-only path.
+__device__ __forceinline__ Box box_load_ro(const float* src) {
+  const float2 a = __ldg(reinterpret_cast<const float2*>(src));
+  const float2 b = __ldg(reinterpret_cast<const float2*>(src) + 1);
+  const float2 c = __ldg(reinterpret_cast<const float2*>(src) + 2);
+  Box o;
+  o.lo[0] = a.x;
+  o.lo[1] = a.y;
+  o.lo[2] = b.x;
+  o.hi[0] = b.y;
+  o.hi[1] = c.x;
+  o.hi[2] = c.y;
+  return o;
+}
+
 // Reduction of (min, max) over 6 lanes-of-values held by each thread; NaN is
 // ignored because every comparison with NaN is false.
 struct MinMax {
@@ -96,11 +126,12 @@ __device__ __forceinline__ MinMax block_reduce_mm(MinMax v, MinMax* sh /* [kThre
 // the first centroid's is, and otherwise equals the min / max over the
 // non-NaN values (the max of c + 0).  A two-level reduction with a last-block
 // ticket computes exactly that.
+template <bool kBox>
 __global__ void __launch_bounds__(kThreads) k_centroid_aabb(uint32_t num_tri, const uint32_t* __restrict__ tri2vtx,
                                                            uint32_t num_vtx, const float* __restrict__ vtx2xyz,
                                                            float* partials, uint32_t* ticket, float* aabb_out,
                                                            float* transform_out, uint32_t* status, float* cent,
-                                                           size_t stride) {
+                                                           size_t stride, float* tribox) {
   __shared__ MinMax sh[kThreads / 32];
   __shared__ bool s_last;
   MinMax v;
@@ -110,7 +141,14 @@ __global__ void __launch_bounds__(kThreads) k_centroid_aabb(uint32_t num_tri, co
     v.hi[d] = -INFINITY;
   }
   for (uint32_t i = blockIdx.x * kThreads + threadIdx.x; i < num_tri; i += gridDim.x * kThreads) {
-    const float3 c = tri_centroid(tri2vtx, num_vtx, vtx2xyz, i, status);
+    float3 c;
+    if constexpr (kBox) {
+      Box tb;
+      c = tri_centroid_box(tri2vtx, num_vtx, vtx2xyz, i, status, &tb);
+      box_store(tribox + 6ull * i, tb);
+    } else {
+      c = tri_centroid(tri2vtx, num_vtx, vtx2xyz, i, status);
+    }
     if (cent) {
       cent[i] = c.x;
       cent[stride + i] = c.y;
@@ -774,7 +812,7 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
                                                               const float* __restrict__ vtx0_all,
                                                               const float* __restrict__ vtx1_all, float* aabb_all,
                                                               uint32_t* hdr, uint32_t* cross_list, float* wseg,
-                                                              uint32_t* status) {
+                                                              uint32_t* status, const float* __restrict__ tribox) {
   __shared__ Box tree[2 * kRefitWindow];
   __shared__ uint32_t s_mesh, s_flag;
   const uint32_t wA = blockIdx.x * kRefitWindow;
@@ -818,8 +856,12 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
         tri[r] = 0u;
       }
       const uint32_t* t2v = tri2vtx_all + 3ull * lm[r].t0;
-      bx = leaf_box(t2v, lm[r].V, vtx0_all + 3ull * lm[r].v0, tri[r], status);
-      if (vtx1_all) bx = box_union(bx, leaf_box(t2v, lm[r].V, vtx1_all + 3ull * lm[r].v0, tri[r], status));
+      if (tribox) {  // boxes the centroid pass computed (one mesh, one vertex state)
+        bx = box_load_ro(tribox + 6ull * (lm[r].t0 + tri[r]));
+      } else {
+        bx = leaf_box(t2v, lm[r].V, vtx0_all + 3ull * lm[r].v0, tri[r], status);
+        if (vtx1_all) bx = box_union(bx, leaf_box(t2v, lm[r].V, vtx1_all + 3ull * lm[r].v0, tri[r], status));
+      }
       box_store(aabb_all + 6 * (2ull * lm[r].t0 - lm[r].m + lm[r].T - 1 + (wA + k - lm[r].t0)), bx);
       nan = nan || box_has_nan(bx);
     }
@@ -1192,10 +1234,14 @@ __global__ void __launch_bounds__(256) k_refit_seg_cross_threads(uint32_t total_
 
 void launch_centroid_aabb(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
                           const float* vtx2xyz, float* partials, uint32_t* ticket, float* aabb_out,
-                          float* transform_out, uint32_t* status, float* cent, size_t stride) {
+                          float* transform_out, uint32_t* status, float* cent, size_t stride, float* tribox) {
   const int grid = grid_for(num_tri, kThreads * 8, kAabbBlocks);
-  k_centroid_aabb<<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, partials, ticket, aabb_out,
-                                            transform_out, status, cent, stride);
+  if (tribox)
+    k_centroid_aabb<true><<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, partials, ticket, aabb_out,
+                                                    transform_out, status, cent, stride, tribox);
+  else
+    k_centroid_aabb<false><<<grid, kThreads, 0, s>>>(num_tri, tri2vtx, num_vtx, vtx2xyz, partials, ticket, aabb_out,
+                                                     transform_out, status, cent, stride, nullptr);
 }
 
 void launch_morton_tri(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
@@ -1234,8 +1280,9 @@ void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, con
 void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
                            const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
                            const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
-                           uint32_t* height_out, uint32_t* status) {
+                           uint32_t* height_out, uint32_t* status, const float* tribox) {
   if (total_tri == 0) return;
+  if (seg.tri_off || vtx2xyz1) tribox = nullptr;  // one mesh, one vertex state only
   const int smem = static_cast<int>(sizeof(WinSmem));
   const uint32_t windows = refit_num_windows(total_tri), supers = refit_num_super(total_tri);
   const uint32_t top_log = refit_top_log(total_tri);
@@ -1272,7 +1319,8 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   float* tseg = const_cast<float*>(v.tseg);
   if (seg.tri_off) {
     k_refit_seg_win<true><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
-                                                          vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg, status);
+                                                          vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg, status,
+                                                          nullptr);
     launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
     launch_pdl(k_refit_seg_cross_groups<true>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb,
                queue, flags, v, cross_groups, status);
@@ -1285,7 +1333,7 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   } else {
     k_refit_seg_win<false><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end,
                                                            tri2vtx, vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg,
-                                                           status);
+                                                           status, tribox);
     launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
     launch_pdl(k_refit_seg_cross_groups<false>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb,
                queue, flags, v, cross_groups, status);

@@ -110,8 +110,8 @@ SortLayout sort_layout(uint32_t n, int num_pass, size_t key_bytes, int radix = d
 
 // -------------------------------------------------------- build layout
 struct BuildLayout {
-  size_t transform, aabb, ticket, height, sort_hdr, partials, codes, akeys, avals, bvals, flags, total, zero_bytes,
-      sort_bytes;
+  size_t transform, aabb, ticket, height, sort_hdr, partials, codes, akeys, avals, bvals, flags, tribox, total,
+      zero_bytes, sort_bytes;
   bool radix10;  // three 10-bit passes (dm::kRadix10MaxKeys), else four 8-bit ones
   SortLayout sort;
 };
@@ -133,7 +133,8 @@ BuildLayout build_layout(uint32_t T) {
   L.avals = L.akeys + align256(static_cast<size_t>(T) * 4);
   L.bvals = L.avals + align256(static_cast<size_t>(T) * 4);
   L.flags = L.bvals + align256(static_cast<size_t>(T) * 4);
-  L.total = L.flags + align256(dm::refit_flags_words(T) * 4);
+  L.tribox = L.flags + align256(dm::refit_flags_words(T) * 4);
+  L.total = L.tribox + align256(static_cast<size_t>(T) * 24);
   return L;
 }
 
@@ -203,8 +204,16 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   // vertices again
   float* cent = at<float>(base, L.akeys);
   const size_t cstride = (L.avals - L.akeys) / 4;
+  // Meshes with few shared vertices (triangle soups: V >= 2T) store each
+  // triangle's box too, so that the refit reads one box per leaf instead of
+  // gathering three scattered vertices in sorted order (4M-triangle soup:
+  // refit 0.89 -> 0.63 ms).  Where vertices are shared the gathers are
+  // cache-friendly and the extra store costs more than it saves (2M torus:
+  // +8 us in the centroid pass, -3 us in the refit).
+  float* tribox = num_vtx >= 2ull * T ? at<float>(base, L.tribox) : nullptr;
   dm::launch_centroid_aabb(s, T, tri2vtx, num_vtx, vtx2xyz, at<float>(base, L.partials),
-                           at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status, cent, cstride);
+                           at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status, cent, cstride,
+                           tribox);
   dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status, cent, cstride, L.radix10);
   if (tri2morton_out) DM_CUDA(cudaMemcpyAsync(tri2morton_out, codes, size_t{4} * T, cudaMemcpyDeviceToDevice, s));
   // 3 passes: codes -> (ak, av) -> (codes, bv) -> (ok, ov), by default the A
@@ -222,7 +231,7 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   if (ev) DM_CUDA(cudaEventRecord(ev[3], s));
   // the height is only computed on request: it needs the tree-order climb
   dm::launch_refit_windowed(s, T, dm::Segments{1, nullptr, nullptr}, num_vtx, bvhnodes, other_end, tri2vtx, vtx2xyz,
-                            nullptr, aabb, flags, height_out ? height : nullptr, status);
+                            nullptr, aabb, flags, height_out ? height : nullptr, status, tribox);
   if (ev) DM_CUDA(cudaEventRecord(ev[4], s));
   if (transform_out) DM_CUDA(cudaMemcpyAsync(transform_out, transform, 64, cudaMemcpyDeviceToDevice, s));
   if (height_out) DM_CUDA(cudaMemcpyAsync(height_out, height, 4, cudaMemcpyDeviceToDevice, s));

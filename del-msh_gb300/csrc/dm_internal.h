@@ -25,10 +25,12 @@ constexpr int kAabbBlocks = 1024;  // upper bound on centroid-AABB reduction blo
 // (16 floats, column-major).  partials: kAabbBlocks*6 floats; ticket: one u32
 // that is zero on entry and left zero.  With cent != nullptr the centroids
 // are also stored, x, y and z each as num_tri floats (cent, cent + stride,
-// cent + 2 * stride).
+// cent + 2 * stride); with tribox != nullptr each triangle's box (6 floats,
+// the leaf box of the refit) too.
 void launch_centroid_aabb(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
                           const float* vtx2xyz, float* partials, uint32_t* ticket, float* aabb_out,
-                          float* transform_out, uint32_t* status, float* cent = nullptr, size_t stride = 0);
+                          float* transform_out, uint32_t* status, float* cent = nullptr, size_t stride = 0,
+                          float* tribox = nullptr);
 
 // Triangle-centroid Morton codes; when hist != nullptr also accumulates the
 // digit histograms of the radix sort (hist10: u32[3][1024] for three 10-bit
@@ -103,10 +105,13 @@ inline size_t refit_seg_words(uint32_t total_tri) {
               (size_t{2} << refit_top_log(total_tri)));
 }
 inline size_t refit_flags_words(uint32_t total_tri) { return refit_seg_offset(total_tri) + refit_seg_words(total_tri); }
+// tribox (optional, one mesh and vtx2xyz1 == nullptr only): each triangle's
+// box, 6 floats in triangle order, as launch_centroid_aabb stores them; the
+// leaf boxes are then read instead of gathered from the vertices.
 void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
                            const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
                            const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
-                           uint32_t* height_out, uint32_t* status);
+                           uint32_t* height_out, uint32_t* status, const float* tribox = nullptr);
 
 // ----------------------------------------------------------------- sort.cu
 constexpr int kSortTile = 3840;  // keys per onesweep tile
