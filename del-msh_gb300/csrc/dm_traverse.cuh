@@ -547,8 +547,9 @@ __global__ void __launch_bounds__(kCastThreads) k_cast_deep(Job job, const uint3
 }
 
 // ------------------------------------------------------------ warp tier
-// Rays that overflowed the persistent cast's stack or ran past its step
-// budget, one warp each.  Every lane runs the same serial traversal on the
+// Rays that overflowed the persistent cast's stack, or that were about to
+// enter a long chain past its step budget once their warp had no more rays to
+// take, one warp each.  Every lane runs the same serial traversal on the
 // same state (the same loads, the same decisions), except at a chain: a run
 // of links, branches j whose left child is leaf j and right child branch
 // j + 1 (runs of equal Morton codes build them).  The recursion's result over
