@@ -227,7 +227,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_topology(uint32_t total_bran
 // (an equal share of positions each, SegSplit), exchanging keys through
 // distributed shared memory.  Per mesh:
 //   fit      centroid AABB (the same operations as k_batch_fit), combined
-//            over the cluster, and the fit transform
+//            over the cluster, and the fit transform; the centroids wait in
+//            the (still empty) sort buffers
 //   codes    Morton code of every centroid, stored at the triangle's position
 //   4 passes stable LSD radix sort on 8-bit digits: warp ballots rank each
 //            key within its warp (as k_onesweep), per-warp and per-block
@@ -240,8 +241,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_topology(uint32_t total_bran
 constexpr int kSegThreads = 1024;
 constexpr int kSegWarps = kSegThreads / 32;
 constexpr uint32_t kSegCap = 16384;                         // keys per block
-constexpr uint32_t kSegWarpKeys = kSegCap / kSegWarps;      // 1024 keys per warp
-constexpr int kSegSlots = static_cast<int>(kSegWarpKeys / 32);  // 32 keys per lane
+constexpr uint32_t kSegWarpKeys = kSegCap / kSegWarps;      // at most 512 keys per warp
+constexpr int kSegSlots = static_cast<int>(kSegWarpKeys / 32);  // at most 16 keys per lane
 constexpr int kSegUnroll = 2;                                 // triangles gathered together per thread
 static_assert(kSegMaxTri == 4 * kSegCap, "clusters of up to four blocks");
 static_assert(kSegMaxTri <= 65536, "triangle indices are held in 16 bits");
