@@ -44,10 +44,11 @@ METRIC = "rays/s (LBVH build + cast per step)"
 UNIT = "rays/s"
 IMG_W, IMG_H = 1920, 1080
 # kernels of this repo launched per single-mesh step: build = centroid AABB,
-# Morton, 4 sort passes, topology, 5 refit kernels (window, superblock,
-# crossing, and the tree-order climb's two, which exit at once without NaN);
-# cast = persistent traversal + 2 overflow tiers (exit at once when empty)
-KERNELS_PER_STEP = 16
+# Morton, 4 sort passes, topology, 6 refit kernels (window, superblock, the
+# two crossing-branch kernels, and the tree-order climb's two, which exit at
+# once without NaN); cast = persistent traversal + the warp tier + 2 serial
+# overflow tiers (the last three exit at once when their lists are empty)
+KERNELS_PER_STEP = 17
 NDIV = 1024
 SEED = 0
 L2_FLUSH_BYTES = 256 << 20
