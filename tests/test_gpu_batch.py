@@ -192,3 +192,35 @@ def test_full_config4_batched(cuda, oracle):
         assert np.array_equal(p2t[m], r_p2t), m
         assert np.array_equal(tt[m], bits(r_tt)), m
     assert _native.device_status(clear=True) == 0
+
+
+def test_batch_cast_through_warp_tier(cuda, oracle):
+    """The batched cast with a one-entry step budget: rays of the soups that
+    reach long runs of chain links go through the warp tier (BatchJob), and
+    every image still equals the oracle's bit for bit."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.batch import MeshBatch, ortho_transforms
+    meshes = [W.clustered_soup(8_000, num_cluster=2, seed=6), _torus(64, 32, 7),
+              W.clustered_soup(20_000, num_cluster=3, seed=8), W.icosphere(2)]
+    b = MeshBatch(meshes)
+    b.build()
+    tf = ortho_transforms(meshes)
+    b.alloc_cast(48, 40)
+    before = _native.get_tuning()
+    try:
+        _native.set_tuning(**dict(before, cast_long_steps=1))
+        p2t, tt = b.cast_pixels(torch.from_numpy(tf).to("cuda:0"))
+        torch.cuda.synchronize()
+    finally:
+        _native.set_tuning(**before)
+    p2t, tt = to_np(p2t, torch), bits(to_np(tt, torch))
+    hits = 0
+    for m, (tri, vtx) in enumerate(meshes):
+        ref = oracle.build(tri, vtx)
+        r_p2t, r_tt = oracle.pix2tri(tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"], tf[m], 48, 40)
+        assert np.array_equal(p2t[m], r_p2t), m
+        assert np.array_equal(tt[m], bits(r_tt)), m
+        hits += int((r_p2t != 0xFFFFFFFF).sum())
+    assert hits > 1000
+    assert _native.device_status(clear=True) == 0
