@@ -91,3 +91,24 @@ def test_t_error_against_f64(oracle):
         t64 = oracle.tri3_ray_f64(vtx[tri[it][0]], vtx[tri[it][1]], vtx[tri[it][2]], o, d)
         worst = max(worst, abs(float(tt.reshape(-1)[i]) - t64) / abs(t64))
     assert worst < 1e-5
+
+
+def test_chain_link_boxes_are_suffix_unions(oracle):
+    """On a duplicate-heavy soup, every chain link j (leaf j left, branch j + 1
+    right) has the box from_two_aabbs(leaf j, branch j + 1), i.e. the
+    first-wins union of its leaf and the rest of the chain: within a run of
+    links the boxes are suffix unions of the sorted leaf boxes, the identity a
+    run-wise suffix scan of the refit would rest on."""
+    tri, vtx = W.clustered_soup(60_000, num_cluster=4, seed=2)
+    r = oracle.build(tri, vtx)
+    bvh, box = r["bvhnodes"].astype(np.int64), r["bvhnode2aabb"]
+    T = tri.shape[0]
+    j = np.arange(T - 1)
+    link = (bvh[j, 1] == T - 1 + j) & (bvh[j, 2] == j + 1)
+    j = j[link]
+    assert j.size > T // 4
+    a, b = box[T - 1 + j], box[j + 1]  # leaf j, branch j + 1
+    lo = np.where(b[:, :3] < a[:, :3], b[:, :3], a[:, :3])  # the first box wins ties (and -0/+0)
+    hi = np.where(b[:, 3:] > a[:, 3:], b[:, 3:], a[:, 3:])
+    want = np.concatenate([lo, hi], axis=1)
+    assert np.array_equal(box[j].view(np.uint32), want.astype(np.float32).view(np.uint32))
