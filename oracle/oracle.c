@@ -466,6 +466,8 @@ typedef struct {
   const uint32_t* bvhnodes;
   const float* aabb;
   float org[3], dir[3], inv[3];
+  uint64_t* n_branch; /* optional work counters (or_pix2tri_work); NULL when not counting */
+  uint64_t* n_leaf;
 } RayCtx;
 
 static void ray_ctx_init(RayCtx* c, const float org[3], const float dir[3]) {
@@ -497,6 +499,7 @@ static int first_hit(const RayCtx* c, uint32_t node, float dis, float* t_out, ui
   if (bn[node * 3 + 2] == OR_UMAX) {
     const uint32_t it = bn[node * 3 + 1];
     float t;
+    if (c->n_leaf) ++*c->n_leaf;
     if (!tri_hit(c, it, &t)) return 0;
     if (!(t < dis)) return 0;
     *t_out = t;
@@ -504,6 +507,7 @@ static int first_hit(const RayCtx* c, uint32_t node, float dis, float* t_out, ui
     return 1;
   }
   const uint32_t l = bn[node * 3 + 1], r = bn[node * 3 + 2];
+  if (c->n_branch) ++*c->n_branch;
   float tl0 = 0, tl1 = 0, tr0 = 0, tr1 = 0;
   const int hl = slab(c, l, &tl0, &tl1), hr = slab(c, r, &tr0, &tr1);
   int near_is_left;
@@ -555,7 +559,7 @@ static int first_hit(const RayCtx* c, uint32_t node, float dis, float* t_out, ui
 int or_first_intersection_ray(const float org[3], const float dir[3], const uint32_t* tri2vtx, const float* vtx2xyz,
                               const uint32_t* bvhnodes, const float* bvhnode2aabb, uint32_t i_bvhnode, float dis,
                               float* t_out, uint32_t* tri_out) {
-  RayCtx c = {tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, {0}, {0}, {0}};
+  RayCtx c = {tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, {0}, {0}, {0}, NULL, NULL};
   ray_ctx_init(&c, org, dir);
   return first_hit(&c, i_bvhnode, dis, t_out, tri_out);
 }
@@ -583,7 +587,7 @@ static void all_hits(const RayCtx* c, uint32_t node, float* ht, uint32_t* hi, ui
 uint32_t or_intersections_ray(const float org[3], const float dir[3], const uint32_t* tri2vtx, const float* vtx2xyz,
                               const uint32_t* bvhnodes, const float* bvhnode2aabb, float* hit_t, uint32_t* hit_tri,
                               uint32_t cap) {
-  RayCtx c = {tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, {0}, {0}, {0}};
+  RayCtx c = {tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, {0}, {0}, {0}, NULL, NULL};
   ray_ctx_init(&c, org, dir);
   uint32_t cnt = 0;
   all_hits(&c, 0, hit_t, hit_tri, cap, &cnt);
@@ -668,6 +672,27 @@ void or_cast_rays(uint32_t num_ray, const float* ray_org, const float* ray_dir, 
                   float* hit_t, int num_threads) {
   CastJob job = {num_ray, 1, 0, 0, NULL, ray_org, ray_dir, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, hit_tri, hit_t, 0};
   run_cast_job(&job, num_threads);
+}
+
+/* The work of first_hit over a pixel grid, one thread: out[0] rays, out[1]
+ * branches entered (each tests its two children's boxes), out[2] triangles
+ * tested (leaves whose box the ray enters).  The GPU traversal makes the same
+ * decisions, so these are its node visits and triangle tests too. */
+void or_pix2tri_work(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], const uint32_t* tri2vtx,
+                     const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb, uint64_t out[3]) {
+  uint64_t n_branch = 0, n_leaf = 0;
+  const uint32_t num = img_w * img_h;
+  for (uint32_t i = 0; i < num; ++i) {
+    float org[3], dir[3], t;
+    uint32_t it;
+    or_ray_for_pixel(i, img_w, img_h, t_ndc2world, org, dir);
+    RayCtx c = {tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, {0}, {0}, {0}, &n_branch, &n_leaf};
+    ray_ctx_init(&c, org, dir);
+    first_hit(&c, 0, INFINITY, &t, &it);
+  }
+  out[0] = num;
+  out[1] = n_branch;
+  out[2] = n_leaf;
 }
 
 /* ------------------------------------------------------------ checkers */

@@ -121,6 +121,11 @@ int or_check_bvh_topology(const uint32_t* bvhnodes, uint32_t num_leaf);
 int or_check_morton_code_range_split(const uint32_t* idx2morton, uint32_t n);
 
 /* Height of the tree (number of nodes on the longest root-to-leaf path). */
+/* first_hit's work over a pixel grid (one thread): rays, branches entered,
+ * triangles tested */
+void or_pix2tri_work(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], const uint32_t* tri2vtx,
+                     const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb, uint64_t out[3]);
+
 /* consumers of a pix2tri image (pix2depth.rs:107-146, pix2tri.rs:176-304) */
 int or_mat4_inverse_pivot(const float m[16], float inv[16]);
 int or_pix2depth(uint32_t img_w, uint32_t img_h, float* pix2depth, const uint32_t* pix2tri, uint32_t num_tri,

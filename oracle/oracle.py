@@ -77,6 +77,8 @@ def lib():
         L.or_qot_check.argtypes = [u32, u32, _u32p, _f32p, _u32p, _u32p, _f32p, u32, u32]
         L.or_interpolate_bwd.argtypes = [u32, u32, _u32p, u32, _u32p, u32, _f32p, u32, _f32p, _f32p, _f32p, _f32p,
                                          _f32p]
+        L.or_pix2tri_work.argtypes = [u32, u32, _f32p, _u32p, _f32p, _u32p, _f32p,
+                                      np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]
         _lib = L
     return _lib
 
@@ -202,6 +204,16 @@ def pix2tri(tri2vtx, vtx2xyz, bvhnodes, aabb, t_ndc2world_colmajor, img_w, img_h
                                 tri2vtx.reshape(-1), vtx2xyz.reshape(-1), bvhnodes.reshape(-1), aabb.reshape(-1),
                                 out.reshape(-1), _vp(tt), threads or default_threads())
     return out, tt
+
+
+def pix2tri_work(tri2vtx, vtx2xyz, bvhnodes, aabb, t_ndc2world_colmajor, img_w, img_h):
+    """The recursion's work over a pixel grid: rays, branches entered (two child
+    boxes tested each) and triangles tested, counted on one thread."""
+    out = np.zeros(3, np.uint64)
+    lib().or_pix2tri_work(img_w, img_h, _c(t_ndc2world_colmajor, np.float32).reshape(-1),
+                          _c(tri2vtx, np.uint32).reshape(-1), _c(vtx2xyz, np.float32).reshape(-1),
+                          _c(bvhnodes, np.uint32).reshape(-1), _c(aabb, np.float32).reshape(-1), out)
+    return {"rays": int(out[0]), "branches": int(out[1]), "tri_tests": int(out[2])}
 
 
 def cast_rays(ray_org, ray_dir, tri2vtx, vtx2xyz, bvhnodes, aabb, threads=None):

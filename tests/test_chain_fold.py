@@ -167,3 +167,40 @@ def test_chain_fold_equals_recursion_and_oracle(oracle):
             assert np.float32(a[0]).view(np.uint32) == np.float32(r_t[k]).view(np.uint32), k
             hits += 1
     assert hits > org.shape[0] // 2
+
+
+class CountingCaster(Caster):
+    """The recursion with counters: branches entered and triangles tested."""
+
+    def __init__(self, *a):
+        super().__init__(*a)
+        self.branches = 0
+        self.tri_tests = 0
+
+    def leaf_hit(self, leaf):
+        self.tri_tests += 1
+        return super().leaf_hit(leaf)
+
+    def branch(self, n, f):
+        self.branches += 1
+        return super().branch(n, f)
+
+
+def test_oracle_work_counts_match_recursion(oracle):
+    """or_pix2tri_work's counts (the traversal-bytes figure) equal the
+    restated recursion's, ray by ray summed over a small pinhole image."""
+    tri, vtx = W.jittered_icosphere(3, seed=2)
+    ref = oracle.build(tri, vtx)
+    bvh, aabb = ref["bvhnodes"], ref["bvhnode2aabb"]
+    m = W.pinhole_ndc2world(W.random_viewpoint(3.0, seed=2), aspect=1.0)
+    w = h = 24
+    work = oracle.pix2tri_work(tri, vtx, bvh, aabb, m, w, h)
+    branches = tri_tests = hits = 0
+    for i in range(w * h):
+        org, d = oracle.ray_for_pixel(i, w, h, m)
+        c = CountingCaster(tri, vtx, bvh, aabb, org, d)
+        hits += c.cast(False)[1] != NONE_ID
+        branches += c.branches
+        tri_tests += c.tri_tests
+    assert work == {"rays": w * h, "branches": branches, "tri_tests": tri_tests}
+    assert hits > w * h // 4 and tri_tests >= hits
