@@ -142,13 +142,15 @@ class ClockSampler:
 
 # -------------------------------------------------------------- CPU side
 
-def cpu_step(O, tri, vtx, m, threads: int):
+def cpu_step(O, tri, vtx, m, threads: int, keep=None):
     """One oracle step: build on one thread (as del-msh-cpu), cast on `threads`."""
     t0 = time.perf_counter()
     r = O.build(tri, vtx)
     t1 = time.perf_counter()
-    O.pix2tri(tri, vtx, r["bvhnodes"], r["bvhnode2aabb"], m, IMG_W, IMG_H, threads=threads)
+    out = O.pix2tri(tri, vtx, r["bvhnodes"], r["bvhnode2aabb"], m, IMG_W, IMG_H, threads=threads)
     t2 = time.perf_counter()
+    if keep is not None:
+        keep[:] = [np.asarray(out[0]).reshape(-1).view(np.uint32), np.asarray(out[1]).reshape(-1)]
     return t1 - t0, t2 - t1
 
 
@@ -159,14 +161,15 @@ def cpu_baseline(tri, vtx, m, reps: int = 3):
     threads = O.default_threads()
     cpu_step(O, tri, vtx, m, threads)  # warm-up
     builds, casts = [], []
+    keep = []
     for _ in range(reps):
-        b, c = cpu_step(O, tri, vtx, m, threads)
+        b, c = cpu_step(O, tri, vtx, m, threads, keep=keep)
         builds.append(b)
         casts.append(c)
     b, c = statistics.median(builds), statistics.median(casts)
-    return {"value": IMG_W * IMG_H / (b + c), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"the full step (build on 1 thread, 1920x1080 cast on {threads} threads), median of {reps}",
-            "build_tris_per_s": tri.shape[0] / b, "cast_rays_per_s": IMG_W * IMG_H / c}
+    return ({"value": IMG_W * IMG_H / (b + c), "unit": UNIT, "cores": threads, "kind": "port",
+             "sample": f"the full step (build on 1 thread, 1920x1080 cast on {threads} threads), median of {reps}",
+             "build_tris_per_s": tri.shape[0] / b, "cast_rays_per_s": IMG_W * IMG_H / c}, tuple(keep))
 
 
 # ------------------------------------------------------------- GPU side
@@ -318,6 +321,30 @@ def run_ours(args):
     stage_ms = {k: statistics.mean(r[i] for r in stage_runs)
                 for i, k in enumerate(("morton", "sort", "topology", "refit"))}
 
+    # refit-only deformed frame through the drop-in refit (the reference's
+    # bvhnode2aabb_update_aabb): v += 0.01 sin(phase + frame), resident tree
+    phase = np.random.default_rng(SEED + 7).uniform(0.0, 2.0 * np.pi, V)
+    d_def = torch.from_numpy((vtx + 0.01 * np.sin(phase + 1.0)[:, None]).astype(np.float32)).to(dev)
+    rs = L.dm_bvhnode2aabb_update_aabb_scratch_bytes(T)
+    r_scratch = torch.zeros((rs,), dtype=torch.uint8, device=dev)
+    r_aabb = torch.empty_like(aabb)
+
+    def refit_frame():
+        _native.call("dm_bvhnode2aabb_update_aabb_ex", sp, 2 * T - 1, r_aabb.data_ptr(), bvh.data_ptr(), T,
+                     d_tri.data_ptr(), V, d_def.data_ptr(), None, r_scratch.data_ptr(), rs)
+
+    for _ in range(3):
+        refit_frame()
+    r_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, z in r_ev:
+        flush.zero_()
+        a.record(stream)
+        refit_frame()
+        z.record(stream)
+    torch.cuda.synchronize()
+    refit_frame_ms = statistics.mean(a.elapsed_time(z) for a, z in r_ev)
+    del r_scratch, r_aabb, d_def
+
     # end to end through the public torch API with host buffers
     h_tri = torch.from_numpy(tri.view(np.int32)).pin_memory()
     h_vtx = torch.from_numpy(vtx).pin_memory()
@@ -419,6 +446,11 @@ def run_ours(args):
         "config": config_dict(tri, vtx),
         "build_tris_per_s": world * T / (build_mean * 1e-3), "cast_rays_per_s": world * R / (cast_mean * 1e-3),
         "build_ms": build_mean, "cast_ms": cast_mean, "stage_ms": stage_ms,
+        "refit_frame": {"ms": refit_frame_ms, "tris_per_s": T / (refit_frame_ms * 1e-3),
+                        "api": "dm_bvhnode2aabb_update_aabb_ex (drop-in refit: leaf ranges derived from bvhnodes, "
+                               "then range queries)",
+                        "workload": "deformed frame v += 0.01 sin(phase + 1) of the torus, resident tree, "
+                                    "L2 flushed"},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": f"{peak_kind} hbm_gbs",
                      "algorithmic_bytes": nbytes[dom]},
@@ -438,21 +470,120 @@ def run_ours(args):
         "device_status": status,
         "wall_s": wall,
     }
+    g_p2t = pix2tri.cpu().numpy().view(np.uint32).reshape(-1)
+    g_tt = pix2t.cpu().numpy().reshape(-1)
+    line["t_error_f64"] = {"gpu": t_error_f64(np.asarray(m), IMG_W, IMG_H, g_p2t, g_tt, tri, vtx),
+                           "definition": "relative error of the f32 hit t against the same pixel ray and "
+                                         "Moller-Trumbore formula evaluated in binary64, over every hit pixel"}
     if not args.no_cpu:
-        line["cpu_baseline"] = cpu_baseline(tri, vtx, np.asarray(m))
+        line["cpu_baseline"], (c_p2t, c_tt) = cpu_baseline(tri, vtx, np.asarray(m))
+        line["t_error_f64"]["cpu"] = t_error_f64(np.asarray(m), IMG_W, IMG_H, c_p2t, c_tt, tri, vtx)
+        line["t_error_f64"]["cpu_bits_equal_gpu"] = bool(np.array_equal(c_p2t, g_p2t) and
+                                                         np.array_equal(c_tt.view(np.uint32), g_tt.view(np.uint32)))
+    if not args.no_extras and world == 1:
+        del b_scratch, c_scratch, bvh, aabb, d_tri, d_vtx
+        torch.cuda.synchronize()
+        torch.cuda.empty_cache()
+        line.update(compact_extras(args))
     print(json.dumps(line), flush=True)
     if pg is not None:
         pg.destroy_process_group()
     return 0
 
 
+def t_error_f64(m, img_w, img_h, p2t, tt, tri, vtx):
+    """Max / median / p99 relative error of the f32 hit t of every hit pixel
+    against binary64: the pixel ray (ray_for_pixel's formula) and the
+    Moller-Trumbore t of the hit triangle, both evaluated in float64."""
+    idx = np.flatnonzero(p2t != 0xFFFFFFFF)
+    if idx.size == 0:
+        return {"hits": 0}
+    ih = idx // img_w
+    iw = idx - ih * img_w
+    x0 = 2.0 * (iw + 0.5) / img_w - 1.0
+    y0 = 1.0 - 2.0 * (ih + 0.5) / img_h
+    mm = np.asarray(m, np.float64).reshape(4, 4).T  # column-major storage -> row-major matrix
+    one = np.ones_like(x0)
+    q0 = np.stack([x0, y0, one, one], 1) @ mm.T
+    q1 = np.stack([x0, y0, -one, one], 1) @ mm.T
+    org = q0[:, :3] / q0[:, 3:4]
+    d = q1[:, :3] / q1[:, 3:4] - org
+    t3 = tri[p2t[idx]].astype(np.int64)
+    v = vtx.astype(np.float64)
+    p0, p1, p2 = v[t3[:, 0]], v[t3[:, 1]], v[t3[:, 2]]
+    e1, e2 = p1 - p0, p2 - p0
+    pv = np.cross(d, e2)
+    det = (e1 * pv).sum(1)
+    qv = np.cross(org - p0, e1)
+    t64 = (e2 * qv).sum(1) / det
+    rel = np.abs(tt[idx].astype(np.float64) - t64) / np.abs(t64)
+    return {"hits": int(idx.size), "max_rel": float(rel.max()), "median_rel": float(np.median(rel)),
+            "p99_rel": float(np.percentile(rel, 99))}
+
+
+def compact_extras(args):
+    """The other spec workloads, measured after the headline step in the
+    same process and reported as compact keys of the same line: the ragged
+    batch (graph replay against the plain per-mesh path), the served stream
+    (p50/p99 at 0.5x and 0.8x of the plain path's capacity) and the
+    adversarial soup (build and cast times).  A failure is reported in the key
+    instead of aborting the line."""
+    out = {}
+    try:
+        bt = measure_batched(4096, steps=10, warmup=2, plain_steps=2)
+        out["batched"] = {"num_mesh": bt["config"]["num_mesh"], "total_tri": bt["config"]["total_tri"],
+                          "rays_per_step": bt["config"]["rays_per_step"],
+                          "graph_ms_per_step": bt["batched_graph"]["ms_per_step"],
+                          "graph_rays_per_s": bt["batched_graph"]["rays_per_s"],
+                          "graph_tris_per_s": bt["batched_graph"]["tris_per_s"],
+                          "plain_ms_per_step": max(bt["plain"]["ms_per_step_device"], bt["plain"]["ms_per_step_wall"]),
+                          "plain_rays_per_s": bt["plain"]["rays_per_s"],
+                          "speedup_vs_plain": bt["speedup_vs_plain"],
+                          "outputs_identical_to_plain": bt["outputs_identical_to_plain"],
+                          "device_status": bt["device_status"]}
+    except Exception as e:  # noqa: BLE001 - reported, not raised
+        out["batched"] = {"error": f"{type(e).__name__}: {e}"}
+    try:
+        sv = measure_served(512, 600, [0.5, 0.8], 8, 120.0)
+        loads = []
+        for ld in sv["loads"]:
+            e = {"fraction_of_plain_capacity": ld["fraction_of_plain_capacity"], "offered_rps": ld["offered_rps"],
+                 "served_p50_ms": ld["served"]["p50_ms"], "served_p99_ms": ld["served"]["p99_ms"],
+                 "served_rays_per_s": ld["served_rays_per_s"]}
+            if "plain" in ld:
+                e.update({"plain_p50_ms": ld["plain"]["p50_ms"], "plain_p99_ms": ld["plain"]["p99_ms"],
+                          "plain_rays_per_s": ld["plain_rays_per_s"],
+                          "served_p99_below_plain_p50": ld["served_p99_below_plain_p50"]})
+            loads.append(e)
+        out["served"] = {"pool": sv["config"]["pool"], "total_tri": sv["config"]["total_tri"],
+                         "plain_capacity_rps": sv["plain_capacity_rps"],
+                         "served_capacity_rps": sv["served_capacity_rps"], "loads": loads,
+                         "requests_per_trace": sv["config"]["requests_per_trace"],
+                         "device_status": sv["device_status"]}
+    except Exception as e:  # noqa: BLE001
+        out["served"] = {"error": f"{type(e).__name__}: {e}"}
+    try:
+        sp = measure_soup(steps=5, warmup=3, cpu=False)
+        out["soup"] = {"num_tri": sp["config"]["num_tri"], "rays": sp["config"]["rays"], "build_ms": sp["build_ms"],
+                       "cast_ms": sp["cast_ms"], "rays_per_s": sp["value"],
+                       "build_roofline_frac": sp["build_roofline_frac"], "device_status": sp["device_status"]}
+    except Exception as e:  # noqa: BLE001
+        out["soup"] = {"error": f"{type(e).__name__}: {e}"}
+    return out
+
+
 def run_batched(args):
-    """Config 4: 4096 seeded jittered icospheres / tori, triangle counts
-    log-uniform in [64, 65536], each with its own 64x64 orthographic image.
-    One step = build every tree + cast every image.  Timed three ways on the
-    same GPU: the plain path (one launch sequence per mesh through the
-    single-mesh entry points), the batched entry points called eagerly, and
-    the batched step replayed from a CUDA graph."""
+    print(json.dumps(measure_batched(args.num_mesh, args.steps, args.warmup)), flush=True)
+    return 0
+
+
+def measure_batched(num_mesh: int, steps: int, warmup: int, plain_steps: int | None = None):
+    """Ragged batch: ``num_mesh`` seeded jittered icospheres / tori, triangle
+    counts log-uniform in [64, 65536] (37.9M triangles for 4096 meshes), each
+    with its own 64x64 orthographic image.  One step = build every tree + cast
+    every image.  Timed three ways on the same GPU: the plain path (one launch
+    sequence per mesh through the single-mesh entry points), the batched entry
+    points called eagerly, and the batched step replayed from a CUDA graph."""
     import torch
     from del_msh_gb300 import _native
     from del_msh_gb300 import workloads as W
@@ -461,7 +592,7 @@ def run_batched(args):
     torch.cuda.set_device(dev)
     _native.load(build_if_missing=True)
     t0 = time.perf_counter()
-    meshes = W.ragged_batch(num_mesh=args.num_mesh, tmin=64, tmax=65536, seed=SEED)
+    meshes = W.ragged_batch(num_mesh=num_mesh, tmin=64, tmax=65536, seed=SEED)
     gen_s = time.perf_counter() - t0
     b = MeshBatch(meshes, dev)
     tf = torch.from_numpy(ortho_transforms(meshes)).to(dev)
@@ -495,22 +626,22 @@ def run_batched(args):
         b.cast_pixels(tf)
         torch.cuda.nvtx.range_pop()
 
-    for _ in range(max(1, args.warmup // 2)):
+    for _ in range(max(1, warmup // 2)):
         plain_step()
         batch_step()
     b.capture(tf)
     b.replay()
     torch.cuda.synchronize()
-    plain_ms, plain_wall = timed(plain_step, max(2, args.steps // 10))
-    eager_ms, eager_wall = timed(batch_step, args.steps)
-    graph_ms, graph_wall = timed(b.replay, args.steps)
+    plain_ms, plain_wall = timed(plain_step, plain_steps or max(2, steps // 10))
+    eager_ms, eager_wall = timed(batch_step, steps)
+    graph_ms, graph_wall = timed(b.replay, steps)
     match = bool(torch.equal(b.pix2tri.view(torch.int32), plain.pix2tri.view(torch.int32)) and
                  torch.equal(b.pix2t, plain.pix2t))
     status = _native.device_status(clear=True)
     plain_eff = max(plain_ms, plain_wall)
     line = {
         "metric": "rays/s (batched LBVH build + cast of ragged meshes)", "unit": UNIT,
-        "value": R / (graph_ms * 1e-3), "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "value": R / (graph_ms * 1e-3), "n_gpus": 1, "steps": steps, "warmup": warmup,
         "ms_per_step": graph_ms, "higher_is_better": True, "dtype": "f32/u32",
         "data": "synthetic (seeded jittered icospheres / tori)",
         "config": {"workload": f"{b.num_mesh} ragged meshes, triangle counts log-uniform in [64, 65536], "
@@ -526,11 +657,18 @@ def run_batched(args):
         "speedup_vs_plain": plain_eff / max(graph_ms, graph_wall),
         "outputs_identical_to_plain": match, "device_status": status,
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    del b, plain
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return line
 
 
 def run_served(args):
+    print(json.dumps(measure_served(args.pool, args.requests, args.loads, args.slots, args.budget_gb)), flush=True)
+    return 0
+
+
+def measure_served(pool: int, requests: int, loads, slots: int, budget_gb: float):
     """Served configuration: a pool of 512 seeded icospheres / tori (triangle
     counts log-uniform in [1k, 1M]), Poisson arrivals, 20% build + 512x512
     cast, 60% refit + re-cast after a per-frame deformation of the resident
@@ -544,16 +682,16 @@ def run_served(args):
     torch.cuda.set_device(0)
     _native.load(build_if_missing=True)
     t0 = time.perf_counter()
-    wl = ServedWorkload(num_mesh=args.pool, tmin=1000, tmax=1_000_000, img=512, num_ray=16384, seed=SEED)
+    wl = ServedWorkload(num_mesh=pool, tmin=1000, tmax=1_000_000, img=512, num_ray=16384, seed=SEED)
     gen_s = time.perf_counter() - t0
-    n = args.requests
+    n = requests
     out = {"metric": "served requests: p50/p99 latency and rays/s against the plain serial path", "unit": "ms",
-           "config": {"pool": args.pool, "total_tri": int(sum(t.shape[0] for t, _ in wl.meshes)),
+           "config": {"pool": pool, "total_tri": int(sum(t.shape[0] for t, _ in wl.meshes)),
                       "max_tri": wl.max_tri, "mix": "20% build+cast 512^2, 60% refit+re-cast, 20% cast 16k rays",
-                      "budget_gb": args.budget_gb, "slots": args.slots, "requests_per_trace": n,
+                      "budget_gb": budget_gb, "slots": slots, "requests_per_trace": n,
                       "generation_s": gen_s}, "data": "synthetic (seeded jittered icospheres / tori)",
            "loads": []}
-    with Server(budget_bytes=int(args.budget_gb * (1 << 30)), num_slots=args.slots, max_tri=wl.max_tri,
+    with Server(budget_bytes=int(budget_gb * (1 << 30)), num_slots=slots, max_tri=wl.max_tri,
                 max_out=wl.max_out) as srv:
         wl.register_all(srv)
         # capacities: a closed burst (all arrivals at t=0) through each path
@@ -567,7 +705,7 @@ def run_served(args):
         served_cap = n / served_burst["span_s"]
         out["plain_capacity_rps"] = plain_cap
         out["served_capacity_rps"] = served_cap
-        for frac in args.loads:
+        for frac in loads:
             rate = frac * plain_cap
             reqs, arr = wl.stream(n, rate)
             rays = sum(r.num_ray if r.kind == 2 else r.img_w * r.img_h for r in reqs)
@@ -585,8 +723,11 @@ def run_served(args):
         out["server_stats"] = srv.stats()
     from del_msh_gb300 import _native as N
     out["device_status"] = N.device_status(clear=True)
-    print(json.dumps(out), flush=True)
-    return 0
+    del wl
+    import torch
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return out
 
 
 def run_render(args):
@@ -805,6 +946,11 @@ def run_selfx(args):
 
 
 def run_soup(args):
+    print(json.dumps(measure_soup(args.steps, args.warmup, cpu=not args.no_cpu)), flush=True)
+    return 0
+
+
+def measure_soup(steps: int, warmup: int, cpu: bool):
     """Adversarial Morton distribution: 4,194,304-triangle soup whose centroids
     come from 32 Gaussian clusters (sigma 1e-3 in the unit cube), so many
     30-bit codes repeat and duplicate runs become long chains in the tree.
@@ -846,12 +992,12 @@ def run_soup(args):
                      aabb.data_ptr(), c_scr.data_ptr(), cs)
 
     build(want_height=True)
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         build()
         cast()
     torch.cuda.synchronize()
-    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(args.steps)]
-    for k in range(args.steps):
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(steps)]
+    for k in range(steps):
         flush.zero_()
         ev[k][0].record(stream)
         build()
@@ -870,7 +1016,7 @@ def run_soup(args):
     peak, _ = peaks()
     nb = algorithmic_bytes(T, V, R)
     line = {"metric": "rays/s (adversarial soup: build + cast per step)", "unit": UNIT,
-            "value": R / ((b_ms + c_ms) * 1e-3), "ms_per_step": b_ms + c_ms, "steps": args.steps,
+            "value": R / ((b_ms + c_ms) * 1e-3), "ms_per_step": b_ms + c_ms, "steps": steps,
             "config": {"workload": "4,194,304-triangle soup in 32 Gaussian clusters (sigma 1e-3), 1,048,576 "
                                    "cube-boundary rays", "num_tri": T, "num_vtx": V, "rays": R,
                        "tree_height": int(height.item()), "l2": "flushed between timed steps"},
@@ -880,7 +1026,7 @@ def run_soup(args):
                          for i, k in enumerate(("morton", "sort", "topology", "refit"))},
             "build_roofline_frac": nb["build"] / (b_ms * 1e-3) / 1e9 / peak,
             "hits": int((hit != -1).sum().item()), "device_status": _native.device_status(clear=True)}
-    if not args.no_cpu:
+    if cpu:
         from oracle import build as obuild
         from oracle import oracle as O
         obuild.build_oracle()
@@ -891,8 +1037,10 @@ def run_soup(args):
         t2 = time.perf_counter()
         line["cpu_baseline"] = {"build_s": t1 - t0, "cast_s": t2 - t1, "cores": O.default_threads(), "kind": "port",
                                 "value": R / (t2 - t0), "unit": UNIT}
-    print(json.dumps(line), flush=True)
-    return 0
+    del d_tri, d_vtx, d_org, d_dir, bvh, aabb, hit, ht, b_scr, c_scr, flush
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return line
 
 
 def read_traffic(kernel: str):
@@ -915,6 +1063,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the batched / served / soup keys of the default line")
     ap.add_argument("--workload", choices=["single", "batched", "served", "soup", "render", "octree", "selfx"],
                     default="single")
     ap.add_argument("--num-mesh", type=int, default=4096, help="meshes of the batched workload")

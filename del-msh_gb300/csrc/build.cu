@@ -343,7 +343,10 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
                                                    const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
                                                    const float* __restrict__ vtx2xyz0,
                                                    const float* __restrict__ vtx2xyz1, float* aabb, uint32_t* flags,
-                                                   uint32_t* height_out, uint32_t* status) {
+                                                   uint32_t* height_out, uint32_t* status, const uint32_t* gate) {
+  // gated (drop-in refit): runs only when the tree was found not to be in
+  // Karras leaf order, so that the range queries could not do the call
+  if (gate != nullptr && (*reinterpret_cast<const volatile uint32_t*>(gate) & kRefitPlainClimb) == 0u) return;
   const uint32_t ii = blockIdx.x * kThreads + threadIdx.x;
   if (ii >= num_tri) return;
   const uint32_t num_node = 2 * num_tri - 1;
@@ -484,8 +487,11 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, S
                                                           uint32_t* height_out, uint32_t* status) {
   pdl_wait();
   pdl_launch_dependents();
-  // runs only when the range-query refit handed over (NaN) or heights are wanted
-  if (*reinterpret_cast<volatile uint32_t*>(queue + 1) == 0u) return;
+  // runs only when the range-query refit handed over (NaN) or heights are
+  // wanted, and not for a tree that is not in Karras leaf order (the plain
+  // climb of k_refit does that call)
+  const uint32_t climb_flag = *reinterpret_cast<volatile uint32_t*>(queue + 1);
+  if (climb_flag == 0u || (climb_flag & kRefitPlainClimb) != 0u) return;
   extern __shared__ __align__(16) unsigned char win_raw[];
   WinSmem& S = *reinterpret_cast<WinSmem*>(win_raw);
   // persistent over the windows: when the range queries did the work, the
@@ -1280,7 +1286,7 @@ void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, con
 void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
                            const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
                            const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
-                           uint32_t* height_out, uint32_t* status, const float* tribox) {
+                           uint32_t* height_out, uint32_t* status, const float* tribox, bool header_ready) {
   if (total_tri == 0) return;
   if (seg.tri_off || vtx2xyz1) tribox = nullptr;  // one mesh, one vertex state only
   const int smem = static_cast<int>(sizeof(WinSmem));
@@ -1304,7 +1310,7 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
     configured[dev] = true;
   }
   const uint32_t sms = (dev >= 0 && dev < 64 && sm_count[dev] > 0) ? static_cast<uint32_t>(sm_count[dev]) : 152u;
-  cudaMemsetAsync(queue, 0, kRefitQueueHdr * sizeof(uint32_t), s);
+  if (!header_ready) cudaMemsetAsync(queue, 0, kRefitQueueHdr * sizeof(uint32_t), s);
   if (height_out) cudaMemsetAsync(queue + 1, 1, sizeof(uint32_t), s);  // heights come from the climb
   const uint32_t top_grid = (capacity + 127) / 128;
   // persistent grids: the crossing list is short, and the climb usually exits at once
@@ -1348,10 +1354,112 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
 
 void launch_refit(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,
                   uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
-                  uint32_t* height_out, uint32_t* status) {
+                  uint32_t* height_out, uint32_t* status, const uint32_t* gate) {
   const uint32_t grid = (num_tri + kThreads - 1) / kThreads;
   k_refit<<<grid, kThreads, 0, s>>>(num_tri, bvhnodes, tri2vtx, num_vtx, vtx2xyz0, vtx2xyz1, aabb, flags, height_out,
-                                    status);
+                                    status, gate);
+}
+
+// ------------------------------------------- refit of a tree given as bvhnodes
+// The drop-in refit gets a tree and nothing else.  The range queries need
+// each branch's leaf range; in a Karras tree a branch's index is one end of
+// its range, and the other end is found from the records alone: a branch
+// that is its parent's left child is the right end of its range, whose left
+// end is the leaf at the bottom of its left spine (left child, left child,
+// ...); a right child is the left end, and the right end ends its right
+// spine.  k_refit_derive_ends walks that spine (at most kSpineWalk records);
+// k_refit_check_ends then checks that every branch's two children split its
+// range exactly, [lo, m] and [m+1, hi], and that the root spans every leaf.
+// By induction from the leaves every range is then the subtree's leaf
+// interval, so the range queries give the climb's boxes.  Anything else (a
+// tree not in Karras leaf order, malformed records, or a spine longer than
+// the walk) sets kRefitPlainClimb in the refit header: the range-query
+// kernels exit at once and the parent-pointer climb k_refit does the call.
+constexpr uint32_t kSpineWalk = 64;
+
+__global__ void __launch_bounds__(kThreads) k_refit_derive_ends(uint32_t num_tri, const uint32_t* __restrict__ bn,
+                                                                uint32_t* __restrict__ other_end, uint32_t* hdr) {
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  const uint32_t nb = num_tri - 1, num_node = 2 * num_tri - 1;
+  if (i >= nb) return;
+  const uint32_t p = __ldg(bn + 3ull * i), c0 = __ldg(bn + 3ull * i + 1), c1 = __ldg(bn + 3ull * i + 2);
+  bool bad = c0 >= num_node || c1 >= num_node;
+  uint32_t oe = i;
+  if (!bad) {
+    const uint32_t k0 = c0 >= nb ? c0 - nb : c0, k1 = c1 >= nb ? c1 - nb : c1;
+    bad = k1 != k0 + 1 || __ldg(bn + 3ull * c0) != i || __ldg(bn + 3ull * c1) != i;
+  }
+  if (!bad) {
+    if (i == 0) {
+      bad = p != kUMax;
+      oe = nb;  // the root spans leaves 0 .. T-1
+    } else if (p >= nb) {
+      bad = true;
+    } else {
+      const uint32_t pl = __ldg(bn + 3ull * p + 1), pr = __ldg(bn + 3ull * p + 2);
+      const int side = pl == i ? 1 : (pr == i ? 2 : 0);  // the spine to walk: left (1) or right (2)
+      if (side == 0) {
+        bad = true;
+      } else {
+        uint32_t x = side == 1 ? c0 : c1, steps = 0;
+        while (x < nb && steps < kSpineWalk) {
+          x = __ldg(bn + 3ull * x + side);
+          ++steps;
+        }
+        if (x < nb || x >= num_node) bad = true;  // spine too long, or a bad index
+        else oe = x - nb;
+      }
+    }
+  }
+  other_end[i] = bad ? i : oe;
+  if (bad) atomicOr(hdr + 1, kRefitPlainClimb);
+}
+
+__global__ void __launch_bounds__(kThreads) k_refit_check_ends(uint32_t num_tri, const uint32_t* __restrict__ bn,
+                                                               const uint32_t* __restrict__ other_end, uint32_t* hdr) {
+  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
+  const uint32_t nb = num_tri - 1, num_node = 2 * num_tri - 1;
+  if (i >= nb) return;
+  if (*reinterpret_cast<const volatile uint32_t*>(hdr + 1) & kRefitPlainClimb) return;
+  const uint32_t c0 = __ldg(bn + 3ull * i + 1), c1 = __ldg(bn + 3ull * i + 2);
+  if (c0 >= num_node || c1 >= num_node) {  // already flagged by the derivation
+    atomicOr(hdr + 1, kRefitPlainClimb);
+    return;
+  }
+  const auto range = [&](uint32_t c, uint32_t& lo, uint32_t& hi) {
+    if (c >= nb) {
+      lo = hi = c - nb;
+    } else {
+      const uint32_t o = __ldg(other_end + c);
+      lo = c < o ? c : o;
+      hi = c < o ? o : c;
+    }
+  };
+  uint32_t lo, hi, lo0, hi0, lo1, hi1;
+  range(i, lo, hi);
+  range(c0, lo0, hi0);
+  range(c1, lo1, hi1);
+  bool ok = lo0 == lo && hi0 + 1 == lo1 && hi1 == hi && hi < num_tri;
+  if (i == 0) ok = ok && lo == 0 && hi == nb;
+  if (!ok) atomicOr(hdr + 1, kRefitPlainClimb);
+}
+
+void launch_refit_any_tree(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,
+                           uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, float* aabb,
+                           uint32_t* other_end, uint32_t* flags, uint32_t* status) {
+  if (num_tri == 0) return;
+  if (num_tri == 1) {  // a single leaf: nothing to climb or query
+    launch_refit(s, num_tri, bvhnodes, tri2vtx, num_vtx, vtx2xyz0, vtx2xyz1, aabb, flags, nullptr, status);
+    return;
+  }
+  uint32_t* hdr = flags + refit_queue_offset(num_tri);
+  cudaMemsetAsync(hdr, 0, kRefitQueueHdr * sizeof(uint32_t), s);
+  const uint32_t grid = (num_tri - 1 + kThreads - 1) / kThreads;
+  k_refit_derive_ends<<<grid, kThreads, 0, s>>>(num_tri, bvhnodes, other_end, hdr);
+  k_refit_check_ends<<<grid, kThreads, 0, s>>>(num_tri, bvhnodes, other_end, hdr);
+  launch_refit_windowed(s, num_tri, Segments{}, num_vtx, bvhnodes, other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb,
+                        flags, nullptr, status, nullptr, /*header_ready=*/true);
+  launch_refit(s, num_tri, bvhnodes, tri2vtx, num_vtx, vtx2xyz0, vtx2xyz1, aabb, flags, nullptr, status, hdr + 1);
 }
 
 }  // namespace dm

@@ -3,6 +3,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <atomic>
 #include <mutex>
 #include <string>
 #include <utility>
@@ -43,6 +44,8 @@ int cuda_fail(cudaError_t e, const char* what) {
 constexpr uint32_t kMaxElems = (1u << 30) - 1;  // sort look-back packs counts in 30 bits
 
 // Device status word: kernels OR error bits into it (see dm::DeviceStatusBits).
+// Its address is looked up once per device and kept for the life of the
+// process, so the library must not be used across a cudaDeviceReset.
 __device__ uint32_t g_status_word;
 
 uint32_t* status_ptr() {
@@ -60,6 +63,13 @@ uint32_t* status_ptr() {
 }
 
 inline size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+
+// Work items of a pixel cast: every image is padded to whole warp tiles of
+// tile_w x (32 / tile_w) pixels, at most (w + 31) x (h + 31) slots whatever
+// the tile shape; the kernels count them in 32 bits.
+inline uint64_t padded_pixel_work(uint32_t img_w, uint32_t img_h, uint32_t num_image) {
+  return (static_cast<uint64_t>(img_w) + 31) * (static_cast<uint64_t>(img_h) + 31) * num_image;
+}
 
 // Temporary device memory: the caller's, or stream-ordered allocation.
 struct Scratch {
@@ -277,6 +287,24 @@ int check_batch(uint32_t num_mesh, const uint32_t* mesh2tri, const uint32_t* mes
 
 }  // namespace
 
+namespace {
+// Scratch of the drop-in refit: the derived other range ends, then the
+// refit's arrival flags, hand-over queue and segment tree.
+size_t refit_any_flags_offset(uint32_t T) { return align256(size_t{4} * T); }
+size_t refit_any_scratch_bytes(uint32_t T) {
+  return refit_any_flags_offset(T) + align256(size_t{4} * dm::refit_flags_words(T));
+}
+
+int refit_any(cudaStream_t s, uint32_t T, const uint32_t* bvhnodes, const uint32_t* tri2vtx, uint32_t V,
+              const float* vtx0, const float* vtx1, float* aabb, void* scratch) {
+  uint32_t* other_end = static_cast<uint32_t*>(scratch);
+  uint32_t* flags = at<uint32_t>(scratch, refit_any_flags_offset(T));
+  dm::launch_refit_any_tree(s, T, bvhnodes, tri2vtx, V, vtx0, vtx1, aabb, other_end, flags, status_ptr());
+  DM_CUDA(cudaGetLastError());
+  return DM_OK;
+}
+}  // namespace
+
 namespace dm {
 
 int set_error(int code, const char* fmt, ...) {
@@ -302,7 +330,11 @@ size_t build_scratch_bytes(uint32_t T) { return build_layout(T).total; }
 namespace {
 std::mutex g_tuning_mutex;
 Tuning g_tuning;
+std::atomic<uint32_t> g_wait_limit{kDefaultWaitLimit};
 }  // namespace
+
+uint32_t get_wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
+void set_wait_limit(uint32_t polls) { g_wait_limit.store(polls, std::memory_order_relaxed); }
 
 Tuning get_tuning() {
   std::lock_guard<std::mutex> lk(g_tuning_mutex);
@@ -370,6 +402,42 @@ int dm_tuning_set(const dm_tuning* in) {
   return DM_OK;
 }
 
+int dm_wait_limit_get(uint32_t* polls) {
+  DM_REQUIRE(polls, "NULL argument");
+  *polls = dm::get_wait_limit();
+  return DM_OK;
+}
+
+int dm_wait_limit_set(uint32_t polls) {
+  dm::set_wait_limit(polls == 0 ? dm::kDefaultWaitLimit : polls);
+  return DM_OK;
+}
+
+size_t dm_selftest_bounded_wait_scratch_bytes(void) { return 4 * (3 * dm::kSortTile + 256 + 2 * 256 + 64); }
+
+int dm_selftest_bounded_wait(uint64_t stream_ptr, uint32_t polls, void* scratch, size_t scratch_bytes) {
+  DM_REQUIRE(polls >= 1 && polls <= (1u << 24), "polls must be in 1..2^24 (got %u)", polls);
+  DM_REQUIRE(scratch, "scratch must not be NULL");
+  const size_t need = dm_selftest_bounded_wait_scratch_bytes();
+  DM_REQUIRE(scratch_bytes >= need, "scratch of %zu bytes is below the %zu needed", scratch_bytes, need);
+  cudaStream_t s = as_stream(stream_ptr);
+  uint32_t* w = static_cast<uint32_t*>(scratch);
+  uint32_t* keys_in = w;                           // kSortTile keys (0)
+  uint32_t* keys_out = keys_in + dm::kSortTile;    // never written (the tile holds no keys)
+  uint32_t* vals_out = keys_out + dm::kSortTile;
+  uint32_t* hist = vals_out + dm::kSortTile;       // 256 digit counts: all keys have digit 0
+  uint32_t* lookback = hist + 256;                 // tiles 0 and 1, zero: tile 0 never publishes
+  uint32_t* counter = lookback + 2 * 256;          // preset to 1: the only block draws tile 1
+  DM_CUDA(cudaMemsetAsync(scratch, 0, need, s));
+  const uint32_t n = dm::kSortTile, one = 1;
+  DM_CUDA(cudaMemcpyAsync(hist, &n, 4, cudaMemcpyHostToDevice, s));
+  DM_CUDA(cudaMemcpyAsync(counter, &one, 4, cudaMemcpyHostToDevice, s));
+  dm::launch_onesweep_wait_probe(s, n, keys_in, keys_out, vals_out, hist, lookback, counter, status_ptr(), polls);
+  DM_CUDA(cudaGetLastError());
+  DM_CUDA(cudaStreamSynchronize(s));  // the host values above are stack copies
+  return DM_OK;
+}
+
 int dm_mortons_vtx2morton_from_vtx2co(uint64_t stream_ptr, uint32_t num_vtx, uint32_t num_dim, const float* vtx2co,
                                       const float* transform_co2unit, uint32_t* vtx2morton) {
   DM_REQUIRE(num_dim == 2 || num_dim == 3, "num_dim must be 2 or 3 (got %u)", num_dim);
@@ -423,18 +491,35 @@ int dm_bvhnode2aabb_update_aabb(uint64_t stream_ptr, uint32_t num_bvhnode, float
   DM_REQUIRE(i_bvhnode == 0, "only i_bvhnode == 0 (the whole tree) is supported");
   DM_REQUIRE(bvhnode2aabb && bvhnodes, "NULL argument");
   cudaStream_t s = as_stream(stream_ptr);
-  Scratch sc;
-  uint32_t* flags = flags_scratch;
-  if (!flags) {
-    bool fresh = false;
-    if (int e = sc.acquire(nullptr, 0, align256(size_t{4} * num_elem), s, &fresh)) return e;
-    flags = static_cast<uint32_t*>(sc.ptr);
-    DM_CUDA(cudaMemsetAsync(flags, 0, size_t{4} * num_elem, s));
+  if (flags_scratch) {  // the caller's arrival flags alone: the parent-pointer climb
+    dm::launch_refit(s, num_elem, bvhnodes, elem2vtx, num_vtx, vtx2xyz0, vtx2xyz1, bvhnode2aabb, flags_scratch,
+                     nullptr, status_ptr());
+    DM_CUDA(cudaGetLastError());
+    return DM_OK;
   }
-  dm::launch_refit(s, num_elem, bvhnodes, elem2vtx, num_vtx, vtx2xyz0, vtx2xyz1, bvhnode2aabb, flags, nullptr,
-                   status_ptr());
-  DM_CUDA(cudaGetLastError());
-  return DM_OK;
+  Scratch sc;
+  bool fresh = false;
+  const size_t need = refit_any_scratch_bytes(num_elem);
+  if (int e = sc.acquire(nullptr, 0, need, s, &fresh)) return e;
+  DM_CUDA(cudaMemsetAsync(static_cast<unsigned char*>(sc.ptr) + refit_any_flags_offset(num_elem), 0,
+                          size_t{4} * num_elem, s));
+  return refit_any(s, num_elem, bvhnodes, elem2vtx, num_vtx, vtx2xyz0, vtx2xyz1, bvhnode2aabb, sc.ptr);
+}
+
+size_t dm_bvhnode2aabb_update_aabb_scratch_bytes(uint32_t num_elem) { return refit_any_scratch_bytes(num_elem); }
+
+int dm_bvhnode2aabb_update_aabb_ex(uint64_t stream_ptr, uint32_t num_bvhnode, float* bvhnode2aabb,
+                                   const uint32_t* bvhnodes, uint32_t num_elem, const uint32_t* elem2vtx,
+                                   uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, void* scratch,
+                                   size_t scratch_bytes) {
+  if (int e = check_mesh(num_elem, elem2vtx, num_vtx, vtx2xyz0)) return e;
+  DM_REQUIRE(num_bvhnode == 2 * num_elem - 1, "num_bvhnode (%u) must be 2*num_elem-1 (%u)", num_bvhnode,
+             2 * num_elem - 1);
+  DM_REQUIRE(bvhnode2aabb && bvhnodes && scratch, "NULL argument");
+  const size_t need = refit_any_scratch_bytes(num_elem);
+  DM_REQUIRE(scratch_bytes >= need, "scratch of %zu bytes is below the %zu needed", scratch_bytes, need);
+  return refit_any(as_stream(stream_ptr), num_elem, bvhnodes, elem2vtx, num_vtx, vtx2xyz0, vtx2xyz1, bvhnode2aabb,
+                   scratch);
 }
 
 size_t dm_trimesh3_build_scratch_bytes(uint32_t num_tri) { return build_layout(num_tri).total; }
@@ -481,6 +566,8 @@ int dm_pix2tri_by_raycast(uint64_t stream_ptr, uint32_t img_w, uint32_t img_h, u
   DM_REQUIRE(bvhnodes && bvhnode2aabb && transform_ndc2world && pix2tri, "NULL argument");
   const uint64_t num_pix = static_cast<uint64_t>(img_w) * img_h;
   DM_REQUIRE(num_pix <= kMaxElems, "image of %llu pixels exceeds the supported maximum", (unsigned long long)num_pix);
+  DM_REQUIRE(padded_pixel_work(img_w, img_h, 1) <= kMaxElems,
+             "image of %u x %u pixels pads to too many tile slots", img_w, img_h);
   if (num_pix == 0) return DM_OK;
   cudaStream_t s = as_stream(stream_ptr);
   const uint32_t n = static_cast<uint32_t>(num_pix);
@@ -732,6 +819,8 @@ int dm_batch_pix2tri_by_raycast(uint64_t stream_ptr, uint32_t num_mesh, const ui
   DM_REQUIRE(max_tri_per_mesh >= 1 && max_tri_per_mesh <= total_tri, "max_tri_per_mesh must be in 1..total_tri");
   const uint64_t num_ray = static_cast<uint64_t>(img_w) * img_h * num_mesh;
   DM_REQUIRE(num_ray <= kMaxElems, "%llu rays exceed the supported maximum", (unsigned long long)num_ray);
+  DM_REQUIRE(padded_pixel_work(img_w, img_h, num_mesh) <= kMaxElems,
+             "%u images of %u x %u pixels pad to too many tile slots", num_mesh, img_w, img_h);
   if (num_ray == 0) return DM_OK;
   cudaStream_t s = as_stream(stream_ptr);
   Scratch sc;

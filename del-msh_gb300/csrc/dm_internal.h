@@ -55,9 +55,11 @@ void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, con
 // Bottom-up refit (bvhnode2aabb.cu:7-65 semantics, values of
 // bvhnode2aabb3.rs:68-142).  flags: u32[num_tri-1], zero on entry, left zero.
 // height_out (optional): number of nodes on the longest root-to-leaf path.
+// gate (optional): a refit header word; the climb then runs only if it has
+// kRefitPlainClimb set (launch_refit_any_tree).
 void launch_refit(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,
                   uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags, uint32_t* height_out,
-                  uint32_t* status);
+                  uint32_t* status, const uint32_t* gate = nullptr);
 
 // Meshes of a batch stored back to back: mesh m owns triangles
 // tri_off[m]..tri_off[m+1]-1 and vertices vtx_off[m]..vtx_off[m+1]-1, and its
@@ -85,6 +87,10 @@ constexpr uint32_t kRefitWindowLog = 9;
 constexpr uint32_t kRefitSuper = 64;        // windows per superblock
 constexpr uint32_t kRefitSuperLog = 15;     // log2(kRefitWindow * kRefitSuper)
 constexpr uint32_t kRefitQueueHdr = 4;      // queue count, climb flag, ticket, spare
+// climb-flag bit: the tree is not in Karras leaf order (or could not be
+// shown to be), so the parent-pointer climb does the refit; bit 0 hands the
+// call to the tree-order climb (NaN leaf boxes, heights)
+constexpr uint32_t kRefitPlainClimb = 2u;
 inline uint32_t refit_num_windows(uint32_t total_tri) { return (total_tri + kRefitWindow - 1) / kRefitWindow; }
 inline uint32_t refit_num_super(uint32_t total_tri) {
   return (refit_num_windows(total_tri) + kRefitSuper - 1) / kRefitSuper;
@@ -111,7 +117,17 @@ inline size_t refit_flags_words(uint32_t total_tri) { return refit_seg_offset(to
 void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
                            const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
                            const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
-                           uint32_t* height_out, uint32_t* status, const float* tribox = nullptr);
+                           uint32_t* height_out, uint32_t* status, const float* tribox = nullptr,
+                           bool header_ready = false);
+// Refit of any tree given as bvhnodes (the drop-in refit): derives every
+// branch's other range end on the device and runs the range-query refit when
+// the tree is in Karras leaf order, else the parent-pointer climb; the choice
+// is made on the device.  other_end: u32[num_tri]; flags:
+// refit_flags_words(num_tri) words whose first num_tri are zero on entry (and
+// left zero).
+void launch_refit_any_tree(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,
+                           uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, float* aabb,
+                           uint32_t* other_end, uint32_t* flags, uint32_t* status);
 
 // ----------------------------------------------------------------- sort.cu
 constexpr int kSortTile = 3840;  // keys per onesweep tile
@@ -149,6 +165,16 @@ void launch_onesweep10_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uin
 void launch_onesweep_u64(cudaStream_t s, uint32_t n, uint32_t shift, const uint64_t* keys_in,
                          const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
                          uint32_t* lookback, uint32_t* tile_counter, uint32_t* status);
+// One pass over one tile with a caller-preset tile counter (see sort.cu):
+// exercises the give-up path of the look-back wait.  lookback: 2*256 words.
+void launch_onesweep_wait_probe(cudaStream_t s, uint32_t n, const uint32_t* keys_in, uint32_t* keys_out,
+                                uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback, uint32_t* tile_counter,
+                                uint32_t* status, uint32_t spin_limit);
+// Polls a bounded device wait makes before it gives up (process-wide; read
+// at each launch).  Default kDefaultWaitLimit.
+constexpr uint32_t kDefaultWaitLimit = 1u << 22;
+uint32_t get_wait_limit();
+void set_wait_limit(uint32_t polls);
 
 // ---------------------------------------------------------------- batch.cu
 // Number of 8-bit passes sorting (mesh << 30 | code) keys of num_mesh meshes.

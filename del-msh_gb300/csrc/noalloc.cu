@@ -13,7 +13,10 @@
 // 4,194,305 triangles; every GPU that loads the library keeps it until the
 // process exits.  Its device address is looked up with cudaGetSymbolAddress
 // the first time the entry point runs on a device (with that device current),
-// so that first call should come before any stream capture.  All calls share
+// so that first call should come before any stream capture.  The address is
+// kept for the life of the process: the library must not be used across a
+// cudaDeviceReset of that device, which unloads the module and leaves the
+// kept address stale.  All calls share
 // the array: each call clears the part it uses, and calls whose work overlaps
 // on the GPU (different streams, or graphs replayed concurrently) race on it.
 #include <mutex>

@@ -413,6 +413,10 @@ int check_request(const dm_server* S, const dm_request* r) {
   const uint64_t n = r->kind == DM_REQ_CAST_RAYS ? r->num_ray : static_cast<uint64_t>(r->img_w) * r->img_h;
   if (n == 0 || n > S->max_out)
     return set_error(DM_ERR_INVALID_ARGUMENT, "request of %llu rays outside 1..%u", (unsigned long long)n, S->max_out);
+  // a pixel cast pads its image to whole warp tiles, counted in 32 bits
+  if (r->kind != DM_REQ_CAST_RAYS && (uint64_t{r->img_w} + 31) * (uint64_t{r->img_h} + 31) > 0xFFFFFFFFull)
+    return set_error(DM_ERR_INVALID_ARGUMENT, "image of %u x %u pixels pads to too many tile slots", r->img_w,
+                     r->img_h);
   if (r->kind == DM_REQ_CAST_RAYS && (!r->ray_org || !r->ray_dir))
     return set_error(DM_ERR_INVALID_ARGUMENT, "ray arrays must not be NULL");
   if (r->kind != DM_REQ_CAST_RAYS && !r->transform_ndc2world)

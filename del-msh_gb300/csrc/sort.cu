@@ -10,8 +10,9 @@
 //
 // The look-back waits on flags written by tiles that started earlier (tile
 // ids are taken in launch order from an atomic counter), and every wait is
-// bounded: after kSpinLimit polls the kernel raises kStatusSpinTimeout and
-// carries on instead of hanging.
+// bounded: after `spin_limit` polls (the process-wide wait limit, by default
+// 2^22, read at each launch) the kernel raises kStatusSpinTimeout and carries
+// on instead of hanging.
 #include "dm_device.cuh"
 #include "dm_internal.h"
 
@@ -24,7 +25,6 @@ constexpr int kKpt = kSortTile / kThreads;  // keys per thread (15)
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kValueMask = (1u << 30) - 1;
-constexpr uint32_t kSpinLimit = 1u << 22;
 static_assert(kThreads == kRadix, "one thread per digit");
 static_assert(kKpt * kThreads == kSortTile, "tile size");
 
@@ -77,7 +77,8 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
                                                       const uint32_t* __restrict__ vals_in, KeyT* __restrict__ keys_out,
                                                       uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift,
                                                       const uint32_t* __restrict__ hist, uint32_t* lookback,
-                                                      uint32_t* tile_counter, uint32_t* status) {
+                                                      uint32_t* tile_counter, uint32_t* status,
+                                                      uint32_t spin_limit) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SortSmem<KeyT>& S = *reinterpret_cast<SortSmem<KeyT>*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -191,7 +192,7 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
         else --k;
       }
       if (stalled) {
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           raise_status(status, kStatusSpinTimeout);
           break;
         }
@@ -255,7 +256,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_onesweep10(const uint32_t* __re
                                                           uint32_t* __restrict__ keys_out,
                                                           uint32_t* __restrict__ vals_out, uint32_t n, uint32_t shift,
                                                           const uint32_t* __restrict__ hist, uint32_t* lookback,
-                                                          uint32_t* tile_counter, uint32_t* status) {
+                                                          uint32_t* tile_counter, uint32_t* status,
+                                                          uint32_t spin_limit) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   SortSmem10& S = *reinterpret_cast<SortSmem10*>(smem_raw);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -392,7 +394,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_onesweep10(const uint32_t* __re
         --k;
       }
       if (stalled) {
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           raise_status(status, kStatusSpinTimeout);
           break;
         }
@@ -439,7 +441,7 @@ void onesweep10_w(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* ke
   }
   auto* kernel = vals_in == nullptr ? k_onesweep10<true, kWindow> : k_onesweep10<false, kWindow>;
   launch_pdl(kernel, dim3(sort_num_tiles(n)), dim3(kThreads), smem, s, keys_in, vals_in, keys_out, vals_out, n, shift,
-             hist, lookback, tile_counter, status);
+             hist, lookback, tile_counter, status, get_wait_limit());
 }
 
 template <typename KeyT>
@@ -474,12 +476,13 @@ void onesweep_w(cudaStream_t s, uint32_t n, uint32_t shift, const KeyT* keys_in,
   }
   const uint32_t grid = sort_num_tiles(n);
   auto* kernel = vals_in == nullptr ? k_onesweep<KeyT, true, kWindow> : k_onesweep<KeyT, false, kWindow>;
+  const uint32_t spin_limit = get_wait_limit();
   if (pdl)
     launch_pdl(kernel, dim3(grid), dim3(kThreads), smem, s, keys_in, vals_in, keys_out, vals_out, n, shift, hist,
-               lookback, tile_counter, status);
+               lookback, tile_counter, status, spin_limit);
   else
     kernel<<<grid, kThreads, smem, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, hist, lookback, tile_counter,
-                                        status);
+                                        status, spin_limit);
 }
 
 template <typename KeyT>
@@ -529,6 +532,22 @@ void launch_onesweep_u64(cudaStream_t s, uint32_t n, uint32_t shift, const uint6
                          const uint32_t* vals_in, uint64_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
                          uint32_t* lookback, uint32_t* tile_counter, uint32_t* status) {
   onesweep<uint64_t>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status, false);
+}
+
+// One 8-bit pass over a single tile of n <= kSortTile keys, launched as one
+// block with the tile counter preset by the caller.  With the counter at 1
+// the block draws tile 1 (beyond the keys: it loads and writes none) and its
+// look-back waits for tile 0, which no block publishes, until `spin_limit`
+// polls have passed.  Used only to check that a wait that never ends gives
+// up, raises kStatusSpinTimeout and returns.
+void launch_onesweep_wait_probe(cudaStream_t s, uint32_t n, const uint32_t* keys_in, uint32_t* keys_out,
+                                uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback, uint32_t* tile_counter,
+                                uint32_t* status, uint32_t spin_limit) {
+  const size_t smem = sizeof(SortSmem<uint32_t>);
+  cudaFuncSetAttribute(k_onesweep<uint32_t, true, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       static_cast<int>(smem));
+  k_onesweep<uint32_t, true, 4><<<1, kThreads, smem, s>>>(keys_in, nullptr, keys_out, vals_out, n, 0u, hist,
+                                                          lookback, tile_counter, status, spin_limit);
 }
 
 }  // namespace dm

@@ -61,33 +61,34 @@ def bwd_wrt_vtx2xyz(dldw_vtx2xyz: torch.Tensor, pix2tri: torch.Tensor, tri2vtx: 
 
 
 class AutogradFunction(torch.autograd.Function):
-    """Differentiable depth rendering as a torch.autograd.Function."""
+    """pix2depth as a differentiable op of the vertex positions: apply(vtx2xyz,
+    pix2tri, tri2vtx, transform_ndc2world) -> (img_h, img_w) depth.  The
+    forward and the vertex gradient are the two kernels above; pix2tri, the
+    triangles and the camera are constants of the op (no gradient)."""
 
     @staticmethod
     def forward(ctx, vtx2xyz, pix2tri, tri2vtx, transform_ndc2world):
-        ctx.save_for_backward(pix2tri, tri2vtx, vtx2xyz, transform_ndc2world)
-        pix2depth = torch.zeros(pix2tri.shape, dtype=torch.float32, device=vtx2xyz.device)
-        update(pix2depth, pix2tri, tri2vtx, vtx2xyz.detach(), transform_ndc2world)
-        return pix2depth
+        out = torch.zeros(tuple(pix2tri.shape), dtype=torch.float32, device=vtx2xyz.device)
+        update(out, pix2tri, tri2vtx, vtx2xyz.detach(), transform_ndc2world)
+        # the camera and the hit map are not differentiated, only replayed
+        ctx.save_for_backward(vtx2xyz, pix2tri, tri2vtx, transform_ndc2world)
+        return out
 
     @staticmethod
-    def backward(ctx, dldw_pix2depth):
-        pix2tri, tri2vtx, vtx2xyz, transform_ndc2world = ctx.saved_tensors
-        dldw_vtx2xyz = torch.zeros_like(vtx2xyz)
-        bwd_wrt_vtx2xyz(dldw_vtx2xyz, pix2tri, tri2vtx, vtx2xyz.detach(), dldw_pix2depth.contiguous(),
-                        transform_ndc2world)
-        return dldw_vtx2xyz, None, None, None
+    def backward(ctx, grad_depth):
+        vtx2xyz, pix2tri, tri2vtx, transform_ndc2world = ctx.saved_tensors
+        if not ctx.needs_input_grad[0]:
+            return None, None, None, None
+        grad_vtx = vtx2xyz.new_zeros(vtx2xyz.shape)
+        bwd_wrt_vtx2xyz(grad_vtx, pix2tri, tri2vtx, vtx2xyz.detach(), grad_depth.contiguous(), transform_ndc2world)
+        return grad_vtx, None, None, None
 
 
 def pix2depth_using_interpolation(vtx2xyz, pix2tri, tri2vtx, transform_ndc2world):
-    """Depth through the interpolated hit position (differentiable through
-    Pix2Tri.AutogradInterpolate)."""
-    from ..Pix2Tri.torch import AutogradInterpolate
-    pix2xyz = AutogradInterpolate.apply(pix2tri, tri2vtx, vtx2xyz, vtx2xyz, transform_ndc2world)
-    transform_world2ndc = transform_ndc2world.inverse()
-    pix2xyzw = torch.cat([pix2xyz, torch.ones_like(pix2xyz[:, :, :1])], dim=-1)
-    background = pix2tri == torch.iinfo(torch.uint32).max
-    pix2ndcw = pix2xyzw @ transform_world2ndc.T
-    pix2depth = (pix2ndcw[:, :, 2] / pix2ndcw[:, :, 3] + 1.0) * 0.5
-    pix2depth[background] = 0.0
-    return pix2depth
+    """The depth of each pixel's hit point, differentiable in vtx2xyz: the
+    function of the reference helper of this name, which interpolates the hit
+    position from the vertex positions and projects it to ndc.  The hit point
+    of a pixel's ray on its triangle is that interpolated position, so the
+    fused depth kernel computes the same function and its gradient directly
+    (one kernel each way, the world->ndc inverse on the device)."""
+    return AutogradFunction.apply(vtx2xyz, pix2tri, tri2vtx, transform_ndc2world)

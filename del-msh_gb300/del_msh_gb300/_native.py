@@ -33,12 +33,18 @@ _SIGNATURES = {
     "dm_pix2tri_interpolate": (i32, [u64, u32, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp]),
     "dm_pix2tri_interpolate_bwd": (i32, [u64, u32, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp, vp, vp]),
     "dm_tuning_set": (i32, [vp]),
+    "dm_wait_limit_get": (i32, [vp]),
+    "dm_wait_limit_set": (i32, [u32]),
+    "dm_selftest_bounded_wait": (i32, [u64, u32, vp, sz]),
+    "dm_selftest_bounded_wait_scratch_bytes": (sz, []),
     "dm_mortons_vtx2morton_from_vtx2co": (i32, [u64, u32, u32, vp, vp, vp]),
     "dm_array1d_argsort": (i32, [u64, u32, vp, vp, vp, sz]),
     "dm_array1d_argsort_scratch_bytes": (sz, [u32]),
     "dm_mortons_make_bvhnodes_from_sorted_mortons": (i32, [u64, u32, vp, vp, vp]),
     "dm_bvhnode2aabb_update_aabb": (i32, [u64, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp]),
     "dm_bvhnode2aabb_update_aabb_noalloc": (i32, [u64, u32, vp, vp, u32, vp, u32, vp, vp]),
+    "dm_bvhnode2aabb_update_aabb_ex": (i32, [u64, u32, vp, vp, u32, vp, u32, vp, vp, vp, sz]),
+    "dm_bvhnode2aabb_update_aabb_scratch_bytes": (sz, [u32]),
     "dm_trimesh3_make_bvhnodes_bvhnode2aabb": (i32, [u64, u32, vp, u32, vp, vp, vp, vp, sz]),
     "dm_trimesh3_build_scratch_bytes": (sz, [u32]),
     "dm_trimesh3_build_ex": (i32, [u64, u32, vp, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, sz]),
@@ -86,6 +92,17 @@ def set_tuning(cast_threads: int, cast_stack: int, tile_w: int, sort_window: int
     t = Tuning(cast_threads, cast_stack, tile_w, sort_window, cast_refill_min, cast_leaf_min, cast_ascend_min,
                cast_long_steps)
     call("dm_tuning_set", C.addressof(t))
+
+
+def get_wait_limit() -> int:
+    v = C.c_uint32(0)
+    call("dm_wait_limit_get", C.byref(v))
+    return int(v.value)
+
+
+def set_wait_limit(polls: int) -> None:
+    """Polls a bounded device wait makes before giving up (0 = the default)."""
+    call("dm_wait_limit_set", polls)
 
 
 class DelMshError(RuntimeError):

@@ -92,6 +92,22 @@ int dm_tuning_get(dm_tuning* out);
  * a combination that is not compiled. */
 int dm_tuning_set(const dm_tuning* in);
 
+/* Polls a bounded device wait (the radix sort's look-back) makes before it
+ * gives up, raises status bit 1 and returns instead of hanging.  Process-wide,
+ * read at each launch; 0 restores the default (2^22).  No reference
+ * counterpart: the reference's sort (thrust) has no bounded waits. */
+int dm_wait_limit_get(uint32_t* polls);
+int dm_wait_limit_set(uint32_t polls);
+
+/* Self-test of the bounded wait: one real 8-bit onesweep pass, launched as a
+ * single block whose tile counter is preset so that the block draws tile 1
+ * and looks back for tile 0, which nothing publishes.  The wait gives up
+ * after `polls` polls (1..2^24), status bit 1 is raised and the call returns
+ * (it synchronizes `stream_ptr`).  scratch: device memory of
+ * dm_selftest_bounded_wait_scratch_bytes() bytes.  No reference counterpart. */
+int dm_selftest_bounded_wait(uint64_t stream_ptr, uint32_t polls, void* scratch, size_t scratch_bytes);
+size_t dm_selftest_bounded_wait_scratch_bytes(void);
+
 /* Morton codes of points after a homogeneous transform (num_dim 2: 3x3, 3: 4x4
  * column-major), clamped to the unit cube as del-msh-cpu does.
  * Replaces: del-msh-dlpack/src/mortons.rs:18-77 mortons_vtx2morton_from_vtx2co
@@ -123,8 +139,16 @@ int dm_mortons_make_bvhnodes_from_sorted_mortons(uint64_t stream_ptr, uint32_t n
  * vertices, branch = union of its children), optionally also enclosing
  * vtx2xyz1 (continuous collision detection; may be NULL).  This is also the
  * refit of a deformed mesh: same bvhnodes, new vertices.  Only i_bvhnode == 0
- * (the whole tree) is supported.  flags_scratch: u32[num_elem-1] that is zero
- * before the first call and that every call leaves zero, or NULL.
+ * (the whole tree) is supported.
+ * With flags_scratch == NULL (the reference binding's form) the call takes
+ * stream-ordered scratch, derives every branch's leaf range from bvhnodes on
+ * the device and, for a tree in Karras leaf order (every tree this library
+ * or the reference builds), answers each branch by range queries over the
+ * leaf boxes; any other tree, or one whose chains of right (left) children
+ * are longer than 64 records, is refit by the parent-pointer climb instead,
+ * chosen on the device.  Both give the reference's boxes bit for bit.
+ * flags_scratch: u32[num_elem-1] that is zero before the first call and that
+ * every call leaves zero; the call then uses only it and always climbs.
  * Replaces: del-msh-dlpack/src/bvhnode2aabb.rs:15-108 bvhnode2aabb_update_aabb
  * (kernel del-msh-cuda-kernels/cuda/bvhnode2aabb.cu:7-65 from_trimesh3;
  * CPU del-msh-cpu/src/bvhnode2aabb3.rs:68-142). */
@@ -132,6 +156,20 @@ int dm_bvhnode2aabb_update_aabb(uint64_t stream_ptr, uint32_t num_bvhnode, float
                                 uint32_t i_bvhnode, const uint32_t* bvhnodes, uint32_t num_elem,
                                 const uint32_t* elem2vtx, uint32_t num_vtx, const float* vtx2xyz0,
                                 const float* vtx2xyz1, uint32_t* flags_scratch);
+
+/* dm_bvhnode2aabb_update_aabb (flags_scratch == NULL form) with caller
+ * scratch of dm_bvhnode2aabb_update_aabb_scratch_bytes(num_elem) bytes,
+ * zero before the first call; every call leaves it ready for the next one
+ * (the words that must be zero are left zero), so a resident tree is refit
+ * frame after frame with no memset and no allocation.
+ * Replaces: del-msh-dlpack/src/bvhnode2aabb.rs:15-108 bvhnode2aabb_update_aabb
+ * with the binding's internal flag allocation (bvhnode2aabb.rs:78-79) moved to
+ * the caller. */
+int dm_bvhnode2aabb_update_aabb_ex(uint64_t stream_ptr, uint32_t num_bvhnode, float* bvhnode2aabb,
+                                   const uint32_t* bvhnodes, uint32_t num_elem, const uint32_t* elem2vtx,
+                                   uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, void* scratch,
+                                   size_t scratch_bytes);
+size_t dm_bvhnode2aabb_update_aabb_scratch_bytes(uint32_t num_elem);
 
 /* dm_bvhnode2aabb_update_aabb for callers that cannot allocate device memory
  * (a per-frame refit loop under a no-allocation rule, a plugin whose host owns
@@ -141,8 +179,12 @@ int dm_bvhnode2aabb_update_aabb(uint64_t stream_ptr, uint32_t num_bvhnode, float
  * of 1..4194305 triangles (16 MiB of flags, held by every GPU that loads the
  * library until exit); larger ones return DM_ERR_INVALID_ARGUMENT.  The first
  * call on a device looks up the array's address (do it before any stream
- * capture).  Calls share the array: each clears the part it uses, and calls
- * that overlap on the GPU race.  No counterpart in the reference. */
+ * capture); the address is kept for the life of the process, so the library
+ * must not be used across a cudaDeviceReset of that device (which unloads
+ * the module and leaves the kept address stale; the device status word's
+ * address is kept the same way).  Calls share the array: each clears the
+ * part it uses, and calls that overlap on the GPU race.  No counterpart in
+ * the reference. */
 int dm_bvhnode2aabb_update_aabb_noalloc(uint64_t stream_ptr, uint32_t num_bvhnode, float* bvhnode2aabb,
                                         const uint32_t* bvhnodes, uint32_t num_elem, const uint32_t* elem2vtx,
                                         uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1);

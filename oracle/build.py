@@ -3,11 +3,12 @@
 * ``build_oracle()`` compiles ``oracle.c`` (the CPU restatement of
   del-msh-cpu's LBVH build and ray cast) into ``oracle/_build/liboracle.so``
   with ``-ffp-contract=off`` so f32 arithmetic rounds as Rust's does.
-* ``build_ref()`` compiles the reference's own CUDA sources for the path
+* ``build_ref(root)`` compiles the reference's own CUDA sources for the path
   (``del-msh-cuda-kernels/cuda/bvhnodes_morton.cu`` + ``mortons.h``) as host
   C++ through ``ref_shim.cpp`` into ``oracle/_ref/libref_topology.so``.  It
-  needs the reference checkout (``DELMSH_REFERENCE`` or /root/reference); when
-  that is absent (as on a machine that only runs the tests) it does nothing.
+  needs the reference checkout, given as ``root`` or by the
+  ``DELMSH_REFERENCE`` environment variable; without one (as on a machine that
+  only runs the tests) it does nothing.
 """
 from __future__ import annotations
 
@@ -20,7 +21,6 @@ BUILD_DIR = HERE / "_build"
 REF_DIR = HERE / "_ref"
 LIB_ORACLE = BUILD_DIR / "liboracle.so"
 LIB_REF = REF_DIR / "libref_topology.so"
-REFERENCE_ROOT = pathlib.Path(os.environ.get("DELMSH_REFERENCE", "/root/reference"))
 COMMON_FLAGS = ["-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared"]
 
 
@@ -39,8 +39,16 @@ def build_oracle(force: bool = False) -> pathlib.Path:
     return LIB_ORACLE
 
 
-def build_ref(force: bool = False) -> pathlib.Path | None:
-    kdir = REFERENCE_ROOT / "del-msh-cuda-kernels" / "cuda"
+def reference_root(root=None) -> pathlib.Path | None:
+    root = root or os.environ.get("DELMSH_REFERENCE")
+    return pathlib.Path(root) if root else None
+
+
+def build_ref(root=None, force: bool = False) -> pathlib.Path | None:
+    ref = reference_root(root)
+    if ref is None:
+        return None
+    kdir = ref / "del-msh-cuda-kernels" / "cuda"
     if not (kdir / "bvhnodes_morton.cu").exists():
         return None
     REF_DIR.mkdir(exist_ok=True)
@@ -54,5 +62,6 @@ def build_ref(force: bool = False) -> pathlib.Path | None:
 
 
 if __name__ == "__main__":
+    import sys
     print(build_oracle(force=True))
-    print(build_ref(force=True))
+    print(build_ref(sys.argv[1] if len(sys.argv) > 1 else None, force=True))

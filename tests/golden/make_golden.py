@@ -8,7 +8,7 @@
   icosphere (build + 256x256 orthographic cast), stored with its inputs so the
   same bits can be checked on any machine.
 
-Usage: python tests/golden/make_golden.py
+Usage: python tests/golden/make_golden.py <reference checkout>
 """
 from __future__ import annotations
 
@@ -55,8 +55,10 @@ def topology_cases():
 
 def main():
     obuild.build_oracle()
-    if obuild.build_ref() is None:
-        raise SystemExit("the reference checkout is required to regenerate the reference-code fixtures")
+    # the reference checkout: first argument, else DELMSH_REFERENCE
+    if obuild.build_ref(sys.argv[1] if len(sys.argv) > 1 else None) is None:
+        raise SystemExit("usage: make_golden.py <reference checkout> (or set DELMSH_REFERENCE): the reference's "
+                         "sources are required to regenerate the reference-code fixtures")
     R = O.ref_lib()
     rng = np.random.default_rng(99)
 

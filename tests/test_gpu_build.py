@@ -213,6 +213,69 @@ def test_refit_deformed_and_ccd(cuda, oracle):
     assert _status_clear() == 0
 
 
+def _relabel_branches(bvh, seed):
+    """The same tree with its branches renumbered at random (root kept at 0):
+    still a valid tree, no longer in Karras leaf order."""
+    bvh = np.asarray(bvh, np.uint32).reshape(-1, 3)
+    nb = (bvh.shape[0] + 1) // 2 - 1
+    perm = np.arange(bvh.shape[0], dtype=np.int64)
+    perm[1:nb] = 1 + np.random.default_rng(seed).permutation(nb - 1)
+    umax = np.uint32(0xFFFFFFFF)
+    mapped = np.where(bvh == umax, umax, perm[np.minimum(bvh, bvh.shape[0] - 1)].astype(np.uint32))
+    mapped[nb:, 1] = bvh[nb:, 1]  # a leaf's second word is its triangle
+    mapped[nb:, 2] = bvh[nb:, 2]
+    out = np.empty_like(bvh)
+    out[perm] = mapped
+    return out
+
+
+@pytest.mark.parametrize("case", ["torus", "torus_ccd", "soup", "relabelled", "nan", "ex_frames", "ex_soup"])
+def test_dropin_refit_paths(cuda, oracle, case):
+    """dm_bvhnode2aabb_update_aabb in the reference binding's form (no flag
+    scratch): range queries for trees in Karras leaf order (the torus), the
+    parent-pointer climb for trees the device cannot show to be (the soup's
+    long chains, a tree with its branches renumbered), the tree-order climb
+    for NaN leaf boxes; and the _ex form with persistent scratch, frame after
+    frame.  Every box equals the oracle's bit for bit."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    if case in ("soup", "ex_soup"):
+        tri, vtx = W.clustered_soup(150_000, num_cluster=4, seed=3)
+    else:
+        tri, vtx = W.displaced_torus(96, seed=4)
+    ref = oracle.build(tri, vtx)
+    bvh_np = _relabel_branches(ref["bvhnodes"], 5) if case == "relabelled" else ref["bvhnodes"]
+    d_tri, bvh = to_dev(tri, torch), to_dev(bvh_np, torch)
+    T = tri.shape[0]
+    aabb = torch.full((2 * T - 1, 6), 7.0, dtype=torch.float32, device="cuda:0")
+    phase = np.random.default_rng(6).uniform(0, 6.28, vtx.shape[0])
+    L = _native.load()
+    ex_scratch = torch.zeros((L.dm_bvhnode2aabb_update_aabb_scratch_bytes(T),), dtype=torch.uint8,
+                             device="cuda:0")
+    sp = torch.cuda.current_stream().cuda_stream
+    for frame in range(3):
+        v = (vtx + 0.01 * np.sin(phase + frame)[:, None]).astype(np.float32)
+        if case == "nan":
+            v[frame * 7 + 1, 1] = np.nan
+        v1 = (v * 1.01).astype(np.float32) if case == "torus_ccd" else None
+        d_v, d_v1 = to_dev(v, torch), (None if v1 is None else to_dev(v1, torch))
+        if case.startswith("ex_"):
+            _native.call("dm_bvhnode2aabb_update_aabb_ex", sp, 2 * T - 1, aabb.data_ptr(), bvh.data_ptr(), T,
+                         d_tri.data_ptr(), v.shape[0], d_v.data_ptr(), None, ex_scratch.data_ptr(),
+                         ex_scratch.numel())
+            # the refit header's climb flag (after the derived ends and the
+            # arrival words): 0 = range queries, bit 2 = parent-pointer climb
+            hdr1 = ((4 * T + 255) // 256 * 256) + 4 * (((T + 3) & ~3) + 1)
+            flag = int(ex_scratch[hdr1:hdr1 + 4].cpu().numpy().view(np.uint32)[0])
+            assert flag == (0 if case == "ex_frames" else 2), (case, flag)
+        else:
+            TriMesh3.update_bvhnode2aabb(d_tri, d_v, bvh, aabb, vtx2xyz1=d_v1)
+        want = oracle.bvhnode2aabb(bvh_np, tri, v, v1)
+        assert np.array_equal(bits(to_np(aabb, torch)), bits(want)), (case, frame)
+    assert _status_clear() == 0
+
+
 def test_cpu_tensors_are_rejected():
     import torch
     from del_msh_gb300.TriMesh3 import torch as TriMesh3

@@ -54,6 +54,12 @@ def test_pix2depth_fwd_bwd(cuda, oracle, ndiv, img):
     v = d_vtx.clone().requires_grad_(True)
     (Pix2Depth.AutogradFunction.apply(v, p2t, d_tri, m_row) * to_dev(g, torch)).sum().backward()
     assert _close_sum(to_np(v.grad, torch), rgrad)
+    # the interpolation-named helper is the same differentiable function
+    v2 = d_vtx.clone().requires_grad_(True)
+    d2 = Pix2Depth.pix2depth_using_interpolation(v2, p2t, d_tri, m_row)
+    assert np.array_equal(bits(to_np(d2.detach(), torch)), bits(ref))
+    (d2 * to_dev(g, torch)).sum().backward()
+    assert _close_sum(to_np(v2.grad, torch), rgrad)
     assert _native.device_status(clear=True) == 0
 
 
