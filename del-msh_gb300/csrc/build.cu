@@ -19,36 +19,16 @@ inline int grid_for(uint32_t n, int per_block, int max_blocks) {
   return static_cast<int>(b < 1 ? 1 : (b > static_cast<uint32_t>(max_blocks) ? max_blocks : b));
 }
 
-// Vertex index checked against num_vtx (out of range -> vertex 0 + status).
-__device__ __forceinline__ uint32_t vtx_index(const uint32_t* __restrict__ p, uint32_t num_vtx, uint32_t* status) {
-  const uint32_t v = __ldg(p);
-  if (v < num_vtx) return v;
-  raise_status(status, kStatusBadIndex);
-  return 0u;
-}
-
-__device__ __forceinline__ float3 tri_centroid(const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
-                                               const float* __restrict__ vtx2xyz, uint32_t it, uint32_t* status) {
-  const uint32_t* t = tri2vtx + static_cast<size_t>(it) * 3;
-  const float3 p0 = load_vtx(vtx2xyz, vtx_index(t, num_vtx, status));
-  const float3 p1 = load_vtx(vtx2xyz, vtx_index(t + 1, num_vtx, status));
-  const float3 p2 = load_vtx(vtx2xyz, vtx_index(t + 2, num_vtx, status));
-  return make_float3(centroid1(p0.x, p1.x, p2.x), centroid1(p0.y, p1.y, p2.y), centroid1(p0.z, p1.z, p2.z));
-}
-
-// tri_centroid, and the triangle's box exactly as leaf_box computes it (the
-// same vertex loads, eps 0) into *box.
-__device__ __forceinline__ float3 tri_centroid_box(const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
-                                                   const float* __restrict__ vtx2xyz, uint32_t it, uint32_t* status,
-                                                   Box* box) {
-  const uint32_t* t = tri2vtx + static_cast<size_t>(it) * 3;
-  const float3 p0 = load_vtx(vtx2xyz, vtx_index(t, num_vtx, status));
-  const float3 p1 = load_vtx(vtx2xyz, vtx_index(t + 1, num_vtx, status));
-  const float3 p2 = load_vtx(vtx2xyz, vtx_index(t + 2, num_vtx, status));
-  box_set(*box, p0, 0.0f);
-  box_add(*box, p1, 0.0f);
-  box_add(*box, p2, 0.0f);
-  return make_float3(centroid1(p0.x, p1.x, p2.x), centroid1(p0.y, p1.y, p2.y), centroid1(p0.z, p1.z, p2.z));
+// Words of the refit header read once per block (thread 0, volatile) and
+// shared: every thread reading the same L2 line would queue thousands of
+// requests on one L2 slice.  Has __syncthreads.
+__device__ __forceinline__ uint2 block_read_hdr(const uint32_t* w0, const uint32_t* w1) {
+  __shared__ uint2 s_words;
+  if (threadIdx.x == 0)
+    s_words = make_uint2(*reinterpret_cast<const volatile uint32_t*>(w0),
+                         w1 ? *reinterpret_cast<const volatile uint32_t*>(w1) : 0u);
+  __syncthreads();
+  return s_words;
 }
 
 // A box stored by box_store, read through the read-only path.
@@ -490,7 +470,7 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_win(uint32_t total_tri, S
   // runs only when the range-query refit handed over (NaN) or heights are
   // wanted, and not for a tree that is not in Karras leaf order (the plain
   // climb of k_refit does that call)
-  const uint32_t climb_flag = *reinterpret_cast<volatile uint32_t*>(queue + 1);
+  const uint32_t climb_flag = block_read_hdr(queue + 1, nullptr).x;
   if (climb_flag == 0u || (climb_flag & kRefitPlainClimb) != 0u) return;
   extern __shared__ __align__(16) unsigned char win_raw[];
   WinSmem& S = *reinterpret_cast<WinSmem*>(win_raw);
@@ -659,7 +639,7 @@ __global__ void __launch_bounds__(128) k_refit_top(uint32_t total_tri, Segments 
   pdl_wait();
   pdl_launch_dependents();
   const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t count = __ldcg(queue);
+  const uint32_t count = block_read_hdr(queue, nullptr).x;
   if (e >= count || e >= capacity) return;
   const uint4 q = __ldcg(reinterpret_cast<const uint4*>(queue + kRefitQueueHdr) + e);
   const LeafMesh lm = leaf_mesh<kBatch>(seg, total_tri, 0u, q.w < total_tri ? q.w : 0u);
@@ -937,7 +917,7 @@ __global__ void __launch_bounds__(256) k_refit_seg_super(uint32_t total_tri, uin
   __shared__ bool s_last;
   pdl_wait();
   pdl_launch_dependents();
-  if (*reinterpret_cast<volatile uint32_t*>(hdr + 1) != 0u) return;
+  if (block_read_hdr(hdr + 1, nullptr).x != 0u) return;
   const uint32_t sb = blockIdx.x;
   const uint64_t sb_start = static_cast<uint64_t>(sb) << kRefitSuperLog;
   if (threadIdx.x < kRefitSuper) {
@@ -1189,8 +1169,9 @@ __global__ void __launch_bounds__(256, 4) k_refit_seg_cross_groups(uint32_t tota
                                                                    uint32_t* status) {
   pdl_wait();
   pdl_launch_dependents();
-  const bool climb = *reinterpret_cast<const volatile uint32_t*>(hdr + 1) != 0u;
-  uint32_t count = *reinterpret_cast<const volatile uint32_t*>(hdr + 3);
+  const uint2 h = block_read_hdr(hdr + 1, hdr + 3);
+  const bool climb = h.x != 0u;
+  uint32_t count = h.y;
   if (count > total_tri) count = total_tri;
   if (count > groups) return;  // the one-thread kernel takes it
   const uint32_t sub = threadIdx.x & 7u;
@@ -1217,8 +1198,9 @@ __global__ void __launch_bounds__(256) k_refit_seg_cross_threads(uint32_t total_
                                                                  uint32_t* status) {
   pdl_wait();
   pdl_launch_dependents();
-  const bool climb = *reinterpret_cast<const volatile uint32_t*>(hdr + 1) != 0u;
-  uint32_t count = *reinterpret_cast<const volatile uint32_t*>(hdr + 3);
+  const uint2 h = block_read_hdr(hdr + 1, hdr + 3);
+  const bool climb = h.x != 0u;
+  uint32_t count = h.y;
   if (count > total_tri) count = total_tri;
   if (count <= groups) return;  // the 8-lane kernel took it
   for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {

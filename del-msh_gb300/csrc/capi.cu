@@ -120,8 +120,8 @@ SortLayout sort_layout(uint32_t n, int num_pass, size_t key_bytes, int radix = d
 
 // -------------------------------------------------------- build layout
 struct BuildLayout {
-  size_t transform, aabb, ticket, height, sort_hdr, partials, codes, akeys, avals, bvals, flags, tribox, total,
-      zero_bytes, sort_bytes;
+  size_t transform, aabb, ticket, height, front_bar, sort_hdr, partials, codes, akeys, avals, bvals, flags, tribox,
+      front_counts, front_totals, total, zero_bytes, sort_bytes;
   bool radix10;  // three 10-bit passes (dm::kRadix10MaxKeys), else four 8-bit ones
   SortLayout sort;
 };
@@ -132,6 +132,7 @@ BuildLayout build_layout(uint32_t T) {
   L.aabb = 64;
   L.ticket = 96;
   L.height = 100;
+  L.front_bar = 104;
   L.sort_hdr = 256;
   L.radix10 = T <= dm::kRadix10MaxKeys;
   L.sort = L.radix10 ? sort_layout(T, 3, 4, dm::kRadix10) : sort_layout(T, 4, 4);
@@ -144,7 +145,9 @@ BuildLayout build_layout(uint32_t T) {
   L.bvals = L.avals + align256(static_cast<size_t>(T) * 4);
   L.flags = L.bvals + align256(static_cast<size_t>(T) * 4);
   L.tribox = L.flags + align256(dm::refit_flags_words(T) * 4);
-  L.total = L.tribox + align256(static_cast<size_t>(T) * 24);
+  L.front_counts = L.tribox + align256(static_cast<size_t>(T) * 24);
+  L.front_totals = L.front_counts + align256(size_t{4} * dm::kRadix * dm::kAabbBlocks);
+  L.total = L.front_totals + align256(size_t{4} * dm::kRadix);
   return L;
 }
 
@@ -221,22 +224,47 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   // cache-friendly and the extra store costs more than it saves (2M torus:
   // +8 us in the centroid pass, -3 us in the refit).
   float* tribox = num_vtx >= 2ull * T ? at<float>(base, L.tribox) : nullptr;
-  dm::launch_centroid_aabb(s, T, tri2vtx, num_vtx, vtx2xyz, at<float>(base, L.partials),
-                           at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status, cent, cstride,
-                           tribox);
-  dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status, cent, cstride, L.radix10);
-  if (tri2morton_out) DM_CUDA(cudaMemcpyAsync(tri2morton_out, codes, size_t{4} * T, cudaMemcpyDeviceToDevice, s));
-  // 3 passes: codes -> (ak, av) -> (codes, bv) -> (ok, ov), by default the A
-  //   buffers (dead after pass 2); other_end then takes bv.
-  // 4 passes: codes -> (ak, av) -> (codes, bv) -> (ak, av) -> (ok, ov), by
-  //   default (codes, bv) (dead after pass 2); other_end then takes ak.
-  uint32_t* ok = idx2morton_out ? idx2morton_out : (L.radix10 ? ak : codes);
-  uint32_t* ov = idx2tri_out ? idx2tri_out : (L.radix10 ? av : bv);
-  if (ev) DM_CUDA(cudaEventRecord(ev[1], s));
-  if (L.radix10) sort3(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
-  else sort4(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
+  // Meshes whose tiles fit on the GPU at once: centroids, fit, codes and the
+  // four passes in one cooperative launch, computed -> (ak, av) -> (codes,
+  // bv) -> (ak, av) -> (ok, ov), by default (codes, bv); other_end then takes
+  // ak.  The profile's Morton stage is then empty and its sort stage covers
+  // the whole front.
+  bool front = false;
+  if (T >= 2 && T <= dm::front_max_tri()) {
+    uint32_t* ok = idx2morton_out ? idx2morton_out : codes;
+    uint32_t* ov = idx2tri_out ? idx2tri_out : bv;
+    if (ev) DM_CUDA(cudaEventRecord(ev[1], s));
+    front = dm::launch_build_front(s, T, tri2vtx, num_vtx, vtx2xyz, tribox, at<float>(base, L.partials),
+                                   dm::kAabbBlocks, transform, at<float>(base, L.aabb), tri2morton_out, ak, av, codes,
+                                   bv, ok, ov, at<uint32_t>(base, L.front_counts),
+                                   at<uint32_t>(base, L.front_totals), at<uint32_t>(base, L.front_bar), status);
+  }
+  uint32_t* ok;
+  uint32_t* ov;
+  uint32_t* other_end;
+  if (front) {
+    ok = idx2morton_out ? idx2morton_out : codes;
+    ov = idx2tri_out ? idx2tri_out : bv;
+    other_end = other_end_out ? other_end_out : ak;
+  } else {
+    dm::launch_centroid_aabb(s, T, tri2vtx, num_vtx, vtx2xyz, at<float>(base, L.partials),
+                             at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status, cent, cstride,
+                             tribox);
+    dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status, cent, cstride,
+                          L.radix10);
+    if (tri2morton_out) DM_CUDA(cudaMemcpyAsync(tri2morton_out, codes, size_t{4} * T, cudaMemcpyDeviceToDevice, s));
+    // 3 passes: codes -> (ak, av) -> (codes, bv) -> (ok, ov), by default the A
+    //   buffers (dead after pass 2); other_end then takes bv.
+    // 4 passes: codes -> (ak, av) -> (codes, bv) -> (ak, av) -> (ok, ov), by
+    //   default (codes, bv) (dead after pass 2); other_end then takes ak.
+    ok = idx2morton_out ? idx2morton_out : (L.radix10 ? ak : codes);
+    ov = idx2tri_out ? idx2tri_out : (L.radix10 ? av : bv);
+    if (ev) DM_CUDA(cudaEventRecord(ev[1], s));
+    if (L.radix10) sort3(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
+    else sort4(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
+    other_end = other_end_out ? other_end_out : (L.radix10 ? bv : ak);
+  }
   if (ev) DM_CUDA(cudaEventRecord(ev[2], s));
-  uint32_t* other_end = other_end_out ? other_end_out : (L.radix10 ? bv : ak);
   dm::launch_topology(s, T, ok, ov, bvhnodes, other_end);
   if (ev) DM_CUDA(cudaEventRecord(ev[3], s));
   // the height is only computed on request: it needs the tree-order climb

@@ -102,6 +102,19 @@ __device__ __forceinline__ float3 transform_homogeneous(const float* m, float x,
   return make_float3(__fdiv_rn(ox, w), __fdiv_rn(oy, w), __fdiv_rn(oz, w));
 }
 
+// transform_homogeneous with the three divisions skipped when w is exactly
+// 1, as it is for an affine matrix (bottom row 0 0 0 1) and finite input:
+// x / 1 is x, so the result is the same bits.  Otherwise (a projective
+// matrix, or 0 * inf = NaN in w) it divides as transform_homogeneous does.
+__device__ __forceinline__ float3 transform_homogeneous_w1(const float* m, float x, float y, float z) {
+  const float w = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[3], x), __fmul_rn(m[7], y)), __fmul_rn(m[11], z)), m[15]);
+  const float ox = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[0], x), __fmul_rn(m[4], y)), __fmul_rn(m[8], z)), m[12]);
+  const float oy = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[1], x), __fmul_rn(m[5], y)), __fmul_rn(m[9], z)), m[13]);
+  const float oz = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(m[2], x), __fmul_rn(m[6], y)), __fmul_rn(m[10], z)), m[14]);
+  if (w == 1.0f) return make_float3(ox, oy, oz);
+  return make_float3(__fdiv_rn(ox, w), __fdiv_rn(oy, w), __fdiv_rn(oz, w));
+}
+
 __device__ __forceinline__ float2 transform_homogeneous2(const float* m, float x, float y) {
   const float w = __fadd_rn(__fadd_rn(__fmul_rn(m[2], x), __fmul_rn(m[5], y)), m[8]);
   const float ox = __fadd_rn(__fadd_rn(__fmul_rn(m[0], x), __fmul_rn(m[3], y)), m[6]);
@@ -299,5 +312,38 @@ __device__ __forceinline__ float3 load_vtx(const float* __restrict__ vtx2xyz, ui
   const float* p = vtx2xyz + static_cast<size_t>(i) * 3;
   return make_float3(__ldg(p), __ldg(p + 1), __ldg(p + 2));
 }
+
+// Vertex index checked against num_vtx (out of range -> vertex 0 + status).
+__device__ __forceinline__ uint32_t vtx_index(const uint32_t* __restrict__ p, uint32_t num_vtx, uint32_t* status) {
+  const uint32_t v = __ldg(p);
+  if (v < num_vtx) return v;
+  raise_status(status, kStatusBadIndex);
+  return 0u;
+}
+
+__device__ __forceinline__ float3 tri_centroid(const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
+                                               const float* __restrict__ vtx2xyz, uint32_t it, uint32_t* status) {
+  const uint32_t* t = tri2vtx + static_cast<size_t>(it) * 3;
+  const float3 p0 = load_vtx(vtx2xyz, vtx_index(t, num_vtx, status));
+  const float3 p1 = load_vtx(vtx2xyz, vtx_index(t + 1, num_vtx, status));
+  const float3 p2 = load_vtx(vtx2xyz, vtx_index(t + 2, num_vtx, status));
+  return make_float3(centroid1(p0.x, p1.x, p2.x), centroid1(p0.y, p1.y, p2.y), centroid1(p0.z, p1.z, p2.z));
+}
+
+// tri_centroid, and the triangle's box exactly as leaf_box computes it (the
+// same vertex loads, eps 0) into *box.
+__device__ __forceinline__ float3 tri_centroid_box(const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
+                                                   const float* __restrict__ vtx2xyz, uint32_t it, uint32_t* status,
+                                                   Box* box) {
+  const uint32_t* t = tri2vtx + static_cast<size_t>(it) * 3;
+  const float3 p0 = load_vtx(vtx2xyz, vtx_index(t, num_vtx, status));
+  const float3 p1 = load_vtx(vtx2xyz, vtx_index(t + 1, num_vtx, status));
+  const float3 p2 = load_vtx(vtx2xyz, vtx_index(t + 2, num_vtx, status));
+  box_set(*box, p0, 0.0f);
+  box_add(*box, p1, 0.0f);
+  box_add(*box, p2, 0.0f);
+  return make_float3(centroid1(p0.x, p1.x, p2.x), centroid1(p0.y, p1.y, p2.y), centroid1(p0.z, p1.z, p2.z));
+}
+
 
 }  // namespace dm

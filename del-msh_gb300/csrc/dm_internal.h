@@ -129,6 +129,22 @@ void launch_refit_any_tree(cudaStream_t s, uint32_t num_tri, const uint32_t* bvh
                            uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, float* aabb,
                            uint32_t* other_end, uint32_t* flags, uint32_t* status);
 
+// ---------------------------------------------------------------- front.cu
+// Centroids, AABB + fit transform, Morton codes and the four-pass stable
+// sort in one cooperative launch (see front.cu).  Returns false, having
+// launched nothing, when the mesh's tiles cannot all be resident at once
+// (or num_tri < 2); the caller then runs the separate kernels.  ka/va/kb/vb:
+// num_tri words each; out_keys/out_vals must not be ka/va; counts:
+// 256 * max_partials words; totals: 256 words; bar: one word, zero;
+// partials: max_partials * 6 floats.
+bool launch_build_front(cudaStream_t s, uint32_t num_tri, const uint32_t* tri2vtx, uint32_t num_vtx,
+                        const float* vtx2xyz, float* tribox, float* partials, uint32_t max_partials,
+                        float* transform_out, float* aabb_out, uint32_t* tri2morton, uint32_t* ka, uint32_t* va,
+                        uint32_t* kb, uint32_t* vb, uint32_t* out_keys, uint32_t* out_vals, uint32_t* counts,
+                        uint32_t* totals, uint32_t* bar, uint32_t* status);
+// Largest mesh the cooperative front takes on the current device (0: none).
+uint32_t front_max_tri();
+
 // ----------------------------------------------------------------- sort.cu
 constexpr int kSortTile = 3840;  // keys per onesweep tile
 constexpr int kRadix = 256;

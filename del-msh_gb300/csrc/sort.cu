@@ -217,6 +217,228 @@ __global__ void __launch_bounds__(kThreads, sizeof(KeyT) == 4 ? 4 : 2) k_oneswee
   }
 }
 
+// ------------------------------------------------------ match-ranked pass
+// The 8-bit pass for u32 keys above kRadix10MaxKeys.  A tile is 4096 keys:
+// 512 threads x 8 keys, warp-striped (key j of a lane at warp base + 32 j +
+// lane, so (j, lane) order is input order).  A warp ranks a key by OR-ing its
+// lane bit into the key's digit slot of a per-warp mask array in shared
+// memory: after a __syncwarp the slot holds exactly the lanes with that digit
+// (the peers), the lowest of them advances the warp's running count of the
+// digit and clears the slot.  That is about 15 instructions per key against
+// the ~40 of eight ballots, and with 8 keys per thread the pass keeps keys,
+// ranks and values in registers without spilling.  Counts, look-back and
+// write-out are those of k_onesweep.
+constexpr int kThreadsM = 512;
+constexpr int kWarpsM = kThreadsM / 32;
+constexpr int kKptM = 8;
+constexpr int kTileM = kThreadsM * kKptM;  // 4096
+static_assert(kTileM >= kSortTile, "a match-pass tile covers at least a k_onesweep tile (look-back sizing)");
+
+struct SortSmemM {
+  uint32_t whist[kWarpsM][kRadix];  // per-warp running counts, then per-warp exclusive offsets
+  uint32_t match[kWarpsM][kRadix];  // peer masks of the rank step; zero between steps
+  uint32_t gbase[kRadix];           // global start of each digit (upfront histogram scan)
+  uint32_t tstart[kRadix];          // start of each digit inside the tile
+  uint32_t offs[kRadix];            // output position minus tile slot, per digit
+  uint32_t scan[kWarpsM];
+  uint32_t tile;
+  uint32_t keys[kTileM];
+  uint32_t vals[kTileM];
+};
+
+// Exclusive scan over the block of one value per thread (threads >= 256
+// contribute zeros in the per-digit steps); has __syncthreads.
+__device__ __forceinline__ uint32_t block_exclusive_scan_m(uint32_t v, uint32_t* s_warp /* kWarpsM */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, x, off);
+    if (lane >= off) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < kWarpsM ? s_warp[lane] : 0u;
+#pragma unroll
+    for (int off = 1; off < kWarpsM; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, w, off);
+      if (lane >= off) w += y;
+    }
+    if (lane < kWarpsM) s_warp[lane] = w;
+  }
+  __syncthreads();
+  const uint32_t r = (warp > 0 ? s_warp[warp - 1] : 0u) + x - v;
+  __syncthreads();
+  return r;
+}
+
+template <bool kIota, int kWindow>
+__global__ void __launch_bounds__(kThreadsM, 2) k_onesweep_match(const uint32_t* __restrict__ keys_in,
+                                                               const uint32_t* __restrict__ vals_in,
+                                                               uint32_t* __restrict__ keys_out,
+                                                               uint32_t* __restrict__ vals_out, uint32_t n,
+                                                               uint32_t shift, const uint32_t* __restrict__ hist,
+                                                               uint32_t* lookback, uint32_t* tile_counter,
+                                                               uint32_t* status, uint32_t spin_limit) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SortSmemM& S = *reinterpret_cast<SortSmemM*>(smem_raw);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  {
+    uint4* z = reinterpret_cast<uint4*>(&S.whist[0][0]);  // whist and match: 2 * kWarpsM * kRadix words
+    for (int i = tid; i < 2 * kWarpsM * kRadix / 4; i += kThreadsM) z[i] = make_uint4(0u, 0u, 0u, 0u);
+  }
+  // This pass's tile counter is zeroed before the sort starts and touched by
+  // no other pass, so the ticket may be taken before the previous pass ends.
+  if (tid == 0) S.tile = atomicAdd(tile_counter, 1u);
+  pdl_wait();
+  pdl_launch_dependents();
+  const uint32_t gb = block_exclusive_scan_m(tid < kRadix ? __ldg(hist + tid) : 0u, S.scan);  // has __syncthreads
+  if (tid < kRadix) S.gbase[tid] = gb;
+  const uint32_t tile = S.tile;
+  const uint32_t tile_base = tile * kTileM;
+  const uint32_t wbase = tile_base + static_cast<uint32_t>(warp) * 32u * kKptM;
+
+  uint32_t keys[kKptM], ranks[kKptM], vals[kKptM];
+#pragma unroll
+  for (int j = 0; j < kKptM; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    keys[j] = idx < n ? keys_in[idx] : 0u;
+  }
+#pragma unroll
+  for (int j = 0; j < kKptM; ++j) {
+    const uint32_t idx = wbase + 32u * j + lane;
+    vals[j] = kIota ? idx : (idx < n ? vals_in[idx] : 0u);
+  }
+
+  // Rank inside the warp in (j, lane) order, i.e. input order.
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint32_t* wh = S.whist[warp];
+  uint32_t* wm = S.match[warp];
+#pragma unroll
+  for (int j = 0; j < kKptM; ++j) {
+    const bool valid = wbase + 32u * j + lane < n;
+    const uint32_t d = (keys[j] >> shift) & (kRadix - 1);
+    if (valid) atomicOr(wm + d, 1u << lane);
+    __syncwarp();
+    const uint32_t peers = valid ? wm[d] : 0u;
+    const uint32_t before = valid ? wh[d] : 0u;
+    __syncwarp();
+    if (valid && lane == __ffs(peers) - 1) {
+      wh[d] = before + __popc(peers);
+      wm[d] = 0u;
+    }
+    __syncwarp();
+    ranks[j] = before + __popc(peers & lt_mask);
+  }
+  __syncthreads();
+
+  // Thread d < 256: per-warp exclusive offsets and the tile count of digit d.
+  const uint32_t d = tid;
+  uint32_t cnt = 0;
+  volatile uint32_t* lb = lookback;
+  if (tid < kRadix) {
+#pragma unroll
+    for (int w = 0; w < kWarpsM; ++w) {
+      const uint32_t c = S.whist[w][d];
+      S.whist[w][d] = cnt;
+      cnt += c;
+    }
+    // publish this tile's count at once, so that successors looking back find it
+    if (tile == 0) lb[d] = kFlagInc | cnt;
+    else lb[static_cast<size_t>(tile) * kRadix + d] = kFlagAgg | cnt;
+  }
+  const uint32_t ts = block_exclusive_scan_m(cnt, S.scan);  // has __syncthreads
+  if (tid < kRadix) S.tstart[d] = ts;
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < kKptM; ++j) {
+    if (wbase + 32u * j + lane < n) {
+      const uint32_t dg = (keys[j] >> shift) & (kRadix - 1);
+      const uint32_t pos = S.tstart[dg] + S.whist[warp][dg] + ranks[j];
+      S.keys[pos] = keys[j];
+      S.vals[pos] = vals[j];
+    }
+  }
+
+  // Decoupled look-back for digit d (as k_onesweep).
+  if (tid < kRadix) {
+    uint32_t excl = 0;
+    if (tile != 0) {
+      int64_t k = static_cast<int64_t>(tile) - 1;
+      uint32_t spins = 0;
+      bool done = false;
+      while (!done && k >= 0) {
+        uint32_t v[kWindow];
+#pragma unroll
+        for (int j = 0; j < kWindow; ++j)
+          v[j] = (k - j >= 0) ? static_cast<uint32_t>(lb[static_cast<size_t>(k - j) * kRadix + d]) : kFlagInc;
+        bool stalled = false;
+#pragma unroll
+        for (int j = 0; j < kWindow; ++j) {
+          if (done || stalled || k < 0) continue;
+          const uint32_t flag = v[j] & ~kValueMask;
+          if (flag == 0u) {
+            stalled = true;  // predecessor k not published yet: re-read from k
+            continue;
+          }
+          excl += v[j] & kValueMask;
+          if (flag == kFlagInc) done = true;
+          else --k;
+        }
+        if (stalled) {
+          if (++spins > spin_limit) {
+            raise_status(status, kStatusSpinTimeout);
+            break;
+          }
+          __nanosleep(32);
+        }
+      }
+      lb[static_cast<size_t>(tile) * kRadix + d] = kFlagInc | ((excl + cnt) & kValueMask);
+    }
+    // output position of tile slot i of digit d: base + excl + (i - tstart),
+    // kept as one word (mod 2^32, so the subtraction may wrap)
+    S.offs[d] = S.gbase[d] + excl - S.tstart[d];
+  }
+  __syncthreads();
+
+  const uint32_t tile_n = (n - tile_base) < static_cast<uint32_t>(kTileM) ? (n - tile_base) : kTileM;
+  for (uint32_t i = tid; i < tile_n; i += kThreadsM) {
+    const uint32_t key = S.keys[i];
+    const uint32_t g = S.offs[(key >> shift) & (kRadix - 1)] + i;
+    if (g < n) {  // always true unless a look-back wait gave up (status already raised)
+      keys_out[g] = key;
+      vals_out[g] = S.vals[i];
+    }
+  }
+}
+
+template <int kWindow>
+void onesweep_match_w(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in, const uint32_t* vals_in,
+                      uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist, uint32_t* lookback,
+                      uint32_t* tile_counter, uint32_t* status, bool pdl) {
+  const size_t smem = sizeof(SortSmemM);
+  static bool configured[64] = {false};  // the attribute is per device and function
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64 && !configured[dev]) {
+    cudaFuncSetAttribute(k_onesweep_match<true, kWindow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
+    cudaFuncSetAttribute(k_onesweep_match<false, kWindow>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         static_cast<int>(smem));
+    configured[dev] = true;
+  }
+  const uint32_t grid = (n + kTileM - 1) / kTileM;
+  auto* kernel = vals_in == nullptr ? k_onesweep_match<true, kWindow> : k_onesweep_match<false, kWindow>;
+  const uint32_t spin_limit = get_wait_limit();
+  if (pdl)
+    launch_pdl(kernel, dim3(grid), dim3(kThreadsM), smem, s, keys_in, vals_in, keys_out, vals_out, n, shift, hist,
+               lookback, tile_counter, status, spin_limit);
+  else
+    kernel<<<grid, kThreadsM, smem, s>>>(keys_in, vals_in, keys_out, vals_out, n, shift, hist, lookback, tile_counter,
+                                         status, spin_limit);
+}
+
 // ---------------------------------------------------------------- 10-bit
 // The same pass over a 10-bit digit of u32 keys (1024 digits), so that three
 // passes sort 30-bit Morton codes.  Each thread owns 4 consecutive digits in
@@ -515,7 +737,11 @@ void launch_digit_hist_u64(cudaStream_t s, uint32_t n, const uint64_t* keys, int
 void launch_onesweep_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in,
                          const uint32_t* vals_in, uint32_t* keys_out, uint32_t* vals_out, const uint32_t* hist,
                          uint32_t* lookback, uint32_t* tile_counter, uint32_t* status, bool pdl) {
-  onesweep<uint32_t>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status, pdl);
+  if (n == 0) return;
+  if (get_tuning().sort_window == 8)
+    onesweep_match_w<8>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status, pdl);
+  else
+    onesweep_match_w<4>(s, n, shift, keys_in, vals_in, keys_out, vals_out, hist, lookback, tile_counter, status, pdl);
 }
 
 void launch_onesweep10_u32(cudaStream_t s, uint32_t n, uint32_t shift, const uint32_t* keys_in,
