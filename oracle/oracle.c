@@ -1352,3 +1352,104 @@ uint32_t or_self_intersection_brute(uint32_t num_tri, const uint32_t* tri2vtx, c
     }
   return cnt;
 }
+
+/* ------------------------------------------------------------------------
+ * pix2tri.rs:50-119 pix2tri_by_rasterization: every triangle is mapped to
+ * pixel space through the inverse of transform_ndc2world
+ * (px = ((x+1)/2 W, (1-y)/2 H)); each pixel whose centre it covers gets it
+ * when its depth, the barycentric interpolation of the three ndc z, is
+ * greater than the pixel's so far (pix2depth starts at -inf; strict >, so
+ * the first triangle wins a tie).  Triangles with a vertex whose homogeneous
+ * w is 0 are skipped, as transform_homogeneous returns None for them.
+ *
+ * del-geo-core's tri2_scanline (absent here) is restated from the definition
+ * of a scanline walk over pixel centres: row iy is visited when its centre
+ * line y = iy + 0.5 lies within the triangle's y extent; on it the triangle
+ * spans x in [xl, xr] (the crossings of that line with the edges), and the
+ * pixels of the row whose centres x = ix + 0.5 lie in [xl, xr] are covered.
+ * barycentric_coords (also absent) is the ratio of signed areas, None for a
+ * triangle of zero area. */
+static float cross2(float ax, float ay, float bx, float by) { return ax * by - ay * bx; }
+
+static int barycentric2(const float a[2], const float b[2], const float c[2], const float q[2], float w[3]) {
+  const float area = cross2(b[0] - a[0], b[1] - a[1], c[0] - a[0], c[1] - a[1]);
+  if (area == 0.0f) return 0;
+  w[0] = cross2(b[0] - q[0], b[1] - q[1], c[0] - q[0], c[1] - q[1]) / area;
+  w[1] = cross2(c[0] - q[0], c[1] - q[1], a[0] - q[0], a[1] - q[1]) / area;
+  w[2] = cross2(a[0] - q[0], a[1] - q[1], b[0] - q[0], b[1] - q[1]) / area;
+  return 1;
+}
+
+static int homogeneous_ok(const float m[16], const float p[3], float out[3]) {
+  const float w = m[3] * p[0] + m[7] * p[1] + m[11] * p[2] + m[15];
+  if (w == 0.0f) return 0;
+  for (int i = 0; i < 3; ++i) out[i] = (m[i] * p[0] + m[4 + i] * p[1] + m[8 + i] * p[2] + m[12 + i]) / w;
+  return 1;
+}
+
+int or_pix2tri_by_rasterization(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], uint32_t num_tri,
+                                const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t* pix2tri, float* pix2depth) {
+  float w2n[16];
+  if (!or_mat4_inverse_pivot(t_ndc2world, w2n)) return 0;
+  for (size_t i = 0; i < (size_t)img_w * img_h; ++i) {
+    pix2tri[i] = OR_UMAX;
+    pix2depth[i] = -INFINITY;
+  }
+  for (uint32_t it = 0; it < num_tri; ++it) {
+    float ndc[3][3], px[3][2];
+    int ok = 1;
+    for (int k = 0; k < 3 && ok; ++k) {
+      ok = homogeneous_ok(w2n, vtx2xyz + (size_t)tri2vtx[(size_t)it * 3 + k] * 3, ndc[k]);
+      px[k][0] = (ndc[k][0] + 1.0f) * 0.5f * (float)img_w;
+      px[k][1] = (1.0f - ndc[k][1]) * 0.5f * (float)img_h;
+    }
+    if (!ok) continue;
+    float ymin = px[0][1], ymax = px[0][1];
+    for (int k = 1; k < 3; ++k) {
+      if (px[k][1] < ymin) ymin = px[k][1];
+      if (px[k][1] > ymax) ymax = px[k][1];
+    }
+    if (!(ymin == ymin) || !(ymax == ymax)) continue;  /* NaN vertex */
+    double r0 = ceil((double)ymin - 0.5), r1 = floor((double)ymax - 0.5);
+    if (r0 < 0) r0 = 0;
+    if (r1 > (double)img_h - 1) r1 = (double)img_h - 1;
+    for (double ry = r0; ry <= r1; ry += 1.0) {
+      const uint32_t iy = (uint32_t)ry;
+      const float yc = (float)iy + 0.5f;
+      float xl = INFINITY, xr = -INFINITY;
+      for (int e = 0; e < 3; ++e) {
+        const float* p = px[e];
+        const float* q = px[(e + 1) % 3];
+        const float lo = p[1] < q[1] ? p[1] : q[1], hi = p[1] < q[1] ? q[1] : p[1];
+        if (yc < lo || yc > hi) continue;
+        if (p[1] == q[1]) { /* a horizontal edge on the centre line: both ends */
+          if (p[0] < xl) xl = p[0];
+          if (q[0] < xl) xl = q[0];
+          if (p[0] > xr) xr = p[0];
+          if (q[0] > xr) xr = q[0];
+          continue;
+        }
+        const float x = p[0] + (yc - p[1]) * (q[0] - p[0]) / (q[1] - p[1]);
+        if (x < xl) xl = x;
+        if (x > xr) xr = x;
+      }
+      if (!(xl <= xr)) continue;
+      double c0 = ceil((double)xl - 0.5), c1 = floor((double)xr - 0.5);
+      if (c0 < 0) c0 = 0;
+      if (c1 > (double)img_w - 1) c1 = (double)img_w - 1;
+      for (double cx = c0; cx <= c1; cx += 1.0) {
+        const uint32_t ix = (uint32_t)cx;
+        const float centre[2] = {(float)ix + 0.5f, yc};
+        float b[3];
+        if (!barycentric2(px[0], px[1], px[2], centre, b)) continue;
+        const float depth = b[0] * ndc[0][2] + b[1] * ndc[1][2] + b[2] * ndc[2][2];
+        const size_t ip = (size_t)iy * img_w + ix;
+        if (depth > pix2depth[ip]) {
+          pix2depth[ip] = depth;
+          pix2tri[ip] = it;
+        }
+      }
+    }
+  }
+  return 1;
+}

@@ -128,6 +128,10 @@ void or_pix2tri_work(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16]
 
 /* consumers of a pix2tri image (pix2depth.rs:107-146, pix2tri.rs:176-304) */
 int or_mat4_inverse_pivot(const float m[16], float inv[16]);
+/* pix2tri.rs:50-119 (scanline walk over pixel centres restated); returns 0
+ * when transform_ndc2world is singular. */
+int or_pix2tri_by_rasterization(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], uint32_t num_tri,
+                                const uint32_t* tri2vtx, const float* vtx2xyz, uint32_t* pix2tri, float* pix2depth);
 int or_pix2depth(uint32_t img_w, uint32_t img_h, float* pix2depth, const uint32_t* pix2tri, uint32_t num_tri,
                  const uint32_t* tri2vtx, uint32_t num_vtx, const float* vtx2xyz, const float ndc2world[16]);
 int or_pix2depth_bwd(uint32_t img_w, uint32_t img_h, float* dldw_vtx2xyz, const uint32_t* pix2tri, uint32_t num_tri,

@@ -59,6 +59,8 @@ def lib():
         L.or_tree_height.argtypes = [_u32p, u32]
         L.or_mat4_inverse_pivot.restype = i32
         L.or_mat4_inverse_pivot.argtypes = [_f32p, _f32p]
+        L.or_pix2tri_by_rasterization.restype = i32
+        L.or_pix2tri_by_rasterization.argtypes = [u32, u32, _f32p, u32, _u32p, _f32p, _u32p, _f32p]
         L.or_pix2depth.restype = i32
         L.or_pix2depth.argtypes = [u32, u32, _f32p, _u32p, u32, _u32p, u32, _f32p, _f32p]
         L.or_pix2depth_bwd.restype = i32
@@ -264,6 +266,18 @@ def tree_height(bvhnodes, num_leaf):
 
 
 # ------------------------------------- consumers of a pix2tri image
+
+def pix2tri_by_rasterization(tri2vtx, vtx2xyz, t_ndc2world_colmajor, img_w, img_h):
+    """(pix2tri, pix2depth) of pix2tri.rs:50-119 (u32::MAX / -inf where nothing covers)."""
+    tri2vtx, vtx2xyz = _c(tri2vtx, np.uint32), _c(vtx2xyz, np.float32)
+    out = np.empty((img_h, img_w), np.uint32)
+    depth = np.empty((img_h, img_w), np.float32)
+    ok = lib().or_pix2tri_by_rasterization(img_w, img_h, _c(t_ndc2world_colmajor, np.float32).reshape(-1),
+                                           tri2vtx.size // 3, tri2vtx.reshape(-1), vtx2xyz.reshape(-1), out, depth)
+    if not ok:
+        raise ValueError("transform_ndc2world is singular")
+    return out, depth
+
 
 def mat4_inverse_pivot(m_colmajor):
     inv = np.empty(16, np.float32)

@@ -7,8 +7,10 @@
 * ``oracle_cfg1.npz`` is the oracle's result for the 1280-triangle jittered
   icosphere (build + 256x256 orthographic cast), stored with its inputs so the
   same bits can be checked on any machine.
+* ``ref_assets.npz`` holds the reference's example meshes (asset/bunny_1k.obj,
+  asset/spot/spot_triangulated.obj) read from the checkout, as inputs.
 
-Usage: python tests/golden/make_golden.py <reference checkout>
+Usage: python tests/golden/make_golden.py <reference checkout> [assets]
 """
 from __future__ import annotations
 
@@ -53,10 +55,45 @@ def topology_cases():
     return cases
 
 
+def load_obj_triangles(path):
+    """Vertices and triangles of a Wavefront OBJ file of triangles (v x y z;
+    f a[/t[/n]] b c with 1-based indices)."""
+    vtx, tri = [], []
+    for line in pathlib.Path(path).read_text().splitlines():
+        f = line.split()
+        if not f:
+            continue
+        if f[0] == "v":
+            vtx.append([float(x) for x in f[1:4]])
+        elif f[0] == "f":
+            idx = [int(w.split("/")[0]) - 1 for w in f[1:]]
+            if len(idx) != 3:
+                raise ValueError(f"{path}: a face that is not a triangle")
+            tri.append(idx)
+    return np.array(tri, np.uint32), np.array(vtx, np.float32)
+
+
+def write_assets(ref_root):
+    """ref_assets.npz: the reference's two example meshes (asset/bunny_1k.obj,
+    asset/spot/spot_triangulated.obj) as arrays, parity inputs of the GPU
+    build and cast tests."""
+    root = pathlib.Path(ref_root)
+    out = {}
+    for name, rel in (("bunny", "asset/bunny_1k.obj"), ("spot", "asset/spot/spot_triangulated.obj")):
+        tri, vtx = load_obj_triangles(root / rel)
+        out[f"{name}__tri2vtx"] = tri
+        out[f"{name}__vtx2xyz"] = vtx
+    np.savez_compressed(HERE / "ref_assets.npz", **out)
+
+
 def main():
     obuild.build_oracle()
+    ref = sys.argv[1] if len(sys.argv) > 1 else None
+    if len(sys.argv) > 2 and sys.argv[2] == "assets":
+        write_assets(obuild.reference_root(ref))
+        return
     # the reference checkout: first argument, else DELMSH_REFERENCE
-    if obuild.build_ref(sys.argv[1] if len(sys.argv) > 1 else None) is None:
+    if obuild.build_ref(ref) is None:
         raise SystemExit("usage: make_golden.py <reference checkout> (or set DELMSH_REFERENCE): the reference's "
                          "sources are required to regenerate the reference-code fixtures")
     R = O.ref_lib()
@@ -94,6 +131,7 @@ def main():
                         tri2morton=r["tri2morton"], idx2tri=r["idx2tri"], idx2morton=r["idx2morton"],
                         bvhnodes=r["bvhnodes"], bvhnode2aabb=r["bvhnode2aabb"], ndc2world=m, pix2tri=p2t,
                         pix2t=p2tt)
+    write_assets(obuild.reference_root(ref))
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)
 

@@ -53,3 +53,25 @@ def lattice_rays(rng, grid, scale, num_ray):
     org = ((rng.random((num_ray, 3)) * 2 - 0.5) * (grid + 2) * scale).astype(np.float32)
     org = np.where(rng.random((num_ray, 3)) < 0.15, tgt, org)
     return np.ascontiguousarray(org), np.ascontiguousarray(tgt - org)
+
+
+def reference_pin_torus():
+    """The scene of del-msh-cpu's pix2tri test (pix2tri.rs:121-173): torus_zup
+    (1.3, 0.4, 64, 32) in f32, rotated by 1.15 rad about x, then translated
+    by (0.01, 0.61, 0.03); transform_ndc2world is the inverse of
+    diag(0.5, 0.5, 0.5, 1), i.e. diag(2, 2, 2, 1) (column-major).  Returns
+    (tri2vtx, vtx2xyz, ndc2world)."""
+    import math
+    from del_msh_gb300 import workloads as W
+    f = np.float32
+    nlg, nlt, R, r = 64, 32, f(1.3), f(0.4)
+    rlg, rlt = f(2 * math.pi) / f(nlg), f(2 * math.pi) / f(nlt)
+    ilg, ilt = np.meshgrid(np.arange(nlg, dtype=f), np.arange(nlt, dtype=f), indexing="ij")
+    lg, lt = ilg * rlg, ilt * rlt
+    r0 = R + r * np.cos(lt)
+    vtx = np.stack([r0 * np.sin(lg), r0 * np.cos(lg), r * np.sin(lt)], -1).reshape(-1, 3).astype(f)
+    c, s = f(math.cos(1.15)), f(math.sin(1.15))
+    m = np.array([[1, 0, 0, 0.01], [0, c, -s, 0.61], [0, s, c, 0.03], [0, 0, 0, 1]], f)  # translate . rot_x
+    vtx = ((vtx @ m[:3, :3].T) + m[:3, 3]).astype(f)
+    ndc2world = np.array([2, 0, 0, 0, 0, 2, 0, 0, 0, 0, 2, 0, 0, 0, 0, 1], f)
+    return W.torus_zup_topology(nlg, nlt), vtx, ndc2world

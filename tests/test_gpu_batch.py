@@ -224,3 +224,39 @@ def test_batch_cast_through_warp_tier(cuda, oracle):
         hits += int((r_p2t != 0xFFFFFFFF).sum())
     assert hits > 1000
     assert _native.device_status(clear=True) == 0
+
+
+def test_mesh_id_partition_matches_whole_batch(cuda):
+    """Meshes split by id over 3 ranks (each rank's MeshBatch built and cast
+    one after another on this GPU): every mesh's tree, boxes and image equal
+    the whole batch's, bit for bit."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300 import partition as P
+    from del_msh_gb300.batch import MeshBatch, ortho_transforms
+    meshes = W.ragged_batch(num_mesh=60, tmin=64, tmax=40000, seed=21)
+    whole = MeshBatch(meshes)
+    whole.build()
+    whole.alloc_cast(32, 24)
+    whole.cast_pixels(torch.from_numpy(ortho_transforms(meshes)).to("cuda:0"))
+    parts = P.partition_meshes([t.shape[0] for t, _ in meshes], 3)
+    results = []
+    for ids in parts:
+        sub = [meshes[m] for m in ids]
+        b = MeshBatch(sub)
+        b.build()
+        b.alloc_cast(32, 24)
+        p2t, tt = b.cast_pixels(torch.from_numpy(ortho_transforms(sub)).to("cuda:0"))
+        outs = []
+        for k in range(len(ids)):
+            bvh, aabb = b.mesh_tree(k)
+            outs.append((to_np(bvh, torch), bits(to_np(aabb, torch)), to_np(p2t[k], torch), bits(to_np(tt[k], torch))))
+        results.append((ids, outs))
+    got = P.gather_meshes(results, len(meshes))
+    for m in range(len(meshes)):
+        bvh, aabb = whole.mesh_tree(m)
+        want = (to_np(bvh, torch), bits(to_np(aabb, torch)), to_np(whole.pix2tri[m], torch),
+                bits(to_np(whole.pix2t[m], torch)))
+        for a, w in zip(got[m], want):
+            assert np.array_equal(a, w), m
+    assert _native.device_status(clear=True) == 0

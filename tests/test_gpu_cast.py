@@ -198,3 +198,50 @@ def test_full_config3_soup(cuda, oracle):
     assert np.array_equal(to_np(hit, torch), r_hit)
     assert np.array_equal(bits(to_np(t, torch)), bits(r_t))
     assert _status() == 0
+
+
+def test_cast_equals_rasterisation_reference_pin(cuda, oracle):
+    """del-msh-cpu's pixel-level pin (pix2tri.rs:121-173): the GPU's hit
+    triangle of every pixel of the 256x256 rotated torus equals the triangle
+    rasterised there (pix2tri.rs:50-119, restated in the oracle), and the
+    oracle's cast, bit for bit with t."""
+    torch = cuda
+    from helpers import reference_pin_torus
+    tri, vtx, m = reference_pin_torus()
+    p2t, tt = _cast_pixels(torch, _dev_mesh(torch, tri, vtx), m, 256, 256)
+    ras, _ = oracle.pix2tri_by_rasterization(tri, vtx, m, 256, 256)
+    assert (p2t != UMAX).sum() > 10000
+    assert np.array_equal(p2t, ras)
+    r = oracle.build(tri, vtx)
+    r_p2t, r_tt = oracle.pix2tri(tri, vtx, r["bvhnodes"], r["bvhnode2aabb"], m, 256, 256)
+    assert np.array_equal(p2t, r_p2t)
+    assert np.array_equal(bits(tt), bits(r_tt))
+    assert _status() == 0
+
+
+@pytest.mark.parametrize("name", ["bunny", "spot"])
+def test_reference_asset_meshes(cuda, oracle, golden_dir, name):
+    """The reference's example meshes (asset/bunny_1k.obj,
+    asset/spot/spot_triangulated.obj): build and a 256x256 orthographic cast
+    over the mesh's box from +z and a pinhole view, bit-exact to the oracle."""
+    torch = cuda
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    g = np.load(golden_dir / "ref_assets.npz")
+    tri, vtx = g[f"{name}__tri2vtx"], g[f"{name}__vtx2xyz"]
+    ref = oracle.build(tri, vtx)
+    got = TriMesh3.make_bvhnodes_bvhnode2aabb_ex(to_dev(tri, torch), to_dev(vtx, torch))
+    assert np.array_equal(to_np(got["bvhnodes"], torch), ref["bvhnodes"])
+    assert np.array_equal(bits(to_np(got["bvhnode2aabb"], torch)), bits(ref["bvhnode2aabb"]))
+    mesh = (to_dev(tri, torch), to_dev(vtx, torch), got["bvhnodes"], got["bvhnode2aabb"])
+    lo, hi = vtx.min(0), vtx.max(0)
+    centre = (lo + hi) / 2
+    cams = [W.box_ortho_ndc2world(lo, hi),
+            W.pinhole_ndc2world(centre + 2.5 * float((hi - lo).max()) * np.array([0.3, 0.4, 0.866]), target=centre,
+                                up=(0, 1, 0), aspect=1.0)]
+    for m in cams:
+        p2t, tt = _cast_pixels(torch, mesh, m, 256, 256)
+        r_p2t, r_tt = oracle.pix2tri(tri, vtx, ref["bvhnodes"], ref["bvhnode2aabb"], m, 256, 256)
+        assert (p2t != UMAX).sum() > 2000
+        assert np.array_equal(p2t, r_p2t)
+        assert np.array_equal(bits(tt), bits(r_tt))
+    assert _status() == 0
