@@ -790,8 +790,12 @@ int launch_batch_seg_build(cudaStream_t s, const Segments& seg, uint32_t max_tri
   k_batch_seg_classify<<<(seg.num_mesh + kThreads - 1) / kThreads, kThreads, 0, s>>>(seg, max_tri, lists, counters,
                                                                                       status);
   const SegArgs a{seg, tri2vtx, vtx2xyz, bvhnodes, other, lists, counters, counters + 2, status};
-  if (max_tri <= kSegCap) return seg_build_w<1>(s, a);
-  if (max_tri <= 2 * kSegCap) return seg_build_w<2>(s, a);
+  // the fewest blocks that hold the largest mesh, or more if tuned so (a
+  // cluster builds every mesh above one block's capacity; smaller meshes are
+  // built by single blocks either way)
+  const uint32_t least = get_tuning().batch_cluster;
+  if (max_tri <= kSegCap && least <= 1) return seg_build_w<1>(s, a);
+  if (max_tri <= 2 * kSegCap && least <= 2) return seg_build_w<2>(s, a);
   return seg_build_w<4>(s, a);
 }
 

@@ -280,12 +280,13 @@ __global__ void __launch_bounds__(kThreads) k_vtx2morton(uint32_t n, uint32_t nu
 
 // ----------------------------------------------------------------- topology
 
-__global__ void __launch_bounds__(kThreads) k_topology(uint32_t n, const uint32_t* __restrict__ c,
-                                                      const uint32_t* __restrict__ idx2obj, uint32_t* bvhnodes,
-                                                      uint32_t* other_end) {
+template <int kTh>
+__global__ void __launch_bounds__(kTh) k_topology(uint32_t n, const uint32_t* __restrict__ c,
+                                                 const uint32_t* __restrict__ idx2obj, uint32_t* bvhnodes,
+                                                 uint32_t* other_end) {
   pdl_wait();
   pdl_launch_dependents();
-  const uint32_t ib = blockIdx.x * kThreads + threadIdx.x;
+  const uint32_t ib = blockIdx.x * kTh + threadIdx.x;
   if (ib >= n - 1) return;
   topology_node(n, Codes32{c}, Objs32{idx2obj}, bvhnodes, ib, other_end);
 }
@@ -1251,13 +1252,16 @@ void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float
 }
 
 void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, const uint32_t* idx2obj,
-                     uint32_t* bvhnodes, uint32_t* other_end) {
+                     uint32_t* bvhnodes, uint32_t* other_end, uint32_t threads) {
   if (n == 1) {
     k_topology_single<<<1, 1, 0, s>>>(idx2obj, bvhnodes);
     return;
   }
-  const uint32_t grid = (n - 1 + kThreads - 1) / kThreads;
-  launch_pdl(k_topology, dim3(grid), dim3(kThreads), 0, s, n, idx2morton, idx2obj, bvhnodes, other_end);
+  const uint32_t th = threads == 128 || threads == 512 ? threads : 256u;
+  const uint32_t grid = (n - 1 + th - 1) / th;
+  if (th == 128) launch_pdl(k_topology<128>, dim3(grid), dim3(128), 0, s, n, idx2morton, idx2obj, bvhnodes, other_end);
+  else if (th == 512) launch_pdl(k_topology<512>, dim3(grid), dim3(512), 0, s, n, idx2morton, idx2obj, bvhnodes, other_end);
+  else launch_pdl(k_topology<256>, dim3(grid), dim3(256), 0, s, n, idx2morton, idx2obj, bvhnodes, other_end);
 }
 
 // The kernels after the first of this sequence are launched with launch_pdl

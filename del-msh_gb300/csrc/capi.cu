@@ -122,8 +122,7 @@ SortLayout sort_layout(uint32_t n, int num_pass, size_t key_bytes, int radix = d
 struct BuildLayout {
   size_t transform, aabb, ticket, height, front_bar, sort_hdr, partials, codes, akeys, avals, bvals, flags, tribox,
       front_counts, front_totals, total, zero_bytes, sort_bytes;
-  bool radix10;  // three 10-bit passes (dm::kRadix10MaxKeys), else four 8-bit ones
-  SortLayout sort;
+  SortLayout sort8, sort10;  // four 8-bit passes / three 10-bit passes
 };
 
 BuildLayout build_layout(uint32_t T) {
@@ -134,9 +133,10 @@ BuildLayout build_layout(uint32_t T) {
   L.height = 100;
   L.front_bar = 104;
   L.sort_hdr = 256;
-  L.radix10 = T <= dm::kRadix10MaxKeys;
-  L.sort = L.radix10 ? sort_layout(T, 3, 4, dm::kRadix10) : sort_layout(T, 4, 4);
-  L.sort_bytes = L.sort.zero_bytes;  // header + lookback (the tmp arrays are carved separately)
+  L.sort8 = sort_layout(T, 4, 4);
+  L.sort10 = sort_layout(T, 3, 4, dm::kRadix10);
+  // header + lookback of either width (the tmp arrays are carved separately)
+  L.sort_bytes = std::max(L.sort8.zero_bytes, L.sort10.zero_bytes);
   L.zero_bytes = L.sort_hdr + L.sort_bytes;
   L.partials = align256(L.zero_bytes);
   L.codes = L.partials + align256(dm::kAabbBlocks * 6 * 4);
@@ -198,12 +198,19 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   if (int e = sc.acquire(scratch, scratch_bytes, L.total, s, nullptr)) return e;
   void* base = sc.ptr;
   uint32_t* status = status_ptr();
-  DM_CUDA(cudaMemsetAsync(base, 0, L.zero_bytes, s));
+  // the size class's choices (autotuned; every choice builds the same tree)
+  const dm::BuildTuning bt = dm::build_tuning_for(T);
+  const bool try_front = bt.build_path == 0 && T >= 2 && T <= dm::front_max_tri();
+  const bool radix10 = bt.sort_radix == 10 || (bt.sort_radix == 0 && T <= dm::kRadix10MaxKeys);
+  const SortLayout& SL = radix10 ? L.sort10 : L.sort8;
+  // the front needs only the header zeroed; the separate kernels also their
+  // histograms, tile counters and look-back words
+  DM_CUDA(cudaMemsetAsync(base, 0, try_front ? L.sort_hdr : L.sort_hdr + SL.zero_bytes, s));
   DM_CUDA(cudaMemsetAsync(at<char>(base, L.flags), 0, static_cast<size_t>(T) * 4, s));
   float* transform = at<float>(base, L.transform);
-  uint32_t* hist = at<uint32_t>(base, L.sort_hdr + L.sort.hist);
-  uint32_t* counters = at<uint32_t>(base, L.sort_hdr + L.sort.counters);
-  uint32_t* lookback = at<uint32_t>(base, L.sort_hdr + L.sort.lookback);
+  uint32_t* hist = at<uint32_t>(base, L.sort_hdr + SL.hist);
+  uint32_t* counters = at<uint32_t>(base, L.sort_hdr + SL.counters);
+  uint32_t* lookback = at<uint32_t>(base, L.sort_hdr + SL.lookback);
   uint32_t* codes = at<uint32_t>(base, L.codes);
   uint32_t* ak = at<uint32_t>(base, L.akeys);
   uint32_t* av = at<uint32_t>(base, L.avals);
@@ -230,7 +237,7 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   // ak.  The profile's Morton stage is then empty and its sort stage covers
   // the whole front.
   bool front = false;
-  if (T >= 2 && T <= dm::front_max_tri()) {
+  if (try_front) {
     uint32_t* ok = idx2morton_out ? idx2morton_out : codes;
     uint32_t* ov = idx2tri_out ? idx2tri_out : bv;
     if (ev) DM_CUDA(cudaEventRecord(ev[1], s));
@@ -247,25 +254,26 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
     ov = idx2tri_out ? idx2tri_out : bv;
     other_end = other_end_out ? other_end_out : ak;
   } else {
+    if (try_front)  // the cooperative launch was refused: zero what the separate kernels need
+      DM_CUDA(cudaMemsetAsync(at<char>(base, L.sort_hdr), 0, SL.zero_bytes, s));
     dm::launch_centroid_aabb(s, T, tri2vtx, num_vtx, vtx2xyz, at<float>(base, L.partials),
                              at<uint32_t>(base, L.ticket), at<float>(base, L.aabb), transform, status, cent, cstride,
                              tribox);
-    dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status, cent, cstride,
-                          L.radix10);
+    dm::launch_morton_tri(s, T, tri2vtx, num_vtx, vtx2xyz, transform, codes, hist, status, cent, cstride, radix10);
     if (tri2morton_out) DM_CUDA(cudaMemcpyAsync(tri2morton_out, codes, size_t{4} * T, cudaMemcpyDeviceToDevice, s));
     // 3 passes: codes -> (ak, av) -> (codes, bv) -> (ok, ov), by default the A
     //   buffers (dead after pass 2); other_end then takes bv.
     // 4 passes: codes -> (ak, av) -> (codes, bv) -> (ak, av) -> (ok, ov), by
     //   default (codes, bv) (dead after pass 2); other_end then takes ak.
-    ok = idx2morton_out ? idx2morton_out : (L.radix10 ? ak : codes);
-    ov = idx2tri_out ? idx2tri_out : (L.radix10 ? av : bv);
+    ok = idx2morton_out ? idx2morton_out : (radix10 ? ak : codes);
+    ov = idx2tri_out ? idx2tri_out : (radix10 ? av : bv);
     if (ev) DM_CUDA(cudaEventRecord(ev[1], s));
-    if (L.radix10) sort3(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
+    if (radix10) sort3(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
     else sort4(s, T, codes, ak, av, codes, bv, ok, ov, hist, counters, lookback, status);
-    other_end = other_end_out ? other_end_out : (L.radix10 ? bv : ak);
+    other_end = other_end_out ? other_end_out : (radix10 ? bv : ak);
   }
   if (ev) DM_CUDA(cudaEventRecord(ev[2], s));
-  dm::launch_topology(s, T, ok, ov, bvhnodes, other_end);
+  dm::launch_topology(s, T, ok, ov, bvhnodes, other_end, bt.topo_threads);
   if (ev) DM_CUDA(cudaEventRecord(ev[3], s));
   // the height is only computed on request: it needs the tree-order climb
   dm::launch_refit_windowed(s, T, dm::Segments{1, nullptr, nullptr}, num_vtx, bvhnodes, other_end, tri2vtx, vtx2xyz,
@@ -361,6 +369,39 @@ Tuning g_tuning;
 std::atomic<uint32_t> g_wait_limit{kDefaultWaitLimit};
 }  // namespace
 
+namespace {
+BuildTuning g_build_classes[kMaxBuildClasses];
+uint32_t g_num_build_classes = 0;
+}  // namespace
+
+BuildTuning build_tuning_for(uint32_t num_tri) {
+  std::lock_guard<std::mutex> lk(g_tuning_mutex);
+  for (uint32_t i = 0; i < g_num_build_classes; ++i)
+    if (num_tri <= g_build_classes[i].max_tri) return g_build_classes[i];
+  return BuildTuning{};
+}
+
+bool set_build_classes(const BuildTuning* classes, uint32_t n) {
+  if (n > static_cast<uint32_t>(kMaxBuildClasses) || (n > 0 && !classes)) return false;
+  for (uint32_t i = 0; i < n; ++i) {
+    const BuildTuning& c = classes[i];
+    if (c.build_path > 1 || !(c.sort_radix == 0 || c.sort_radix == 8 || c.sort_radix == 10)) return false;
+    if (!(c.topo_threads == 0 || c.topo_threads == 128 || c.topo_threads == 256 || c.topo_threads == 512))
+      return false;
+    if (i > 0 && c.max_tri <= classes[i - 1].max_tri) return false;  // ascending bounds
+  }
+  std::lock_guard<std::mutex> lk(g_tuning_mutex);
+  for (uint32_t i = 0; i < n; ++i) g_build_classes[i] = classes[i];
+  g_num_build_classes = n;
+  return true;
+}
+
+uint32_t get_build_classes(BuildTuning* out, uint32_t cap) {
+  std::lock_guard<std::mutex> lk(g_tuning_mutex);
+  for (uint32_t i = 0; i < g_num_build_classes && i < cap; ++i) out[i] = g_build_classes[i];
+  return g_num_build_classes;
+}
+
 uint32_t get_wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
 void set_wait_limit(uint32_t polls) { g_wait_limit.store(polls, std::memory_order_relaxed); }
 
@@ -378,6 +419,7 @@ bool set_tuning(const Tuning& t) {
   if (!cast_ok || !tile_ok || !sort_ok) return false;
   if (!phase_ok(t.cast_refill_min) || !phase_ok(t.cast_leaf_min) || !phase_ok(t.cast_ascend_min)) return false;
   if (t.cast_long_steps < 1 || t.cast_long_steps > (1u << 30)) return false;
+  if (t.batch_path > 1 || !(t.batch_cluster <= 2 || t.batch_cluster == 4)) return false;
   std::lock_guard<std::mutex> lk(g_tuning_mutex);
   g_tuning = t;
   return true;
@@ -406,7 +448,8 @@ int dm_tuning_get(dm_tuning* out) {
   DM_REQUIRE(out, "NULL argument");
   const dm::Tuning t = dm::get_tuning();
   *out = dm_tuning{t.cast_threads,    t.cast_stack,    t.tile_w,          t.sort_window,
-                   t.cast_refill_min, t.cast_leaf_min, t.cast_ascend_min, t.cast_long_steps};
+                   t.cast_refill_min, t.cast_leaf_min, t.cast_ascend_min, t.cast_long_steps,
+                   t.batch_path,      t.batch_cluster};
   return DM_OK;
 }
 
@@ -422,11 +465,36 @@ int dm_tuning_set(const dm_tuning* in) {
   t.cast_leaf_min = phase(in->cast_leaf_min);
   t.cast_ascend_min = phase(in->cast_ascend_min);
   t.cast_long_steps = in->cast_long_steps == 0 ? dm::kDefaultLongSteps : in->cast_long_steps;
+  t.batch_path = in->batch_path;
+  t.batch_cluster = in->batch_cluster;
   DM_REQUIRE(dm::set_tuning(t),
              "unsupported tuning (cast %u threads x %u frames, tile_w %u, sort window %u, phase minima %u/%u/%u, "
-             "long-ray steps %u)",
+             "long-ray steps %u, batch path %u, batch cluster %u)",
              in->cast_threads, in->cast_stack, in->tile_w, in->sort_window, t.cast_refill_min, t.cast_leaf_min,
-             t.cast_ascend_min, t.cast_long_steps);
+             t.cast_ascend_min, t.cast_long_steps, t.batch_path, t.batch_cluster);
+  return DM_OK;
+}
+
+int dm_build_classes_set(const dm_build_class* classes, uint32_t num_class) {
+  DM_REQUIRE(num_class <= static_cast<uint32_t>(dm::kMaxBuildClasses), "at most %d build classes",
+             dm::kMaxBuildClasses);
+  DM_REQUIRE(num_class == 0 || classes, "NULL argument");
+  dm::BuildTuning b[dm::kMaxBuildClasses];
+  for (uint32_t i = 0; i < num_class; ++i)
+    b[i] = dm::BuildTuning{classes[i].max_tri, classes[i].build_path, classes[i].sort_radix, classes[i].topo_threads};
+  DM_REQUIRE(dm::set_build_classes(b, num_class),
+             "unsupported build classes (bounds must ascend; build_path 0/1, sort_radix 0/8/10, topo_threads "
+             "0/128/256/512)");
+  return DM_OK;
+}
+
+int dm_build_classes_get(dm_build_class* out, uint32_t capacity, uint32_t* num_class) {
+  DM_REQUIRE(num_class && (capacity == 0 || out), "NULL argument");
+  dm::BuildTuning b[dm::kMaxBuildClasses];
+  const uint32_t n = dm::get_build_classes(b, dm::kMaxBuildClasses);
+  for (uint32_t i = 0; i < n && i < capacity; ++i)
+    out[i] = dm_build_class{b[i].max_tri, b[i].build_path, b[i].sort_radix, b[i].topo_threads};
+  *num_class = n;
   return DM_OK;
 }
 
@@ -792,7 +860,7 @@ int dm_batch_trimesh3_build(uint64_t stream_ptr, uint32_t num_mesh, const uint32
   uint32_t* status = status_ptr();
   const dm::Segments seg{num_mesh, mesh2tri, mesh2vtx};
   DM_CUDA(cudaMemsetAsync(at<char>(base, L.flags), 0, size_t{4} * total_tri, s));
-  if (max_tri_per_mesh <= dm::kSegMaxTri) {
+  if (max_tri_per_mesh <= dm::kSegMaxTri && dm::get_tuning().batch_path == 0) {
     // every mesh sorted and linked on chip (the lists reuse the key buffer)
     uint32_t* seg_counters = at<uint32_t>(base, L.counters) + 8;
     DM_CUDA(cudaMemsetAsync(seg_counters, 0, 4 * sizeof(uint32_t), s));

@@ -49,7 +49,7 @@ void launch_vtx2morton(cudaStream_t s, uint32_t n, uint32_t num_dim, const float
 // u32[n-1]): for each branch the end of its leaf range that is not its own
 // index (a branch index is always one end of its range).
 void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, const uint32_t* idx2obj,
-                     uint32_t* bvhnodes, uint32_t* other_end = nullptr);
+                     uint32_t* bvhnodes, uint32_t* other_end = nullptr, uint32_t threads = 256);
 
 // Vertex indices >= num_vtx are replaced by 0 and raise kStatusBadIndex.
 // Bottom-up refit (bvhnode2aabb.cu:7-65 semantics, values of
@@ -235,7 +235,26 @@ struct Tuning {
   // node entries after which the persistent cast, once a warp has no more
   // rays to take, hands a ray entering a long chain to the warp tier
   uint32_t cast_long_steps = kDefaultLongSteps;
+  // batched build: 0 = every mesh sorted and linked on chip when the largest
+  // fits (<= kSegMaxTri triangles), 1 = the global 64-bit sort
+  uint32_t batch_path = 0;
+  // batched on-chip build: the least number of blocks (1, 2 or 4) that
+  // build a mesh too large for one block (0 = the fewest that fit)
+  uint32_t batch_cluster = 0;
 };
+// Single-mesh build choices for meshes of up to max_tri triangles (the
+// smallest class that holds the mesh applies; none: the defaults).  Every
+// choice gives the same tree and boxes.
+struct BuildTuning {
+  uint32_t max_tri = 0xFFFFFFFFu;
+  uint32_t build_path = 0;    // 0 = the cooperative front where it fits, 1 = separate kernels
+  uint32_t sort_radix = 0;    // separate kernels: 0 = 10 bits up to kRadix10MaxKeys keys, else 8; or 8 / 10
+  uint32_t topo_threads = 0;  // threads per block of the topology kernel: 0 = 256, or 128 / 256 / 512
+};
+constexpr int kMaxBuildClasses = 8;
+BuildTuning build_tuning_for(uint32_t num_tri);
+bool set_build_classes(const BuildTuning* classes, uint32_t n);  // false (nothing changed) for a bad table
+uint32_t get_build_classes(BuildTuning* out, uint32_t cap);
 // (threads, stack) pairs compiled for the persistent cast
 constexpr uint32_t kCastVariants[][2] = {{128, 64}, {64, 64}, {256, 64}, {128, 32}, {128, 96}};
 Tuning get_tuning();

@@ -33,6 +33,8 @@ _SIGNATURES = {
     "dm_pix2tri_interpolate": (i32, [u64, u32, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp]),
     "dm_pix2tri_interpolate_bwd": (i32, [u64, u32, u32, vp, u32, vp, u32, vp, u32, vp, vp, vp, vp, vp]),
     "dm_tuning_set": (i32, [vp]),
+    "dm_build_classes_set": (i32, [vp, u32]),
+    "dm_build_classes_get": (i32, [vp, u32, vp]),
     "dm_wait_limit_get": (i32, [vp]),
     "dm_wait_limit_set": (i32, [u32]),
     "dm_selftest_bounded_wait": (i32, [u64, u32, vp, sz]),
@@ -72,12 +74,35 @@ class Tuning(C.Structure):
     """dm_tuning of include/delmsh_gb300.h."""
     _fields_ = [("cast_threads", C.c_uint32), ("cast_stack", C.c_uint32), ("tile_w", C.c_uint32),
                 ("sort_window", C.c_uint32), ("cast_refill_min", C.c_uint32), ("cast_leaf_min", C.c_uint32),
-                ("cast_ascend_min", C.c_uint32), ("cast_long_steps", C.c_uint32)]
+                ("cast_ascend_min", C.c_uint32), ("cast_long_steps", C.c_uint32), ("batch_path", C.c_uint32),
+                ("batch_cluster", C.c_uint32)]
     KEYS = ("cast_threads", "cast_stack", "tile_w", "sort_window", "cast_refill_min", "cast_leaf_min",
-            "cast_ascend_min", "cast_long_steps")
+            "cast_ascend_min", "cast_long_steps", "batch_path", "batch_cluster")
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k in self.KEYS}
+
+
+class BuildClass(C.Structure):
+    """dm_build_class of include/delmsh_gb300.h."""
+    _fields_ = [("max_tri", C.c_uint32), ("build_path", C.c_uint32), ("sort_radix", C.c_uint32),
+                ("topo_threads", C.c_uint32)]
+    KEYS = ("max_tri", "build_path", "sort_radix", "topo_threads")
+
+
+def set_build_classes(classes) -> None:
+    """Sets the single-mesh build's size classes (a list of dicts with the
+    BuildClass keys, bounds ascending; [] clears them)."""
+    arr = (BuildClass * max(1, len(classes)))(*[BuildClass(*(int(c.get(k, 0)) for k in BuildClass.KEYS))
+                                                 for c in classes])
+    call("dm_build_classes_set", C.addressof(arr), len(classes))
+
+
+def get_build_classes() -> list:
+    arr = (BuildClass * 8)()
+    n = C.c_uint32(0)
+    call("dm_build_classes_get", C.addressof(arr), 8, C.byref(n))
+    return [{k: int(getattr(arr[i], k)) for k in BuildClass.KEYS} for i in range(n.value)]
 
 
 def get_tuning() -> dict:
@@ -87,10 +112,11 @@ def get_tuning() -> dict:
 
 
 def set_tuning(cast_threads: int, cast_stack: int, tile_w: int, sort_window: int, cast_refill_min: int = 0,
-               cast_leaf_min: int = 0, cast_ascend_min: int = 0, cast_long_steps: int = 0) -> None:
+               cast_leaf_min: int = 0, cast_ascend_min: int = 0, cast_long_steps: int = 0, batch_path: int = 0,
+               batch_cluster: int = 0) -> None:
     """Sets dm_tuning; a phase minimum or step budget of 0 selects the library default."""
     t = Tuning(cast_threads, cast_stack, tile_w, sort_window, cast_refill_min, cast_leaf_min, cast_ascend_min,
-               cast_long_steps)
+               cast_long_steps, batch_path, batch_cluster)
     call("dm_tuning_set", C.addressof(t))
 
 

@@ -20,11 +20,13 @@ flushed (a 256 MiB write) outside the timed region between repetitions.
 ``del_msh_gb300._native.load()`` calls ``apply()`` on the table shipped next to
 this file, if there is one.
 
-The radix width stays at 8 bits.  With 256 digits a 2M-key pass is one wave
-of 547 tiles, four 41 KB tiles per SM.  10-bit digits need 32 KB of per-warp
-digit counters (74 KB per tile, three tiles per SM) and 11-bit ones 64 KB (one
-or two per SM), so a pass would take two waves or more, which costs more than
-the one pass (of four) it saves over 30-bit codes.
+``tune_build()`` sweeps the single-mesh build by size class (a displaced
+torus standing for each class): the cooperative front or the separate
+kernels, for the separate kernels the radix width (three 10-bit or four 8-bit
+passes), and the topology kernel's block size; ``tune_batched()`` sweeps the
+batched build's path (on chip or the global sort) and least cluster size on
+the ragged 4096-mesh workload and on a batch of meshes of up to 16384
+triangles.  ``tune_all()`` runs the three and writes one table.
 """
 from __future__ import annotations
 
@@ -42,7 +44,7 @@ SORT_WINDOWS = [4, 8]
 PHASE_CHOICES = [(1, 1, 1), (4, 4, 4), (6, 6, 6), (8, 8, 8), (8, 6, 6), (12, 8, 8), (16, 8, 8), (12, 12, 12),
                  (16, 12, 12), (24, 8, 8), (20, 10, 10), (8, 4, 4), (12, 4, 4), (12, 6, 6), (16, 6, 6), (6, 2, 2)]
 DEFAULT = dict(cast_threads=128, cast_stack=64, tile_w=8, sort_window=4, cast_refill_min=6, cast_leaf_min=6,
-               cast_ascend_min=6, cast_long_steps=64)
+               cast_ascend_min=6, cast_long_steps=64, batch_path=0, batch_cluster=0)
 _PHASE_KEYS = ("cast_refill_min", "cast_leaf_min", "cast_ascend_min")
 
 
@@ -66,9 +68,15 @@ def apply(path=DEFAULT_TABLE, device="cuda:0") -> dict | None:
     name = _device_name(device)
     if name is None or table.get("device") != name:
         return None
-    best = table["best"]
+    best = dict(table["best"])
+    batched = table.get("batched_best", {})
     _native.set_tuning(best["cast_threads"], best["cast_stack"], best["tile_w"], best["sort_window"],
-                       *(best.get(k, 0) for k in _PHASE_KEYS))  # 0: the library default
+                       *(best.get(k, 0) for k in _PHASE_KEYS),  # 0: the library default
+                       0, batched.get("batch_path", 0), batched.get("batch_cluster", 0))
+    if "build_classes" in table:
+        _native.set_build_classes([{k: c[k] for k in ("max_tri", "build_path", "sort_radix", "topo_threads")}
+                                   for c in table["build_classes"]])
+    best.update(batched)
     return best
 
 
@@ -81,6 +89,15 @@ def pick_cast(cast_sweep, tolerance: float = 0.01) -> dict:
     fastest = min(c["ms"] for c in ok)
     near = [c for c in ok if c["ms"] <= fastest * (1 + tolerance)]
     return min(near, key=lambda c: (-c["cast_stack"], c["ms"]))
+
+
+def pick_over_default(sweep, is_default, key="ms", tolerance: float = 0.01) -> dict:
+    """The default choice unless an identical-output choice is more than
+    `tolerance` faster; then the fastest."""
+    ok = [c for c in sweep if c["identical"]]
+    dflt = next(c for c in ok if is_default(c))
+    fastest = min(ok, key=lambda c: c[key])
+    return fastest if fastest[key] < dflt[key] * (1 - tolerance) else dflt
 
 
 def _events_ms(torch, stream, fn, flush, reps: int) -> float:
@@ -207,6 +224,127 @@ def tune(device="cuda:0", out=DEFAULT_TABLE, reps: int = 15, ndiv: int = 1024, i
     return table
 
 
+BUILD_CLASSES = [(131_072, 181), (1_048_576, 512), (4_194_304, 1024), (0xFFFFFFFF, 2048)]  # (bound, torus ndiv)
+BUILD_CHOICES = ([dict(build_path=0, sort_radix=0, topo_threads=t) for t in (128, 256, 512)] +
+                 [dict(build_path=1, sort_radix=r, topo_threads=t) for r in (8, 10) for t in (128, 256, 512)])
+BATCH_CHOICES = [dict(batch_path=0, batch_cluster=0), dict(batch_path=0, batch_cluster=2),
+                 dict(batch_path=0, batch_cluster=4), dict(batch_path=1, batch_cluster=0)]
+
+
+def tune_build(device="cuda:0", reps: int = 15, classes=BUILD_CLASSES, seed: int = 0) -> list:
+    """Per size class, every build choice on a displaced torus of that class:
+    build time (median, L2 flushed) and whether the tree and boxes equal the
+    default choice's bit for bit.  Returns the table's class entries, each
+    with its fastest identical choice and its sweep."""
+    import numpy as np
+    import torch
+
+    from . import workloads as W
+
+    dev = torch.device(device)
+    L = _native.load()
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    flush = torch.empty((256 << 20,), dtype=torch.uint8, device=dev)
+    before = _native.get_build_classes()
+    out = []
+    try:
+        for bound, ndiv in classes:
+            tri, vtx = W.displaced_torus(ndiv, seed=seed)
+            T, V = tri.shape[0], vtx.shape[0]
+            d_tri = torch.from_numpy(tri.view(np.int32)).to(dev)
+            d_vtx = torch.from_numpy(vtx).to(dev)
+            bvh = torch.empty((2 * T - 1, 3), dtype=torch.int32, device=dev)
+            aabb = torch.empty((2 * T - 1, 6), dtype=torch.float32, device=dev)
+            bs = L.dm_trimesh3_build_scratch_bytes(T)
+            scr = torch.empty((bs,), dtype=torch.uint8, device=dev)
+
+            def build():
+                _native.call("dm_trimesh3_make_bvhnodes_bvhnode2aabb", sp, T, d_tri.data_ptr(), V,
+                             d_vtx.data_ptr(), bvh.data_ptr(), aabb.data_ptr(), scr.data_ptr(), bs)
+
+            _native.set_build_classes([])
+            build()
+            torch.cuda.synchronize(dev)
+            ref = (bvh.clone(), aabb.clone().view(torch.int32))
+            sweep = []
+            for c in BUILD_CHOICES:
+                _native.set_build_classes([dict(max_tri=0xFFFFFFFF, **c)])
+                for _ in range(3):
+                    build()
+                ms = _events_ms(torch, stream, build, flush, reps)
+                same = bool(torch.equal(bvh, ref[0]) and torch.equal(aabb.view(torch.int32), ref[1]))
+                sweep.append(dict(c, ms=ms, identical=same))
+            best = pick_over_default(sweep, lambda c: c["build_path"] == 0 and c["topo_threads"] == 256)
+            out.append(dict(max_tri=bound, build_path=best["build_path"], sort_radix=best["sort_radix"],
+                            topo_threads=best["topo_threads"], ms=best["ms"], workload_tri=T, sweep=sweep))
+            del d_tri, d_vtx, bvh, aabb, scr
+            torch.cuda.empty_cache()
+    finally:
+        _native.set_build_classes(before)
+    return out
+
+
+def tune_batched(device="cuda:0", reps: int = 5, seed: int = 0) -> list:
+    """The batched build's choices on the ragged 4096-mesh workload (triangle
+    counts log-uniform in [64, 65536]) and on 4096 meshes of [64, 16384]
+    triangles: build time of MeshBatch.build (median, L2 flushed) and whether
+    every tree and box equals the default's bit for bit."""
+    import torch
+
+    from . import workloads as W
+    from .batch import MeshBatch
+
+    dev = torch.device(device)
+    stream = torch.cuda.current_stream(dev)
+    flush = torch.empty((256 << 20,), dtype=torch.uint8, device=dev)
+    base = _native.get_tuning()
+    out = []
+    try:
+        for tmax in (65536, 16384):
+            meshes = W.ragged_batch(num_mesh=4096, tmin=64, tmax=tmax, seed=seed)
+            b = MeshBatch(meshes, dev)
+            _native.set_tuning(**dict(base, batch_path=0, batch_cluster=0))
+            b.build()
+            torch.cuda.synchronize(dev)
+            ref = (b.bvhnodes.clone().view(torch.int32), b.bvhnode2aabb.clone().view(torch.int32))
+            sweep = []
+            for c in BATCH_CHOICES:
+                _native.set_tuning(**dict(base, **c))
+                for _ in range(2):
+                    b.build()
+                ms = _events_ms(torch, stream, b.build, flush, reps)
+                same = bool(torch.equal(b.bvhnodes.view(torch.int32), ref[0]) and
+                            torch.equal(b.bvhnode2aabb.view(torch.int32), ref[1]))
+                sweep.append(dict(c, ms=ms, identical=same))
+            best = pick_over_default(sweep, lambda c: c["batch_path"] == 0 and c["batch_cluster"] == 0)
+            out.append(dict(max_tri=b.max_tri, total_tri=b.total_tri, batch_path=best["batch_path"],
+                            batch_cluster=best["batch_cluster"], ms=best["ms"], sweep=sweep))
+            del b
+            torch.cuda.empty_cache()
+    finally:
+        _native.set_tuning(**base)
+    return out
+
+
+def tune_all(device="cuda:0", out=DEFAULT_TABLE, reps: int = 15) -> dict:
+    """tune() (cast and look-back window on the single-mesh workload), then
+    tune_build() and tune_batched(); one table with all three.  The batched
+    choice applied is the one measured on the ragged 4096-mesh workload."""
+    table = tune(device, None, reps)
+    start = time.time()
+    table["build_classes"] = tune_build(device, reps)
+    table["batched"] = tune_batched(device)
+    big = table["batched"][0]
+    table["batched_best"] = {"batch_path": big["batch_path"], "batch_cluster": big["batch_cluster"]}
+    table["device_status"] = max(table["device_status"], _native.device_status(clear=True))
+    table["sweep_s"] += time.time() - start
+    if out is not None:
+        pathlib.Path(out).write_text(json.dumps(table, indent=1) + "\n")
+        apply(out)
+    return table
+
+
 if __name__ == "__main__":
     import argparse
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
@@ -214,5 +352,8 @@ if __name__ == "__main__":
     ap.add_argument("--out", default=str(DEFAULT_TABLE))
     ap.add_argument("--reps", type=int, default=15)
     args = ap.parse_args()
-    t = tune(args.device, args.out, args.reps)
-    print(json.dumps({k: t[k] for k in ("device", "best", "speedup_cast_vs_default", "sweep_s")}))
+    t = tune_all(args.device, args.out, args.reps)
+    print(json.dumps({"device": t["device"], "best": t["best"], "batched_best": t["batched_best"],
+                      "build_classes": [{k: c[k] for k in ("max_tri", "build_path", "sort_radix", "topo_threads",
+                                                          "ms")} for c in t["build_classes"]],
+                      "sweep_s": t["sweep_s"]}))

@@ -83,6 +83,14 @@ typedef struct dm_tuning {
      tier, where one warp runs it and folds the links 32 at a time: 1..2^30,
      0 = the default (64).  Results do not depend on it. */
   uint32_t cast_long_steps;
+  /* Batched build: 0 = every mesh sorted and linked on chip when the largest
+     has at most 65536 triangles (else the global sort), 1 = the global 64-bit
+     sort always. */
+  uint32_t batch_path;
+  /* Batched on-chip build: the least number of blocks (1, 2 or 4) that build
+     a mesh too large for one block; 0 = the fewest that hold the largest
+     mesh. */
+  uint32_t batch_cluster;
 } dm_tuning;
 
 /* The current launch parameters. */
@@ -91,6 +99,20 @@ int dm_tuning_get(dm_tuning* out);
 /* Sets the launch parameters; DM_ERR_INVALID_ARGUMENT (nothing changed) for
  * a combination that is not compiled. */
 int dm_tuning_set(const dm_tuning* in);
+
+/* Single-mesh build choices by mesh size: a build of T triangles uses the
+ * first class (bounds ascending) with T <= max_tri, or the defaults (all 0)
+ * when none holds it.  Every choice builds the same tree and boxes.
+ * Process-wide, read at each build.  No reference counterpart. */
+typedef struct dm_build_class {
+  uint32_t max_tri;      /* the class holds meshes of up to this many triangles */
+  uint32_t build_path;   /* 0 = centroids, codes and sort in one cooperative launch where the mesh fits on the
+                            device at once, 1 = the separate kernels */
+  uint32_t sort_radix;   /* separate kernels: 0 = 10-bit digits up to 2^19 keys, else 8; or 8 / 10 */
+  uint32_t topo_threads; /* threads per block of the topology kernel: 0 (= 256), 128, 256 or 512 */
+} dm_build_class;
+int dm_build_classes_set(const dm_build_class* classes, uint32_t num_class);  /* at most 8; 0 clears */
+int dm_build_classes_get(dm_build_class* out, uint32_t capacity, uint32_t* num_class);
 
 /* Polls a bounded device wait (the radix sort's look-back) makes before it
  * gives up, raises status bit 1 and returns instead of hanging.  Process-wide,

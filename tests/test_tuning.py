@@ -19,7 +19,8 @@ def test_tuning_roundtrip_and_validation():
                     _native.set_tuning(threads, frames, tile_w, window)  # phase minima 0: the default, 6
                     assert _native.get_tuning() == dict(cast_threads=threads, cast_stack=frames, tile_w=tile_w,
                                                         sort_window=window, cast_refill_min=6, cast_leaf_min=6,
-                                                        cast_ascend_min=6, cast_long_steps=64)
+                                                        cast_ascend_min=6, cast_long_steps=64, batch_path=0,
+                                                        batch_cluster=0)
         for mins in PHASE_CHOICES + [(1, 32, 32), (32, 1, 32), (32, 32, 1)]:
             _native.set_tuning(128, 64, 8, 4, *mins)
             assert tuple(_native.get_tuning()[k] for k in ("cast_refill_min", "cast_leaf_min",
@@ -27,12 +28,34 @@ def test_tuning_roundtrip_and_validation():
         _native.set_tuning(**DEFAULT)
         for bad in [(96, 64, 8, 4), (128, 48, 8, 4), (128, 64, 3, 4), (128, 64, 64, 4), (128, 64, 8, 5),
                     (128, 64, 8, 4, 33, 6, 6), (128, 64, 8, 4, 6, 40, 6), (128, 64, 8, 4, 6, 6, 33),
-                    (128, 64, 8, 4, 6, 6, 6, (1 << 30) + 1)]:
+                    (128, 64, 8, 4, 6, 6, 6, (1 << 30) + 1), (128, 64, 8, 4, 6, 6, 6, 64, 2),
+                    (128, 64, 8, 4, 6, 6, 6, 64, 0, 3)]:
             with pytest.raises(_native.DelMshError):
                 _native.set_tuning(*bad)
             assert _native.get_tuning() == DEFAULT  # a rejected choice changes nothing
     finally:
         _native.set_tuning(**before)
+
+
+def test_build_classes_roundtrip_and_validation():
+    from del_msh_gb300 import _native
+    before = _native.get_build_classes()
+    try:
+        good = [dict(max_tri=1 << 16, build_path=1, sort_radix=10, topo_threads=128),
+                dict(max_tri=1 << 21, build_path=0, sort_radix=0, topo_threads=512),
+                dict(max_tri=0xFFFFFFFF, build_path=1, sort_radix=8, topo_threads=256)]
+        _native.set_build_classes(good)
+        assert _native.get_build_classes() == good
+        for bad in ([dict(max_tri=10), dict(max_tri=5)],  # bounds must ascend
+                    [dict(max_tri=10, build_path=2)], [dict(max_tri=10, sort_radix=9)],
+                    [dict(max_tri=10, topo_threads=64)], [dict(max_tri=k + 1) for k in range(9)]):
+            with pytest.raises(_native.DelMshError):
+                _native.set_build_classes(bad)
+            assert _native.get_build_classes() == good  # a rejected table changes nothing
+        _native.set_build_classes([])
+        assert _native.get_build_classes() == []
+    finally:
+        _native.set_build_classes(before)
 
 
 def test_apply_ignores_foreign_table(tmp_path):
@@ -79,6 +102,61 @@ def test_every_tuning_choice_matches_oracle(cuda, oracle):
             p2t, tt = Pix2Tri.by_raycasting(d_tri, d_vtx, bvh, aabb, m_row, (200, 150), return_depth=True)
             assert np.array_equal(to_np(p2t, torch), r_p2t), mins
             assert np.array_equal(bits(to_np(tt, torch)), bits(r_tt)), mins
+    finally:
+        _native.set_tuning(**before)
+    assert _native.device_status(clear=True) == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mesh", ["torus", "soup", "small"])
+def test_every_build_choice_matches_oracle(cuda, oracle, mesh):
+    """Every single-mesh build choice of the size classes (cooperative front
+    or separate kernels, 8- or 10-bit digits, topology block size) builds the
+    oracle's tree and boxes."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.autotune import BUILD_CHOICES
+    from del_msh_gb300.TriMesh3 import torch as TriMesh3
+    if mesh == "torus":
+        tri, vtx = W.displaced_torus(400, seed=12)  # 320k triangles
+    elif mesh == "soup":
+        tri, vtx = W.clustered_soup(120_000, num_cluster=5, seed=13)
+    else:
+        tri, vtx = W.jittered_icosphere(2, seed=14)
+    ref = oracle.build(tri, vtx)
+    d_tri, d_vtx = to_dev(tri, torch), to_dev(vtx, torch)
+    before = _native.get_build_classes()
+    try:
+        for c in BUILD_CHOICES:
+            _native.set_build_classes([dict(max_tri=0xFFFFFFFF, **c)])
+            bvh, aabb = TriMesh3.make_bvhnodes_bvhnode2aabb(d_tri, d_vtx)
+            assert np.array_equal(to_np(bvh, torch), ref["bvhnodes"]), c
+            assert np.array_equal(bits(to_np(aabb, torch)), bits(ref["bvhnode2aabb"])), c
+    finally:
+        _native.set_build_classes(before)
+    assert _native.device_status(clear=True) == 0
+
+
+@pytest.mark.gpu
+def test_every_batch_choice_matches_oracle(cuda, oracle):
+    """Every batched build choice (on chip with the fewest or more blocks per
+    large mesh, or the global sort) builds every mesh's oracle tree and boxes."""
+    torch = cuda
+    from del_msh_gb300 import _native
+    from del_msh_gb300.autotune import BATCH_CHOICES
+    from del_msh_gb300.batch import MeshBatch
+    meshes = W.ragged_batch(num_mesh=30, tmin=64, tmax=30000, seed=15)
+    refs = [oracle.build(t, v) for t, v in meshes]
+    b = MeshBatch(meshes)
+    before = _native.get_tuning()
+    try:
+        for c in BATCH_CHOICES:
+            _native.set_tuning(**dict(before, **c))
+            b.build()
+            for m, r in enumerate(refs):
+                bvh, aabb = b.mesh_tree(m)
+                assert np.array_equal(to_np(bvh, torch), r["bvhnodes"]), (c, m)
+                assert np.array_equal(bits(to_np(aabb, torch)), bits(r["bvhnode2aabb"])), (c, m)
     finally:
         _native.set_tuning(**before)
     assert _native.device_status(clear=True) == 0
