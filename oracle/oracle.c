@@ -468,6 +468,8 @@ typedef struct {
   float org[3], dir[3], inv[3];
   uint64_t* n_branch; /* optional work counters (or_pix2tri_work); NULL when not counting */
   uint64_t* n_leaf;
+  uint64_t* n_depth; /* optional: branches entered per depth (the root is depth 0), last bin = deeper */
+  uint32_t depth, max_depth;
 } RayCtx;
 
 static void ray_ctx_init(RayCtx* c, const float org[3], const float dir[3]) {
@@ -508,6 +510,7 @@ static int first_hit(const RayCtx* c, uint32_t node, float dis, float* t_out, ui
   }
   const uint32_t l = bn[node * 3 + 1], r = bn[node * 3 + 2];
   if (c->n_branch) ++*c->n_branch;
+  if (c->n_depth) ++c->n_depth[c->depth < c->max_depth ? c->depth : c->max_depth - 1];
   float tl0 = 0, tl1 = 0, tr0 = 0, tr1 = 0;
   const int hl = slab(c, l, &tl0, &tl1), hr = slab(c, r, &tr0, &tr1);
   int near_is_left;
@@ -517,7 +520,9 @@ static int first_hit(const RayCtx* c, uint32_t node, float dis, float* t_out, ui
   const uint32_t nn = near_is_left ? l : r, nf = near_is_left ? r : l;
   float tn = 0, tf = 0;
   uint32_t in = 0, iff = 0;
+  ((RayCtx*)c)->depth++;
   const int hn = first_hit(c, nn, dis, &tn, &in);
+  ((RayCtx*)c)->depth--;
   if (hn) {
     float f0, f1;
     if (slab(c, nf, &f0, &f1)) {
@@ -532,7 +537,9 @@ static int first_hit(const RayCtx* c, uint32_t node, float dis, float* t_out, ui
       return 1;
     }
   }
+  ((RayCtx*)c)->depth++;
   const int hf = first_hit(c, nf, dis, &tf, &iff);
+  ((RayCtx*)c)->depth--;
   if (hn && hf) {
     if (tn < tf) {
       *t_out = tn;
@@ -680,13 +687,24 @@ void or_cast_rays(uint32_t num_ray, const float* ray_org, const float* ray_dir, 
  * decisions, so these are its node visits and triangle tests too. */
 void or_pix2tri_work(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], const uint32_t* tri2vtx,
                      const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb, uint64_t out[3]) {
+  or_pix2tri_work_depth(img_w, img_h, t_ndc2world, tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, out, NULL, 0);
+}
+
+/* or_pix2tri_work, with the branches entered also counted per depth into
+ * by_depth[0 .. max_depth-1] (the last bin takes every deeper entry). */
+void or_pix2tri_work_depth(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], const uint32_t* tri2vtx,
+                           const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb, uint64_t out[3],
+                           uint64_t* by_depth, uint32_t max_depth) {
   uint64_t n_branch = 0, n_leaf = 0;
+  if (by_depth)
+    for (uint32_t k = 0; k < max_depth; ++k) by_depth[k] = 0;
   const uint32_t num = img_w * img_h;
   for (uint32_t i = 0; i < num; ++i) {
     float org[3], dir[3], t;
     uint32_t it;
     or_ray_for_pixel(i, img_w, img_h, t_ndc2world, org, dir);
-    RayCtx c = {tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, {0}, {0}, {0}, &n_branch, &n_leaf};
+    RayCtx c = {tri2vtx, vtx2xyz, bvhnodes, bvhnode2aabb, {0}, {0}, {0}, &n_branch, &n_leaf,
+                by_depth && max_depth ? by_depth : NULL, 0, max_depth};
     ray_ctx_init(&c, org, dir);
     first_hit(&c, 0, INFINITY, &t, &it);
   }

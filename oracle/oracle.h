@@ -125,6 +125,9 @@ int or_check_morton_code_range_split(const uint32_t* idx2morton, uint32_t n);
  * triangles tested */
 void or_pix2tri_work(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], const uint32_t* tri2vtx,
                      const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb, uint64_t out[3]);
+void or_pix2tri_work_depth(uint32_t img_w, uint32_t img_h, const float t_ndc2world[16], const uint32_t* tri2vtx,
+                           const float* vtx2xyz, const uint32_t* bvhnodes, const float* bvhnode2aabb, uint64_t out[3],
+                           uint64_t* by_depth, uint32_t max_depth);
 
 /* consumers of a pix2tri image (pix2depth.rs:107-146, pix2tri.rs:176-304) */
 int or_mat4_inverse_pivot(const float m[16], float inv[16]);

@@ -81,6 +81,10 @@ def lib():
                                          _f32p]
         L.or_pix2tri_work.argtypes = [u32, u32, _f32p, _u32p, _f32p, _u32p, _f32p,
                                       np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")]
+        L.or_pix2tri_work_depth.restype = None
+        L.or_pix2tri_work_depth.argtypes = [u32, u32, _f32p, _u32p, _f32p, _u32p, _f32p,
+                                            np.ctypeslib.ndpointer(np.uint64, flags="C"),
+                                            np.ctypeslib.ndpointer(np.uint64, flags="C"), u32]
         _lib = L
     return _lib
 
@@ -216,6 +220,18 @@ def pix2tri_work(tri2vtx, vtx2xyz, bvhnodes, aabb, t_ndc2world_colmajor, img_w, 
                           _c(tri2vtx, np.uint32).reshape(-1), _c(vtx2xyz, np.float32).reshape(-1),
                           _c(bvhnodes, np.uint32).reshape(-1), _c(aabb, np.float32).reshape(-1), out)
     return {"rays": int(out[0]), "branches": int(out[1]), "tri_tests": int(out[2])}
+
+
+def pix2tri_work_depth(tri2vtx, vtx2xyz, bvhnodes, aabb, t_ndc2world_colmajor, img_w, img_h, max_depth=64):
+    """pix2tri_work's counts and the branches entered per tree depth (root 0;
+    the last bin takes every deeper entry)."""
+    out = np.zeros(3, np.uint64)
+    hist = np.zeros(max_depth, np.uint64)
+    lib().or_pix2tri_work_depth(img_w, img_h, _c(t_ndc2world_colmajor, np.float32).reshape(-1),
+                                _c(tri2vtx, np.uint32).reshape(-1), _c(vtx2xyz, np.float32).reshape(-1),
+                                _c(bvhnodes, np.uint32).reshape(-1), _c(aabb, np.float32).reshape(-1), out, hist,
+                                max_depth)
+    return out, hist
 
 
 def cast_rays(ray_org, ray_dir, tri2vtx, vtx2xyz, bvhnodes, aabb, threads=None):
