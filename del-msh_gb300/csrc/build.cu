@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
                                                    uint32_t* height_out, uint32_t* status, const uint32_t* gate) {
   // gated (drop-in refit): runs only when the tree was found not to be in
   // Karras leaf order, so that the range queries could not do the call
-  if (gate != nullptr && (*reinterpret_cast<const volatile uint32_t*>(gate) & kRefitPlainClimb) == 0u) return;
+  if (gate != nullptr && (block_read_hdr(gate, nullptr).x & kRefitPlainClimb) == 0u) return;
   const uint32_t ii = blockIdx.x * kThreads + threadIdx.x;
   if (ii >= num_tri) return;
   const uint32_t num_node = 2 * num_tri - 1;
@@ -1348,86 +1348,66 @@ void launch_refit(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, co
 
 // ------------------------------------------- refit of a tree given as bvhnodes
 // The drop-in refit gets a tree and nothing else.  The range queries need
-// each branch's leaf range; in a Karras tree a branch's index is one end of
-// its range, and the other end is found from the records alone: a branch
-// that is its parent's left child is the right end of its range, whose left
-// end is the leaf at the bottom of its left spine (left child, left child,
-// ...); a right child is the left end, and the right end ends its right
-// spine.  k_refit_derive_ends walks that spine (at most kSpineWalk records);
-// k_refit_check_ends then checks that every branch's two children split its
-// range exactly, [lo, m] and [m+1, hi], and that the root spans every leaf.
-// By induction from the leaves every range is then the subtree's leaf
-// interval, so the range queries give the climb's boxes.  Anything else (a
-// tree not in Karras leaf order, malformed records, or a spine longer than
-// the walk) sets kRefitPlainClimb in the refit header: the range-query
-// kernels exit at once and the parent-pointer climb k_refit does the call.
+// each branch's leaf range.  k_refit_ends finds, for branch i with children
+// c0, c1 and with bounded walks (at most kSpineWalk records each, all four
+// walked together), lo(i) at the bottom of i's left spine (left child, left
+// child, ...), hi(i) at the bottom of its right spine, hi(c0) at the bottom of
+// c0's right spine and lo(c1) at the bottom of c1's left spine (a leaf child
+// is its own position), and checks that
+//   - hi(c0) + 1 == lo(c1): the children's leaf runs meet;
+//   - i is lo(i) or hi(i): a branch index is one end of its range (the
+//     property the window refit uses), and other_end[i] is the other end;
+//   - both children name i as their parent, and the root spans 0 .. T-1.
+// By induction from the leaves every subtree's leaves then form the run
+// [lo, hi] in order (lo(c0) = lo(i) and hi(c1) = hi(i) hold by construction),
+// so the range queries give the climb's boxes.  Anything else (a tree not in
+// Karras leaf order, malformed records, or a spine longer than the walk) sets
+// kRefitPlainClimb in the refit header: the range-query kernels exit at once
+// and the parent-pointer climb k_refit does the call.
 constexpr uint32_t kSpineWalk = 64;
 
-__global__ void __launch_bounds__(kThreads) k_refit_derive_ends(uint32_t num_tri, const uint32_t* __restrict__ bn,
-                                                                uint32_t* __restrict__ other_end, uint32_t* hdr) {
+__global__ void __launch_bounds__(kThreads) k_refit_ends(uint32_t num_tri, const uint32_t* __restrict__ bn,
+                                                         uint32_t* __restrict__ other_end, uint32_t* hdr) {
   const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
   const uint32_t nb = num_tri - 1, num_node = 2 * num_tri - 1;
   if (i >= nb) return;
   const uint32_t p = __ldg(bn + 3ull * i), c0 = __ldg(bn + 3ull * i + 1), c1 = __ldg(bn + 3ull * i + 2);
   bool bad = c0 >= num_node || c1 >= num_node;
-  uint32_t oe = i;
+  uint32_t lo = 0, hi = 0;
   if (!bad) {
-    const uint32_t k0 = c0 >= nb ? c0 - nb : c0, k1 = c1 >= nb ? c1 - nb : c1;
-    bad = k1 != k0 + 1 || __ldg(bn + 3ull * c0) != i || __ldg(bn + 3ull * c1) != i;
-  }
-  if (!bad) {
-    if (i == 0) {
-      bad = p != kUMax;
-      oe = nb;  // the root spans leaves 0 .. T-1
-    } else if (p >= nb) {
+    // four walks at once: x[0] left spine of i (from c0), x[1] right spine of
+    // i (from c1), x[2] right spine of c0, x[3] left spine of c1
+    uint32_t x[4] = {c0, c1, c0, c1};
+    const uint32_t side[4] = {1u, 2u, 2u, 1u};
+    const bool parents_ok = __ldg(bn + 3ull * c0) == i && __ldg(bn + 3ull * c1) == i;
+    for (uint32_t step = 0; step < kSpineWalk; ++step) {
+      bool more = false;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (x[k] < nb) {
+          x[k] = __ldg(bn + 3ull * x[k] + side[k]);
+          more = true;
+        }
+      }
+      if (!more) break;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+        if (x[k] >= num_node) x[k] = kUMax - 1;  // a bad index: stops the walk, fails below
+    }
+    bool leaves = true;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) leaves = leaves && x[k] >= nb && x[k] < num_node;
+    if (!leaves || !parents_ok) {
       bad = true;
     } else {
-      const uint32_t pl = __ldg(bn + 3ull * p + 1), pr = __ldg(bn + 3ull * p + 2);
-      const int side = pl == i ? 1 : (pr == i ? 2 : 0);  // the spine to walk: left (1) or right (2)
-      if (side == 0) {
-        bad = true;
-      } else {
-        uint32_t x = side == 1 ? c0 : c1, steps = 0;
-        while (x < nb && steps < kSpineWalk) {
-          x = __ldg(bn + 3ull * x + side);
-          ++steps;
-        }
-        if (x < nb || x >= num_node) bad = true;  // spine too long, or a bad index
-        else oe = x - nb;
-      }
+      lo = x[0] - nb;
+      hi = x[1] - nb;
+      bad = (x[2] - nb) + 1 != x[3] - nb || (i != lo && i != hi) || lo >= hi;
+      if (i == 0) bad = bad || p != kUMax || lo != 0 || hi != nb;
     }
   }
-  other_end[i] = bad ? i : oe;
+  other_end[i] = bad ? i : (i == lo ? hi : lo);
   if (bad) atomicOr(hdr + 1, kRefitPlainClimb);
-}
-
-__global__ void __launch_bounds__(kThreads) k_refit_check_ends(uint32_t num_tri, const uint32_t* __restrict__ bn,
-                                                               const uint32_t* __restrict__ other_end, uint32_t* hdr) {
-  const uint32_t i = blockIdx.x * kThreads + threadIdx.x;
-  const uint32_t nb = num_tri - 1, num_node = 2 * num_tri - 1;
-  if (i >= nb) return;
-  if (*reinterpret_cast<const volatile uint32_t*>(hdr + 1) & kRefitPlainClimb) return;
-  const uint32_t c0 = __ldg(bn + 3ull * i + 1), c1 = __ldg(bn + 3ull * i + 2);
-  if (c0 >= num_node || c1 >= num_node) {  // already flagged by the derivation
-    atomicOr(hdr + 1, kRefitPlainClimb);
-    return;
-  }
-  const auto range = [&](uint32_t c, uint32_t& lo, uint32_t& hi) {
-    if (c >= nb) {
-      lo = hi = c - nb;
-    } else {
-      const uint32_t o = __ldg(other_end + c);
-      lo = c < o ? c : o;
-      hi = c < o ? o : c;
-    }
-  };
-  uint32_t lo, hi, lo0, hi0, lo1, hi1;
-  range(i, lo, hi);
-  range(c0, lo0, hi0);
-  range(c1, lo1, hi1);
-  bool ok = lo0 == lo && hi0 + 1 == lo1 && hi1 == hi && hi < num_tri;
-  if (i == 0) ok = ok && lo == 0 && hi == nb;
-  if (!ok) atomicOr(hdr + 1, kRefitPlainClimb);
 }
 
 void launch_refit_any_tree(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,
@@ -1441,8 +1421,7 @@ void launch_refit_any_tree(cudaStream_t s, uint32_t num_tri, const uint32_t* bvh
   uint32_t* hdr = flags + refit_queue_offset(num_tri);
   cudaMemsetAsync(hdr, 0, kRefitQueueHdr * sizeof(uint32_t), s);
   const uint32_t grid = (num_tri - 1 + kThreads - 1) / kThreads;
-  k_refit_derive_ends<<<grid, kThreads, 0, s>>>(num_tri, bvhnodes, other_end, hdr);
-  k_refit_check_ends<<<grid, kThreads, 0, s>>>(num_tri, bvhnodes, other_end, hdr);
+  k_refit_ends<<<grid, kThreads, 0, s>>>(num_tri, bvhnodes, other_end, hdr);
   launch_refit_windowed(s, num_tri, Segments{}, num_vtx, bvhnodes, other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb,
                         flags, nullptr, status, nullptr, /*header_ready=*/true);
   launch_refit(s, num_tri, bvhnodes, tri2vtx, num_vtx, vtx2xyz0, vtx2xyz1, aabb, flags, nullptr, status, hdr + 1);
