@@ -320,16 +320,10 @@ __device__ __forceinline__ Box leaf_box(const uint32_t* __restrict__ tri2vtx, ui
 // box (stored just before) and, for the second arriver, makes the sibling's
 // box visible, without a full memory fence per level.  The climbing thread
 // keeps its own child's box in registers and loads only the sibling's.
-__global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint32_t* __restrict__ bvhnodes,
-                                                   const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
-                                                   const float* __restrict__ vtx2xyz0,
-                                                   const float* __restrict__ vtx2xyz1, float* aabb, uint32_t* flags,
-                                                   uint32_t* height_out, uint32_t* status, const uint32_t* gate) {
-  // gated (drop-in refit): runs only when the tree was found not to be in
-  // Karras leaf order, so that the range queries could not do the call
-  if (gate != nullptr && (block_read_hdr(gate, nullptr).x & kRefitPlainClimb) == 0u) return;
-  const uint32_t ii = blockIdx.x * kThreads + threadIdx.x;
-  if (ii >= num_tri) return;
+__device__ __forceinline__ void refit_climb(uint32_t ii, uint32_t num_tri, const uint32_t* __restrict__ bvhnodes,
+                                            const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
+                                            const float* __restrict__ vtx2xyz0, const float* __restrict__ vtx2xyz1,
+                                            float* aabb, uint32_t* flags, uint32_t* height_out, uint32_t* status) {
   const uint32_t num_node = 2 * num_tri - 1;
   const uint32_t leaf = num_tri - 1 + ii;
   const uint32_t it = __ldg(bvhnodes + static_cast<size_t>(leaf) * 3 + 1);
@@ -370,6 +364,20 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
     node = parent;
   }
   if (height_out) *height_out = h;
+}
+
+// Grid-stride over the leaves (a leaf's climb never waits, so a thread may
+// take several).
+__global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint32_t* __restrict__ bvhnodes,
+                                                   const uint32_t* __restrict__ tri2vtx, uint32_t num_vtx,
+                                                   const float* __restrict__ vtx2xyz0,
+                                                   const float* __restrict__ vtx2xyz1, float* aabb, uint32_t* flags,
+                                                   uint32_t* height_out, uint32_t* status, const uint32_t* gate) {
+  // gated (drop-in refit): runs only when the tree was found not to be in
+  // Karras leaf order, so that the range queries could not do the call
+  if (gate != nullptr && (block_read_hdr(gate, nullptr).x & kRefitPlainClimb) == 0u) return;
+  for (uint32_t ii = blockIdx.x * kThreads + threadIdx.x; ii < num_tri; ii += gridDim.x * kThreads)
+    refit_climb(ii, num_tri, bvhnodes, tri2vtx, num_vtx, vtx2xyz0, vtx2xyz1, aabb, flags, height_out, status);
 }
 
 // Tree-order refit, in two kernels: the path taken when a leaf box holds NaN
@@ -1341,7 +1349,10 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
 void launch_refit(cudaStream_t s, uint32_t num_tri, const uint32_t* bvhnodes, const uint32_t* tri2vtx,
                   uint32_t num_vtx, const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
                   uint32_t* height_out, uint32_t* status, const uint32_t* gate) {
-  const uint32_t grid = (num_tri + kThreads - 1) / kThreads;
+  uint32_t grid = (num_tri + kThreads - 1) / kThreads;
+  // gated, it usually exits at once: a grid of a few blocks per SM costs
+  // less to launch than one thread per leaf
+  if (gate != nullptr && grid > 152u * 8u) grid = 152u * 8u;
   k_refit<<<grid, kThreads, 0, s>>>(num_tri, bvhnodes, tri2vtx, num_vtx, vtx2xyz0, vtx2xyz1, aabb, flags, height_out,
                                     status, gate);
 }
