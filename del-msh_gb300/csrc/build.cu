@@ -807,7 +807,8 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
                                                               const float* __restrict__ vtx0_all,
                                                               const float* __restrict__ vtx1_all, float* aabb_all,
                                                               uint32_t* hdr, uint32_t* cross_list, float* wseg,
-                                                              uint32_t* status, const float* __restrict__ tribox) {
+                                                              uint32_t* status, const float* __restrict__ tribox,
+                                                              const uint32_t* __restrict__ leaf_tri) {
   __shared__ Box tree[2 * kRefitWindow];
   __shared__ uint32_t s_mesh, s_flag;
   const uint32_t wA = blockIdx.x * kRefitWindow;
@@ -837,7 +838,10 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
     oth[r] = kUMax;
     if (!lm[r].ok) continue;
     const uint32_t n = g - lm[r].t0;
-    tri[r] = __ldg(bvhnodes_all + 3 * (2ull * lm[r].t0 - lm[r].m + lm[r].T - 1 + n) + 1);
+    // the leaf's triangle: from the sorted indices when given (contiguous),
+    // else from its record (12-byte stride)
+    tri[r] = (!kBatch && leaf_tri) ? __ldg(leaf_tri + g)
+                                   : __ldg(bvhnodes_all + 3 * (2ull * lm[r].t0 - lm[r].m + lm[r].T - 1 + n) + 1);
     if (n + 1 < lm[r].T) oth[r] = __ldg(other_all + (static_cast<size_t>(lm[r].t0) - lm[r].m) + n);
   }
   bool nan = false;
@@ -1280,7 +1284,8 @@ void launch_topology(cudaStream_t s, uint32_t n, const uint32_t* idx2morton, con
 void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
                            const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
                            const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
-                           uint32_t* height_out, uint32_t* status, const float* tribox, bool header_ready) {
+                           uint32_t* height_out, uint32_t* status, const float* tribox, bool header_ready,
+                           const uint32_t* leaf_tri) {
   if (total_tri == 0) return;
   if (seg.tri_off || vtx2xyz1) tribox = nullptr;  // one mesh, one vertex state only
   const int smem = static_cast<int>(sizeof(WinSmem));
@@ -1320,7 +1325,7 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   if (seg.tri_off) {
     k_refit_seg_win<true><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
                                                           vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg, status,
-                                                          nullptr);
+                                                          nullptr, nullptr);
     launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
     launch_pdl(k_refit_seg_cross_groups<true>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb,
                queue, flags, v, cross_groups, status);
@@ -1333,7 +1338,7 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   } else {
     k_refit_seg_win<false><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end,
                                                            tri2vtx, vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg,
-                                                           status, tribox);
+                                                           status, tribox, leaf_tri);
     launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
     launch_pdl(k_refit_seg_cross_groups<false>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb,
                queue, flags, v, cross_groups, status);

@@ -277,7 +277,7 @@ int build_impl(uint64_t stream_ptr, uint32_t T, const uint32_t* tri2vtx, uint32_
   if (ev) DM_CUDA(cudaEventRecord(ev[3], s));
   // the height is only computed on request: it needs the tree-order climb
   dm::launch_refit_windowed(s, T, dm::Segments{1, nullptr, nullptr}, num_vtx, bvhnodes, other_end, tri2vtx, vtx2xyz,
-                            nullptr, aabb, flags, height_out ? height : nullptr, status, tribox);
+                            nullptr, aabb, flags, height_out ? height : nullptr, status, tribox, false, ov);
   if (ev) DM_CUDA(cudaEventRecord(ev[4], s));
   if (transform_out) DM_CUDA(cudaMemcpyAsync(transform_out, transform, 64, cudaMemcpyDeviceToDevice, s));
   if (height_out) DM_CUDA(cudaMemcpyAsync(height_out, height, 4, cudaMemcpyDeviceToDevice, s));

@@ -113,12 +113,14 @@ inline size_t refit_seg_words(uint32_t total_tri) {
 inline size_t refit_flags_words(uint32_t total_tri) { return refit_seg_offset(total_tri) + refit_seg_words(total_tri); }
 // tribox (optional, one mesh and vtx2xyz1 == nullptr only): each triangle's
 // box, 6 floats in triangle order, as launch_centroid_aabb stores them; the
-// leaf boxes are then read instead of gathered from the vertices.
+// leaf boxes are then read instead of gathered from the vertices.  leaf_tri
+// (optional, one mesh): the triangle of each leaf position (the sort's
+// values), read instead of the leaf records.
 void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& seg, uint32_t num_vtx_single,
                            const uint32_t* bvhnodes, const uint32_t* other_end, const uint32_t* tri2vtx,
                            const float* vtx2xyz0, const float* vtx2xyz1, float* aabb, uint32_t* flags,
                            uint32_t* height_out, uint32_t* status, const float* tribox = nullptr,
-                           bool header_ready = false);
+                           bool header_ready = false, const uint32_t* leaf_tri = nullptr);
 // Refit of any tree given as bvhnodes (the drop-in refit): derives every
 // branch's other range end on the device and runs the range-query refit when
 // the tree is in Karras leaf order, else the parent-pointer climb; the choice
