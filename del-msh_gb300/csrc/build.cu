@@ -408,10 +408,11 @@ __global__ void __launch_bounds__(kThreads) k_refit(uint32_t num_tri, const uint
 // the chain upward, box(j) = from_two(leaf j, box(j+1)).  In k_refit_top the
 // fold prefetches eight links at a time (their records and leaf boxes sit at
 // consecutive addresses).  Values and merge order are those of k_refit.
-constexpr int kWinThreads = 256;
+constexpr int kWinThreads = 512;
 constexpr int kWinPerThread = kRefitWindow / kWinThreads;
 constexpr int kFoldDepth = 8;
 static_assert(kWinPerThread * kWinThreads == kRefitWindow, "window");
+static_assert(kWinThreads >= kRefitWinHeap, "a thread per stored window-heap node");
 
 // The records and other ends of branches wA..wA+kRefitWindow-1 (every local
 // branch has its index in the window) are loaded into shared memory once.
@@ -742,12 +743,12 @@ __global__ void __launch_bounds__(128) k_refit_top(uint32_t total_tri, Segments 
 // leftmost extreme of the leaves below.  So branch i's box equals the fold of
 // the leaf boxes over its leaf range [min(i, other_end[i]), max(...)], which a
 // segment tree over the sorted leaf boxes answers with no climb at all.
-// The tree is a perfect binary heap per 512-leaf window (nodes of 8..512
-// leaves kept), per 64-window superblock and over the superblocks; only nodes
+// The tree is a perfect binary heap per kRefitWindow-leaf window (nodes of 8
+// leaves and up kept), per 64-window superblock and over the superblocks; only nodes
 // lying wholly inside [0, total_tri) are ever built or read.  Identity boxes
 // are (+inf, -inf), which box_union returns unchanged bit for bit.
 struct SegView {
-  const float* wseg;  // [window][128] boxes, heap index 1..127
+  const float* wseg;  // [window][kRefitWinHeap] boxes, heap index 1..kRefitWinHeap - 1
   const float* sseg;  // [superblock][64] boxes, heap index 1..63
   const float* tseg;  // [2 << top_log] boxes, heap index 1..
   uint32_t top_log;
@@ -756,7 +757,7 @@ struct SegView {
 __device__ __forceinline__ const float* seg_node(const SegView& v, uint32_t lvl, uint32_t j) {
   if (lvl <= kRefitWindowLog) {
     const uint32_t sh = kRefitWindowLog - lvl;
-    return v.wseg + 6 * (static_cast<size_t>(j >> sh) * 128 + (1u << sh) + (j & ((1u << sh) - 1)));
+    return v.wseg + 6 * (static_cast<size_t>(j >> sh) * kRefitWinHeap + (1u << sh) + (j & ((1u << sh) - 1)));
   }
   if (lvl <= kRefitSuperLog) {
     const uint32_t sh = kRefitSuperLog - lvl;
@@ -796,6 +797,8 @@ __device__ __forceinline__ uint32_t mesh_from(const Segments& seg, uint32_t m0, 
   return m;
 }
 
+constexpr int kSegWinSmem = static_cast<int>(2 * kRefitWindow * sizeof(Box));
+
 // Window kernel: leaf boxes, the window heap, and every branch whose range
 // lies inside the window.
 template <bool kBatch>
@@ -809,7 +812,8 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
                                                               uint32_t* hdr, uint32_t* cross_list, float* wseg,
                                                               uint32_t* status, const float* __restrict__ tribox,
                                                               const uint32_t* __restrict__ leaf_tri) {
-  __shared__ Box tree[2 * kRefitWindow];
+  extern __shared__ __align__(16) unsigned char seg_raw[];
+  Box* tree = reinterpret_cast<Box*>(seg_raw);  // 2 * kRefitWindow boxes
   __shared__ uint32_t s_mesh, s_flag;
   const uint32_t wA = blockIdx.x * kRefitWindow;
   if (threadIdx.x == 0) {
@@ -885,11 +889,11 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
     }
   }
   __syncthreads();
-  // heap nodes of 8..512 leaves for the crossing queries
-  if (threadIdx.x >= 1 && threadIdx.x < 128) {
+  // heap nodes of 8 leaves and up for the crossing queries
+  if (threadIdx.x >= 1 && threadIdx.x < kRefitWinHeap) {
     uint32_t lvl, j;
     heap_node(threadIdx.x, kRefitWindowLog, lvl, j);
-    if (node_inside(wA, lvl, j, total_tri)) box_store(wseg + 6 * (static_cast<size_t>(blockIdx.x) * 128 + threadIdx.x), tree[threadIdx.x]);
+    if (node_inside(wA, lvl, j, total_tri)) box_store(wseg + 6 * (static_cast<size_t>(blockIdx.x) * kRefitWinHeap + threadIdx.x), tree[threadIdx.x]);
   }
 #pragma unroll
   for (int r = 0; r < kWinPerThread; ++r) {
@@ -936,7 +940,7 @@ __global__ void __launch_bounds__(256) k_refit_seg_super(uint32_t total_tri, uin
   if (threadIdx.x < kRefitSuper) {
     const uint32_t w = sb * kRefitSuper + threadIdx.x;
     t[kRefitSuper + threadIdx.x] = (static_cast<uint64_t>(w + 1) << kRefitWindowLog) <= total_tri
-                                       ? box_load_cg(wseg + 6 * (static_cast<size_t>(w) * 128 + 1))
+                                       ? box_load_cg(wseg + 6 * (static_cast<size_t>(w) * kRefitWinHeap + 1))
                                        : box_identity();
   }
   __syncthreads();
@@ -1294,7 +1298,8 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   const uint32_t capacity = refit_queue_capacity(total_tri);
   uint32_t* queue = flags + refit_queue_offset(total_tri);  // also the header: count, climb flag, ticket
   float* segbase = reinterpret_cast<float*>(flags + refit_seg_offset(total_tri));
-  SegView v{segbase, segbase + 6 * size_t{128} * windows, segbase + 6 * (size_t{128} * windows + size_t{64} * supers),
+  SegView v{segbase, segbase + 6 * size_t{kRefitWinHeap} * windows,
+            segbase + 6 * (size_t{kRefitWinHeap} * windows + size_t{64} * supers),
             top_log};
   // the attribute is per device; set it once so that later calls (possibly
   // under stream capture) make no further runtime configuration calls
@@ -1305,6 +1310,8 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   if (dev >= 0 && dev < 64 && !configured[dev]) {
     cudaFuncSetAttribute(k_refit_win<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_refit_win<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaFuncSetAttribute(k_refit_seg_win<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSegWinSmem);
+    cudaFuncSetAttribute(k_refit_seg_win<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSegWinSmem);
     cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
     configured[dev] = true;
   }
@@ -1323,7 +1330,7 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   float* sseg = const_cast<float*>(v.sseg);
   float* tseg = const_cast<float*>(v.tseg);
   if (seg.tri_off) {
-    k_refit_seg_win<true><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
+    k_refit_seg_win<true><<<windows, kWinThreads, kSegWinSmem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
                                                           vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg, status,
                                                           nullptr, nullptr);
     launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
@@ -1336,7 +1343,7 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
     launch_pdl(k_refit_top<true>, dim3(top_grid), dim3(128), 0, s, total_tri, seg, bvhnodes, aabb, flags, queue,
                capacity, height_out, status);
   } else {
-    k_refit_seg_win<false><<<windows, kWinThreads, 0, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end,
+    k_refit_seg_win<false><<<windows, kWinThreads, kSegWinSmem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end,
                                                            tri2vtx, vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg,
                                                            status, tribox, leaf_tri);
     launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);

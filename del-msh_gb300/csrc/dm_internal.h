@@ -82,10 +82,11 @@ struct Segments {
 // arrival counters, zero on entry and left zero; the rest (queue, segment
 // tree) needs no initialisation.  height_out (optional) receives one height
 // per mesh.
-constexpr uint32_t kRefitWindow = 512;      // leaves per window (a power of two)
-constexpr uint32_t kRefitWindowLog = 9;
-constexpr uint32_t kRefitSuper = 64;        // windows per superblock
-constexpr uint32_t kRefitSuperLog = 15;     // log2(kRefitWindow * kRefitSuper)
+constexpr uint32_t kRefitWindowLog = 10;
+constexpr uint32_t kRefitWindow = 1u << kRefitWindowLog;  // leaves per window
+constexpr uint32_t kRefitWinHeap = kRefitWindow / 4;      // stored window heap: nodes of 8.. leaves, index 1..
+constexpr uint32_t kRefitSuper = 64;                      // windows per superblock
+constexpr uint32_t kRefitSuperLog = kRefitWindowLog + 6;  // log2(kRefitWindow * kRefitSuper)
 constexpr uint32_t kRefitQueueHdr = 4;      // queue count, climb flag, ticket, spare
 // climb-flag bit: the tree is not in Karras leaf order (or could not be
 // shown to be), so the parent-pointer climb does the refit; bit 0 hands the
@@ -105,9 +106,9 @@ inline size_t refit_queue_offset(uint32_t total_tri) { return (static_cast<size_
 inline size_t refit_seg_offset(uint32_t total_tri) {
   return refit_queue_offset(total_tri) + kRefitQueueHdr + 4 * static_cast<size_t>(refit_queue_capacity(total_tri));
 }
-// window heaps (128 boxes each), superblock heaps (64 each), top heap (2 * 2^top_log)
+// window heaps (kRefitWinHeap boxes each), superblock heaps (64 each), top heap (2 * 2^top_log)
 inline size_t refit_seg_words(uint32_t total_tri) {
-  return 6 * (size_t{128} * refit_num_windows(total_tri) + size_t{64} * refit_num_super(total_tri) +
+  return 6 * (size_t{kRefitWinHeap} * refit_num_windows(total_tri) + size_t{64} * refit_num_super(total_tri) +
               (size_t{2} << refit_top_log(total_tri)));
 }
 inline size_t refit_flags_words(uint32_t total_tri) { return refit_seg_offset(total_tri) + refit_seg_words(total_tri); }
