@@ -874,8 +874,8 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
     if (threadIdx.x == 0) atomicOr(hdr + 1, 1u);  // hand the whole call to the climb
     return;
   }
-  // heap levels of 64..256 nodes by the block, the 5 top levels (32..1
-  // nodes) by warp 0 alone
+  // heap levels of 64 .. kRefitWindow / 2 nodes by the block, the top six
+  // levels (32 .. 1 nodes) by warp 0 alone
 #pragma unroll 1
   for (uint32_t half = kRefitWindow / 2; half > 32; half >>= 1) {
     for (uint32_t h = half + threadIdx.x; h < 2 * half; h += kWinThreads) tree[h] = box_union(tree[2 * h], tree[2 * h + 1]);
