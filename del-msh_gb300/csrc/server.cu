@@ -154,6 +154,11 @@ struct Job {
 
 struct dm_server {
   int device = 0;
+  // resident meshes' blocks come from this pool, which keeps freed memory
+  // (release threshold: never) so that admitting a mesh after an eviction, or
+  // for the first time after a synchronisation, maps no memory; nullptr: the
+  // device's default pool
+  cudaMemPool_t pool = nullptr;
   size_t budget = 0, used = 0, slot_bytes = 0;
   uint32_t max_tri = 0, max_out = 0;
   std::vector<dm::Slot> slots;
@@ -334,7 +339,9 @@ DevMesh* ensure_resident(dm_server* S, uint32_t id, int slot, std::unique_lock<s
   }
   DevMesh& m = S->dev[id];
   if (!m.last) cudaEventCreateWithFlags(&m.last, cudaEventDisableTiming);
-  if (cudaMallocAsync(&m.block, bytes, st) != cudaSuccess) {
+  const cudaError_t ae = S->pool ? cudaMallocFromPoolAsync(&m.block, bytes, S->pool, st)
+                                 : cudaMallocAsync(&m.block, bytes, st);
+  if (ae != cudaSuccess) {
     m.block = nullptr;
     *err = DM_ERR_CUDA;
     return nullptr;
@@ -468,6 +475,19 @@ int dm_server_create(int device, size_t budget_bytes, int num_slots, uint32_t ma
   }
   S->used = S->slot_bytes;
   S->stats.bytes_budget = budget_bytes;
+  {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = device;
+    if (cudaMemPoolCreate(&S->pool, &props) == cudaSuccess) {
+      uint64_t keep = ~uint64_t{0};
+      cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    } else {
+      cudaGetLastError();  // pools unsupported: the default pool
+      S->pool = nullptr;
+    }
+  }
   if (S->slot_bytes > budget_bytes) {
     dm_server_destroy(S);
     return set_error(DM_ERR_INVALID_ARGUMENT, "budget smaller than the slots' own memory");
@@ -608,6 +628,7 @@ int dm_server_destroy(dm_server* S) {
     if (kv.second.block) cudaFree(kv.second.block);
     if (kv.second.last) cudaEventDestroy(kv.second.last);
   }
+  if (S->pool) cudaMemPoolDestroy(S->pool);
   for (auto& sl : S->slots) {
     cudaFree(sl.build_scratch);
     cudaFree(sl.cast_scratch);
