@@ -522,7 +522,7 @@ def t_error_f64(m, img_w, img_h, p2t, tt, tri, vtx):
 
 
 def compact_extras(args):
-    """The other spec workloads, measured after the headline step in the
+    """The other workloads, measured after the headline step in the
     same process and reported as compact keys of the same line: the ragged
     batch (graph replay against the plain per-mesh path), the served stream
     (p50/p99 at 0.5x and 0.8x of the plain path's capacity) and the
@@ -734,7 +734,7 @@ def measure_served(pool: int, requests: int, loads, slots: int, budget_gb: float
 
 
 def run_render(args):
-    """The consumers of the config-2 pix2tri image (1920x1080 over the
+    """The consumers of the torus's pix2tri image (1920x1080 over the
     2,097,152-triangle torus): depth and 3-channel interpolation, forward and
     backward, each timed alone with CUDA events (L2 flushed between
     repetitions), with the oracle on the host cores beside them."""
@@ -793,7 +793,7 @@ def run_render(args):
     status = _native.device_status(clear=True)
     line = {"metric": "pixels/s (depth / interpolation from a 1920x1080 pix2tri image, fwd and bwd)",
             "unit": "pixels/s", "value": res["interp_fwd"]["pixels_per_s"], "steps": args.steps,
-            "config": {"workload": "config-2 torus (2,097,152 tris), 1920x1080 pinhole pix2tri, 3 value channels",
+            "config": {"workload": "displaced torus (2,097,152 tris), 1920x1080 pinhole pix2tri, 3 value channels",
                        "hit_pixels": hits, "l2": "flushed between repetitions"},
             "ops": res, "peak": {"hbm_gbs": peak, "kind": peak_kind}, "device_status": status,
             "note": "backward passes accumulate with atomicAdd, as the reference's kernels do"}
@@ -1048,8 +1048,8 @@ def measure_soup(steps: int, warmup: int, cpu: bool):
 
 def read_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from the committed ncu summary
-    (profiles/ncu_config2.md lines `traffic <kernel> <bytes>`), else None."""
-    p = ROOT / "profiles" / "ncu_config2.md"
+    (profiles/ncu_torus2m_step.md lines `traffic <kernel> <bytes>`), else None."""
+    p = ROOT / "profiles" / "ncu_torus2m_step.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():

@@ -4,7 +4,7 @@
   the reference's OWN code: del-msh-cuda-kernels/cuda/mortons.h and
   bvhnodes_morton.cu compiled as host C++ by oracle/build.py into oracle/_ref
   (needs the reference checkout; run in the container that has it).
-* ``oracle_cfg1.npz`` is the oracle's result for the 1280-triangle jittered
+* ``oracle_icosphere1280_256.npz`` is the oracle's result for the 1280-triangle jittered
   icosphere (build + 256x256 orthographic cast), stored with its inputs so the
   same bits can be checked on any machine.
 * ``ref_assets.npz`` holds the reference's example meshes (asset/bunny_1k.obj,
@@ -127,7 +127,7 @@ def main():
     r = O.build(tri, vtx)
     m = W.ortho_ndc2world()
     p2t, p2tt = O.pix2tri(tri, vtx, r["bvhnodes"], r["bvhnode2aabb"], m, 256, 256)
-    np.savez_compressed(HERE / "oracle_cfg1.npz", tri2vtx=tri, vtx2xyz=vtx, transform=r["transform"],
+    np.savez_compressed(HERE / "oracle_icosphere1280_256.npz", tri2vtx=tri, vtx2xyz=vtx, transform=r["transform"],
                         tri2morton=r["tri2morton"], idx2tri=r["idx2tri"], idx2morton=r["idx2morton"],
                         bvhnodes=r["bvhnodes"], bvhnode2aabb=r["bvhnode2aabb"], ndc2world=m, pix2tri=p2t,
                         pix2t=p2tt)

@@ -165,7 +165,7 @@ def test_batch_build_understated_max_tri(cuda, oracle):
     assert np.array_equal(bits(aabb[0]), bits(root))
 
 
-def test_full_config4_batched(cuda, oracle):
+def test_full_ragged_batch_4096(cuda, oracle):
     """The full ragged batch: 4096 meshes (37.9M triangles, counts realised up
     to 65024, so clusters of four blocks), each with its 64x64 orthographic
     image.  Every mesh's tree, boxes and image equal the oracle's bit for bit."""

@@ -97,9 +97,9 @@ def _compare_build(got, ref, T):
         assert np.array_equal(bits(got[k]), bits(ref[k])), k
 
 
-def test_build_cfg1_matches_golden(cuda, golden_dir):
+def test_build_icosphere1280_matches_golden(cuda, golden_dir):
     torch = cuda
-    g = np.load(golden_dir / "oracle_cfg1.npz")
+    g = np.load(golden_dir / "oracle_icosphere1280_256.npz")
     got = _build_ex(torch, g["tri2vtx"], g["vtx2xyz"])
     _compare_build(got, {k: g[k] for k in g.files}, g["tri2vtx"].shape[0])
     assert _status_clear() == 0

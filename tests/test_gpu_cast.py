@@ -33,9 +33,9 @@ def _status():
     return _native.device_status(clear=True)
 
 
-def test_cast_cfg1_matches_golden(cuda, golden_dir):
+def test_cast_icosphere1280_matches_golden(cuda, golden_dir):
     torch = cuda
-    g = np.load(golden_dir / "oracle_cfg1.npz")
+    g = np.load(golden_dir / "oracle_icosphere1280_256.npz")
     mesh = _dev_mesh(torch, g["tri2vtx"], g["vtx2xyz"])
     p2t, tt = _cast_pixels(torch, mesh, g["ndc2world"], 256, 256)
     assert np.array_equal(p2t, g["pix2tri"])
@@ -160,7 +160,7 @@ def test_t_error_against_f64(cuda, oracle):
     assert worst < 1e-6 * 10  # f32 rounding of the MT formula; reported in the bench
 
 
-def test_full_config2_torus(cuda, oracle):
+def test_full_torus_2m_1080p(cuda, oracle):
     """2,097,152-triangle displaced torus, 1920x1080 pinhole camera: build
     and cast bit-exact to the oracle at full size."""
     torch = cuda
@@ -179,7 +179,7 @@ def test_full_config2_torus(cuda, oracle):
     assert _status() == 0
 
 
-def test_full_config3_soup(cuda, oracle):
+def test_full_clustered_soup_4m(cuda, oracle):
     """4,194,304-triangle clustered soup with duplicate Morton codes: sort,
     topology and AABBs bit-exact at full size; 1M boundary rays bit-exact."""
     torch = cuda

@@ -59,10 +59,10 @@ def test_stable_argsort_ties_by_index(oracle):
     assert srt.tolist() == sorted(codes.tolist())
 
 
-def test_oracle_snapshot_cfg1(oracle, golden_dir):
+def test_oracle_snapshot_icosphere1280(oracle, golden_dir):
     """The committed oracle result of the 1280-triangle icosphere reproduces
     bit for bit on this machine (x86 and Arm alike)."""
-    g = np.load(golden_dir / "oracle_cfg1.npz")
+    g = np.load(golden_dir / "oracle_icosphere1280_256.npz")
     r = oracle.build(g["tri2vtx"], g["vtx2xyz"])
     for k in ("transform", "tri2morton", "idx2tri", "idx2morton", "bvhnodes", "bvhnode2aabb"):
         assert np.array_equal(np.asarray(r[k]).view(np.uint32), g[k].view(np.uint32)), k
