@@ -1,8 +1,8 @@
 /*
  * oracle.c — CPU restatement of del-msh-cpu's LBVH build and BVH ray cast.
  *
- * TEST INFRASTRUCTURE ONLY (see oracle.h): the checker for the CUDA path and
- * the timed CPU baseline.  Built with -O2 -ffp-contract=off so that every f32
+ * TEST INFRASTRUCTURE ONLY (see oracle.h): what the CUDA path's results are
+ * tested against, and the timed CPU baseline.  Built with -O2 -ffp-contract=off so that every f32
  * expression rounds exactly as the reference's Rust code does.
  */
 #include "oracle.h"

@@ -3,7 +3,7 @@
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the
  * cpu_baseline / reference arm of bench.py may load this library, and only as
- * the checker or the timed CPU baseline.  The product (the CUDA library under
+ * what results are tested against or as the timed CPU baseline.  The product (the CUDA library under
  * del-msh_gb300/) never calls it and has no CPU fallback.
  *
  * Every function names the reference file:line it follows (paths relative to

@@ -3,8 +3,8 @@ and BVH ray cast, ``oracle.c``) and of the reference's own Morton/topology code
 compiled as host C++ (``oracle/_ref``).
 
 TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()``
-and the CPU-baseline / reference arm of ``bench.py``, always as the checker or
-the timed CPU baseline — never by the product path.
+and the CPU-baseline / reference arm of ``bench.py``, always as what results
+are tested against or as the timed CPU baseline — never by the product path.
 """
 from __future__ import annotations
 
