@@ -183,6 +183,24 @@ def test_build_matches_oracle(cuda, oracle, case, want_height):
     assert _status_clear() == 0
 
 
+@pytest.mark.parametrize("want_height", [False, True])
+def test_full_torus_8m_build(cuda, oracle, want_height):
+    """8,388,608-triangle displaced torus: above the cooperative front's
+    capacity, so the separate kernels build it (centroid pass with the fit
+    transform, Morton codes with the digit histograms, the onesweep passes,
+    topology, the refit windows and their crossing branches, or the
+    tree-order climb when the height is asked for); every intermediate and
+    the tree and boxes bit-exact to the oracle."""
+    torch = cuda
+    tri, vtx = W.displaced_torus(2048, seed=1)
+    ref = oracle.build(tri, vtx)
+    got = _build_ex(torch, tri, vtx, want_height)
+    _compare_build(got, ref, tri.shape[0])
+    if want_height:
+        assert got["height"] == oracle.tree_height(ref["bvhnodes"], tri.shape[0])
+    assert _status_clear() == 0
+
+
 def test_build_single_triangle(cuda):
     torch = cuda
     tri = np.array([[0, 1, 2]], np.uint32)
