@@ -190,7 +190,8 @@ def test_full_torus_8m_build(cuda, oracle, want_height):
     transform, Morton codes with the digit histograms, the onesweep passes,
     topology, the refit windows and their crossing branches, or the
     tree-order climb when the height is asked for); every intermediate and
-    the tree and boxes bit-exact to the oracle."""
+    the tree and boxes bit-exact to the oracle, and a deformed frame through
+    the drop-in refit too."""
     torch = cuda
     tri, vtx = W.displaced_torus(2048, seed=1)
     ref = oracle.build(tri, vtx)
@@ -198,6 +199,17 @@ def test_full_torus_8m_build(cuda, oracle, want_height):
     _compare_build(got, ref, tri.shape[0])
     if want_height:
         assert got["height"] == oracle.tree_height(ref["bvhnodes"], tri.shape[0])
+    else:
+        # a deformed frame through the drop-in refit (leaf ranges derived on
+        # the device from bvhnodes alone, then the range queries)
+        from del_msh_gb300.TriMesh3 import torch as TriMesh3
+        v = (vtx + 0.01 * np.sin(np.random.default_rng(2).uniform(0, 6.28, vtx.shape[0]) + 1.0)[:, None])
+        v = v.astype(np.float32)
+        bvh = to_dev(got["bvhnodes"], torch)
+        aabb = torch.empty((2 * tri.shape[0] - 1, 6), dtype=torch.float32, device="cuda:0")
+        TriMesh3.update_bvhnode2aabb(to_dev(tri, torch), to_dev(v, torch), bvh, aabb)
+        want = oracle.bvhnode2aabb(ref["bvhnodes"], tri, v)
+        assert np.array_equal(bits(to_np(aabb, torch)), bits(want))
     assert _status_clear() == 0
 
 
