@@ -31,6 +31,24 @@ __device__ __forceinline__ uint2 block_read_hdr(const uint32_t* w0, const uint32
   return s_words;
 }
 
+// A box written by an earlier kernel and not written in this one, read
+// through L1 (ld.global.ca): the crossing-branch queries of neighbouring
+// branches read mostly the same leaves and segment-tree nodes.  Read after
+// the kernel's dependency wait, which makes the earlier kernels' writes
+// visible to it.
+__device__ __forceinline__ Box box_load_l1(const float* src) {
+  const float2* s2 = reinterpret_cast<const float2*>(src);
+  const float2 a = __ldca(s2), b = __ldca(s2 + 1), c = __ldca(s2 + 2);
+  Box o;
+  o.lo[0] = a.x;
+  o.lo[1] = a.y;
+  o.lo[2] = b.x;
+  o.hi[0] = b.y;
+  o.hi[1] = c.x;
+  o.hi[2] = c.y;
+  return o;
+}
+
 // A box stored by box_store, read through the read-only path.
 __device__ __forceinline__ Box box_load_ro(const float* src) {
   const float2 a = __ldg(reinterpret_cast<const float2*>(src));
@@ -1075,12 +1093,12 @@ __device__ __forceinline__ void refit_cross_group(uint32_t g, uint32_t sub, uint
     pr[q] = (act && (rj & 1u)) ? seg_node(v, 3 + j, rj - 1) : nullptr;
   }
   const Box id = box_identity();
-  Box A = pa ? box_load_cg(pa) : id, B = pb ? box_load_cg(pb) : id;
+  Box A = pa ? box_load_l1(pa) : id, B = pb ? box_load_l1(pb) : id;
   Box bl[4], br[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    bl[q] = pl[q] ? box_load_cg(pl[q]) : id;
-    br[q] = pr[q] ? box_load_cg(pr[q]) : id;
+    bl[q] = pl[q] ? box_load_l1(pl[q]) : id;
+    br[q] = pr[q] ? box_load_l1(pr[q]) : id;
   }
   Box Lp = bl[0], Rp = br[3];
 #pragma unroll
@@ -1127,8 +1145,8 @@ __device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, 
     Box bl[7], br[7];
 #pragma unroll
     for (int q = 0; q < 7; ++q) {
-      bl[q] = box_load_cg(static_cast<uint32_t>(q) < nl ? leaf0 + 6ull * (l + q) : dummy);
-      br[q] = box_load_cg(static_cast<uint32_t>(q) < nr ? leaf0 + 6ull * (r - 1 - q) : dummy);
+      bl[q] = box_load_l1(static_cast<uint32_t>(q) < nl ? leaf0 + 6ull * (l + q) : dummy);
+      br[q] = box_load_l1(static_cast<uint32_t>(q) < nr ? leaf0 + 6ull * (r - 1 - q) : dummy);
     }
 #pragma unroll
     for (int q = 0; q < 7; ++q) {
@@ -1158,8 +1176,8 @@ __device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, 
     Box bl[4], br[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      bl[q] = box_load_cg(pl[q]);
-      br[q] = box_load_cg(pr[q]);
+      bl[q] = box_load_l1(pl[q]);
+      br[q] = box_load_l1(pr[q]);
     }
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
