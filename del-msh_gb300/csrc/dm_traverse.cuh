@@ -681,6 +681,8 @@ __device__ __forceinline__ int phase_inner_warp(const MeshView& m, const Ray& r,
   return phase_inner(m, r, stack, cap, s, bad);
 }
 
+constexpr uint32_t kChainPrefetch = 2;  // chunks of links prefetched ahead of the fold
+
 // Fold frames {c0 | bit, c1 | bit, saved}: the tail's result (the current
 // one) is folded through the chain, and the chain's result into `saved`.
 struct ChainFold {
@@ -693,8 +695,21 @@ struct ChainFold {
     const uint32_t c0 = f.x & ~kChainBit, c1 = f.y & ~kChainBit;
     if (c0 > c1 || c1 + 1 >= 2 * m.num_tri - 1) return 2;
     Hit x = s.best;
+    const uint32_t nb = m.num_tri - 1;
     for (uint32_t hi = c1;;) {
       const uint32_t lo = hi - c0 >= 32 * kFoldBatch - 1 ? hi - (32 * kFoldBatch - 1) : c0;
+      // the links of the next kChainPrefetch chunks (lane k: one link each)
+      // toward L2 while this chunk is folded: a long chain's tree does not
+      // fit L2, and each chunk is otherwise a few dependent DRAM round trips
+#pragma unroll
+      for (uint32_t d = 0; d < kChainPrefetch; ++d) {
+        const int64_t j = static_cast<int64_t>(lo) - 1 - lane - 32 * static_cast<int64_t>(d);
+        if (j >= static_cast<int64_t>(c0)) {
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(m.bvhnodes + 3 * (nb + static_cast<uint64_t>(j))));
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(m.aabb + 6 * (nb + static_cast<uint64_t>(j))));
+          asm volatile("prefetch.global.L2 [%0];" ::"l"(m.aabb + 6 * (static_cast<uint64_t>(j) + 1)));
+        }
+      }
       x = fold_links(m, r, lo, hi, x, lane, *bad);
       if (lo == c0) break;
       hi = lo - 1;
