@@ -30,6 +30,15 @@ __device__ __forceinline__ uint2 block_read_hdr(const uint32_t* w0, const uint32
   __syncthreads();
   return s_words;
 }
+__device__ __forceinline__ uint3 block_read_hdr3(const uint32_t* w0, const uint32_t* w1, const uint32_t* w2) {
+  __shared__ uint3 s_words3;
+  if (threadIdx.x == 0)
+    s_words3 = make_uint3(*reinterpret_cast<const volatile uint32_t*>(w0),
+                          *reinterpret_cast<const volatile uint32_t*>(w1),
+                          *reinterpret_cast<const volatile uint32_t*>(w2));
+  __syncthreads();
+  return s_words3;
+}
 
 // A box written by an earlier kernel and not written in this one, read
 // through L1 (ld.global.ca): the crossing-branch queries of neighbouring
@@ -818,8 +827,9 @@ __device__ __forceinline__ uint32_t mesh_from(const Segments& seg, uint32_t m0, 
 constexpr int kSegWinSmem = static_cast<int>(2 * kRefitWindow * sizeof(Box));
 
 // Window kernel: leaf boxes, the window heap, and every branch whose range
-// lies inside the window.
-template <bool kBatch>
+// lies inside the window.  kRuns (one mesh only): set aside the run branches
+// for refit_runs (below).
+template <bool kBatch, bool kRuns>
 __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tri, Segments seg,
                                                               uint32_t num_vtx_single,
                                                               const uint32_t* __restrict__ bvhnodes_all,
@@ -832,9 +842,11 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
                                                               const uint32_t* __restrict__ leaf_tri) {
   extern __shared__ __align__(16) unsigned char seg_raw[];
   Box* tree = reinterpret_cast<Box*>(seg_raw);  // 2 * kRefitWindow boxes
-  __shared__ uint32_t s_mesh, s_flag;
+  __shared__ uint32_t s_mesh, s_flag, s_bstar, s_runs;
   const uint32_t wA = blockIdx.x * kRefitWindow;
+  static_assert(!(kBatch && kRuns), "run branches are set aside for one mesh only");
   if (threadIdx.x == 0) {
+    if (kRuns) s_runs = 0u;
     // another block may raise the flag meanwhile: read it once for the block
     s_flag = *reinterpret_cast<volatile uint32_t*>(hdr + 1);
     if (kBatch) s_mesh = mesh_of_leaf(seg, wA);
@@ -866,6 +878,19 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
                                    : __ldg(bvhnodes_all + 3 * (2ull * lm[r].t0 - lm[r].m + lm[r].T - 1 + n) + 1);
     if (n + 1 < lm[r].T) oth[r] = __ldg(other_all + (static_cast<size_t>(lm[r].t0) - lm[r].m) + n);
   }
+  if (kRuns && threadIdx.x == kWinThreads - 1) {
+    // the window's last branch, when its range starts inside the window and
+    // ends beyond it: its right end b* is shared by every branch of a run of
+    // equal codes that crosses the right edge
+    constexpr int rl = kWinPerThread - 1;
+    const uint32_t g = wA + kRefitWindow - 1;
+    uint32_t bstar = kUMax;
+    if (oth[rl] != kUMax) {
+      const uint32_t lo = g < oth[rl] ? g : oth[rl], hi = g < oth[rl] ? oth[rl] : g;
+      if (lo >= wA && hi > g && hi < total_tri) bstar = hi;
+    }
+    s_bstar = bstar;
+  }
   bool nan = false;
 #pragma unroll
   for (int r = 0; r < kWinPerThread; ++r) {
@@ -892,6 +917,24 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
     if (threadIdx.x == 0) atomicOr(hdr + 1, 1u);  // hand the whole call to the climb
     return;
   }
+  // Run branches: ranges [a, b*] with a inside the window (chain links of a
+  // run of equal codes crossing the right edge).  When the window holds at
+  // least kRefitRunMin of them, each gets its in-window part fold(a .. wEnd)
+  // below and refit_runs folds in the shared fold(wEnd + 1 .. b*) once per
+  // window; the window's heap slot 0 (otherwise unused) tells it b*.  Counted
+  // here; the heap build's barriers order the count before its use.
+  uint32_t run_mask = 0u;
+  if (kRuns && s_bstar != kUMax) {
+    const uint32_t bstar = s_bstar;
+#pragma unroll
+    for (int r = 0; r < kWinPerThread; ++r) {
+      const uint32_t g = wA + threadIdx.x + r * kWinThreads;
+      const bool run = oth[r] != kUMax && (g < oth[r] ? g : oth[r]) >= wA && (g < oth[r] ? oth[r] : g) == bstar;
+      if (run) run_mask |= 1u << r;
+      const uint32_t bal = __ballot_sync(0xffffffffu, run);
+      if ((threadIdx.x & 31u) == 0u && bal != 0u) atomicAdd(&s_runs, static_cast<uint32_t>(__popc(bal)));
+    }
+  }
   // heap levels of 64 .. kRefitWindow / 2 nodes by the block, the top six
   // levels (32 .. 1 nodes) by warp 0 alone
 #pragma unroll 1
@@ -913,6 +956,11 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
     heap_node(threadIdx.x, kRefitWindowLog, lvl, j);
     if (node_inside(wA, lvl, j, total_tri)) box_store(wseg + 6 * (static_cast<size_t>(blockIdx.x) * kRefitWinHeap + threadIdx.x), tree[threadIdx.x]);
   }
+  const bool runs = kRuns && s_bstar != kUMax && s_runs >= kRefitRunMin;
+  if (kRuns && threadIdx.x == 0) {
+    *reinterpret_cast<uint32_t*>(wseg + 6 * static_cast<size_t>(blockIdx.x) * kRefitWinHeap) = runs ? s_bstar : kUMax;
+    if (runs) atomicOr(hdr + 4, 1u);  // refit_runs has work
+  }
 #pragma unroll
   for (int r = 0; r < kWinPerThread; ++r) {
     if (oth[r] == kUMax) continue;
@@ -923,6 +971,18 @@ __global__ void __launch_bounds__(kWinThreads) k_refit_seg_win(uint32_t total_tr
       continue;
     }
     const uint32_t a = lm[r].t0 + lo, b = lm[r].t0 + hi;
+    if (runs && (run_mask >> r & 1u)) {  // in-window part [a, wEnd]
+      uint32_t l = a - wA + kRefitWindow, rr = 2 * kRefitWindow;
+      Box L = box_identity(), R = box_identity();
+      while (l < rr) {
+        if (l & 1u) L = box_union(L, tree[l++]);
+        if (rr & 1u) R = box_union(tree[--rr], R);
+        l >>= 1;
+        rr >>= 1;
+      }
+      box_store(aabb_all + 6 * static_cast<size_t>(n), box_union(L, R));
+      continue;
+    }
     if ((a >> kRefitWindowLog) != (b >> kRefitWindowLog)) {
       // crossing: listed for k_refit_seg_cross in the (zero) arrival
       // counters, which that kernel clears again as it reads them
@@ -1113,31 +1173,10 @@ __device__ __forceinline__ void refit_cross_group(uint32_t g, uint32_t sub, uint
   if (sub == 0) box_store(aabb_all + 6 * (2ull * t0 - m + n), box_union(box_union(A, Lp), box_union(Rp, B)));
 }
 
-// One thread per branch: the same query walked level by level, its loads
+// Fold of the leaf boxes at global positions [l, r) through the segment tree
+// (leaf0 + 6 p: the box of the leaf at position p), one thread, its loads
 // issued four levels at a time.
-template <bool kBatch>
-__device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, const Segments& seg,
-                                                const uint32_t* __restrict__ other_all, float* aabb_all,
-                                                const SegView& v, uint32_t* status) {
-  uint32_t m = 0, t0 = 0, T = total_tri;
-  if (kBatch) {
-    m = mesh_of_leaf(seg, g);
-    t0 = __ldg(seg.tri_off + m);
-    T = __ldg(seg.tri_off + m + 1) - t0;
-  }
-  const uint32_t n = g - t0;
-  if (g < t0 || n + 1 >= T) {
-    raise_status(status, kStatusBadIndex);
-    return;
-  }
-  const uint32_t oth = __ldg(other_all + (static_cast<size_t>(t0) - m) + n);
-  const uint32_t lo = n < oth ? n : oth, hi = n < oth ? oth : n;
-  if (hi >= T) {
-    raise_status(status, kStatusBadIndex);
-    return;
-  }
-  uint32_t l = t0 + lo, r = t0 + hi + 1;
-  const float* leaf0 = aabb_all + 6 * (2ull * t0 - m + T - 1) - 6ull * t0;  // + 6*p: leaf of global position p
+__device__ __forceinline__ Box seg_fold(const float* leaf0, uint32_t l, uint32_t r, const SegView& v) {
   const float* dummy = leaf0 + 6ull * l;
   Box L = box_identity(), R = box_identity();
   {  // ragged ends: up to 7 leaves on each side
@@ -1185,7 +1224,77 @@ __device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, 
       if (tr[q]) R = box_union(br[q], R);
     }
   }
-  box_store(aabb_all + 6 * (2ull * t0 - m + n), box_union(L, R));
+  return box_union(L, R);
+}
+
+// One thread per branch: the query of its leaf range by seg_fold.
+template <bool kBatch>
+__device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, const Segments& seg,
+                                                const uint32_t* __restrict__ other_all, float* aabb_all,
+                                                const SegView& v, uint32_t* status) {
+  uint32_t m = 0, t0 = 0, T = total_tri;
+  if (kBatch) {
+    m = mesh_of_leaf(seg, g);
+    t0 = __ldg(seg.tri_off + m);
+    T = __ldg(seg.tri_off + m + 1) - t0;
+  }
+  const uint32_t n = g - t0;
+  if (g < t0 || n + 1 >= T) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  const uint32_t oth = __ldg(other_all + (static_cast<size_t>(t0) - m) + n);
+  const uint32_t lo = n < oth ? n : oth, hi = n < oth ? oth : n;
+  if (hi >= T) {
+    raise_status(status, kStatusBadIndex);
+    return;
+  }
+  const float* leaf0 = aabb_all + 6 * (2ull * t0 - m + T - 1) - 6ull * t0;  // + 6*p: leaf of global position p
+  box_store(aabb_all + 6 * (2ull * t0 - m + n), seg_fold(leaf0, t0 + lo, t0 + hi + 1, v));
+}
+
+
+// The run branches the window kernel set aside, a window per warp: its heap
+// slot 0 holds b*, or kUMax when the window had too few of them (header word
+// 4 says whether any window has them).  Lane 0 folds the leaves wEnd + 1 ..
+// b* once and the warp unions that into the in-window part each run branch
+// holds: union(fold(a .. wEnd), fold(wEnd + 1 .. b*)) is fold(a .. b*), the
+// leftmost extreme in leaf order.  The branches are found by the window
+// kernel's own test on other_end.  Run by the one-thread crossing kernel,
+// which then also takes the list; one mesh only.
+__device__ __forceinline__ void refit_runs(uint32_t total_tri, const uint32_t* __restrict__ other_end, float* aabb,
+                                           const SegView& v, uint32_t* status) {
+  const uint32_t windows = (total_tri + kRefitWindow - 1) >> kRefitWindowLog;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < windows; w += nwarps) {
+    const uint32_t wA = w * kRefitWindow, wEnd = wA + kRefitWindow - 1;
+    uint32_t bstar = kUMax;
+    if (lane == 0) bstar = __ldcg(reinterpret_cast<const uint32_t*>(v.wseg + 6 * static_cast<size_t>(w) * kRefitWinHeap));
+    bstar = __shfl_sync(0xffffffffu, bstar, 0);
+    if (bstar == kUMax) continue;
+    if (bstar <= wEnd || bstar >= total_tri) {
+      if (lane == 0) raise_status(status, kStatusBadIndex);
+      continue;
+    }
+    Box right = box_identity();
+    if (lane == 0) right = seg_fold(aabb + 6ull * (total_tri - 1), wEnd + 1, bstar + 1, v);
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      right.lo[d] = __shfl_sync(0xffffffffu, right.lo[d], 0);
+      right.hi[d] = __shfl_sync(0xffffffffu, right.hi[d], 0);
+    }
+    for (uint32_t k = lane; k < kRefitWindow; k += 32) {
+      const uint32_t g = wA + k;
+      if (g + 1 >= total_tri) break;  // branches are 0 .. total_tri - 2
+      const uint32_t oth = __ldg(other_end + g);
+      const uint32_t lo = g < oth ? g : oth, hi = g < oth ? oth : g;
+      if (lo >= wA && hi == bstar) {
+        float* dst = aabb + 6ull * g;
+        box_store(dst, box_union(box_load_cg(dst), right));
+      }
+    }
+  }
 }
 
 // Branches whose range crosses a window edge, from the list the window kernel
@@ -1194,9 +1303,11 @@ __device__ __forceinline__ void refit_cross_one(uint32_t g, uint32_t total_tri, 
 // (k_refit_seg_cross_groups, refit_cross_group), which cuts the latency of
 // each query; a long one (runs of equal codes across many windows) one
 // thread per branch (k_refit_seg_cross_threads, refit_cross_one), which costs
-// fewer instructions in all.  Every list entry read is cleared, also when the
+// fewer instructions in all.  When a window set run branches aside (header
+// word 4), the one-thread kernel takes the call whatever the list's length
+// and runs refit_runs first.  Every list entry read is cleared, also when the
 // climb took over.
-template <bool kBatch>
+template <bool kBatch, bool kRuns>
 __global__ void __launch_bounds__(256, 4) k_refit_seg_cross_groups(uint32_t total_tri, Segments seg,
                                                                    const uint32_t* __restrict__ other_all,
                                                                    float* aabb_all, const uint32_t* hdr,
@@ -1204,11 +1315,17 @@ __global__ void __launch_bounds__(256, 4) k_refit_seg_cross_groups(uint32_t tota
                                                                    uint32_t* status) {
   pdl_wait();
   pdl_launch_dependents();
-  const uint2 h = block_read_hdr(hdr + 1, hdr + 3);
+  uint3 h;  // climb flag, list length, runs present (kRuns only)
+  if constexpr (kRuns) {
+    h = block_read_hdr3(hdr + 1, hdr + 3, hdr + 4);
+  } else {
+    const uint2 h2 = block_read_hdr(hdr + 1, hdr + 3);
+    h = make_uint3(h2.x, h2.y, 0u);
+  }
   const bool climb = h.x != 0u;
   uint32_t count = h.y;
   if (count > total_tri) count = total_tri;
-  if (count > groups) return;  // the one-thread kernel takes it
+  if (count > groups || h.z != 0u) return;  // the one-thread kernel takes it
   const uint32_t sub = threadIdx.x & 7u;
   const uint32_t mask = 0xffu << (threadIdx.x & 24u);  // the group's lanes in the warp
   const uint32_t stride = (gridDim.x * blockDim.x) >> 3;
@@ -1225,7 +1342,7 @@ __global__ void __launch_bounds__(256, 4) k_refit_seg_cross_groups(uint32_t tota
   }
 }
 
-template <bool kBatch>
+template <bool kBatch, bool kRuns>
 __global__ void __launch_bounds__(256) k_refit_seg_cross_threads(uint32_t total_tri, Segments seg,
                                                                  const uint32_t* __restrict__ other_all,
                                                                  float* aabb_all, const uint32_t* hdr,
@@ -1233,11 +1350,18 @@ __global__ void __launch_bounds__(256) k_refit_seg_cross_threads(uint32_t total_
                                                                  uint32_t* status) {
   pdl_wait();
   pdl_launch_dependents();
-  const uint2 h = block_read_hdr(hdr + 1, hdr + 3);
+  uint3 h;  // climb flag, list length, runs present (kRuns only)
+  if constexpr (kRuns) {
+    h = block_read_hdr3(hdr + 1, hdr + 3, hdr + 4);
+  } else {
+    const uint2 h2 = block_read_hdr(hdr + 1, hdr + 3);
+    h = make_uint3(h2.x, h2.y, 0u);
+  }
   const bool climb = h.x != 0u;
   uint32_t count = h.y;
   if (count > total_tri) count = total_tri;
-  if (count <= groups) return;  // the 8-lane kernel took it
+  if (count <= groups && h.z == 0u) return;  // the 8-lane kernel took it
+  if (kRuns && !climb && h.z != 0u) refit_runs(total_tri, other_all, aabb_all, v, status);
   for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < count; e += gridDim.x * blockDim.x) {
     const uint32_t entry = cross_list[e];
     cross_list[e] = 0u;
@@ -1328,8 +1452,9 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   if (dev >= 0 && dev < 64 && !configured[dev]) {
     cudaFuncSetAttribute(k_refit_win<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     cudaFuncSetAttribute(k_refit_win<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    cudaFuncSetAttribute(k_refit_seg_win<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSegWinSmem);
-    cudaFuncSetAttribute(k_refit_seg_win<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSegWinSmem);
+    cudaFuncSetAttribute(k_refit_seg_win<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSegWinSmem);
+    cudaFuncSetAttribute(k_refit_seg_win<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSegWinSmem);
+    cudaFuncSetAttribute(k_refit_seg_win<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, kSegWinSmem);
     cudaDeviceGetAttribute(&sm_count[dev], cudaDevAttrMultiProcessorCount, dev);
     configured[dev] = true;
   }
@@ -1348,27 +1473,40 @@ void launch_refit_windowed(cudaStream_t s, uint32_t total_tri, const Segments& s
   float* sseg = const_cast<float*>(v.sseg);
   float* tseg = const_cast<float*>(v.tseg);
   if (seg.tri_off) {
-    k_refit_seg_win<true><<<windows, kWinThreads, kSegWinSmem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
+    k_refit_seg_win<true, false><<<windows, kWinThreads, kSegWinSmem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end, tri2vtx,
                                                           vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg, status,
                                                           nullptr, nullptr);
     launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
-    launch_pdl(k_refit_seg_cross_groups<true>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb,
+    launch_pdl(k_refit_seg_cross_groups<true, false>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb,
                queue, flags, v, cross_groups, status);
-    launch_pdl(k_refit_seg_cross_threads<true>, dim3(cross_grid1), dim3(256), 0, s, total_tri, seg, other_end, aabb,
+    launch_pdl(k_refit_seg_cross_threads<true, false>, dim3(cross_grid1), dim3(256), 0, s, total_tri, seg, other_end, aabb,
                queue, flags, v, cross_groups, status);
     launch_pdl(k_refit_win<true>, dim3(climb_grid), dim3(kWinThreads), smem, s, total_tri, seg, num_vtx_single,
                bvhnodes, other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out, status);
     launch_pdl(k_refit_top<true>, dim3(top_grid), dim3(128), 0, s, total_tri, seg, bvhnodes, aabb, flags, queue,
                capacity, height_out, status);
   } else {
-    k_refit_seg_win<false><<<windows, kWinThreads, kSegWinSmem, s>>>(total_tri, seg, num_vtx_single, bvhnodes, other_end,
-                                                           tri2vtx, vtx2xyz0, vtx2xyz1, aabb, queue, flags, wseg,
-                                                           status, tribox, leaf_tri);
-    launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
-    launch_pdl(k_refit_seg_cross_groups<false>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end, aabb,
-               queue, flags, v, cross_groups, status);
-    launch_pdl(k_refit_seg_cross_threads<false>, dim3(cross_grid1), dim3(256), 0, s, total_tri, seg, other_end, aabb,
-               queue, flags, v, cross_groups, status);
+    // run branches are set aside for soups (the meshes with stored triangle
+    // boxes), whose clusters make runs of equal codes across windows
+    if (tribox) {
+      k_refit_seg_win<false, true><<<windows, kWinThreads, kSegWinSmem, s>>>(total_tri, seg, num_vtx_single, bvhnodes,
+                                                                      other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb,
+                                                                      queue, flags, wseg, status, tribox, leaf_tri);
+      launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
+      launch_pdl(k_refit_seg_cross_groups<false, true>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end,
+                 aabb, queue, flags, v, cross_groups, status);
+      launch_pdl(k_refit_seg_cross_threads<false, true>, dim3(cross_grid1), dim3(256), 0, s, total_tri, seg, other_end,
+                 aabb, queue, flags, v, cross_groups, status);
+    } else {
+      k_refit_seg_win<false, false><<<windows, kWinThreads, kSegWinSmem, s>>>(total_tri, seg, num_vtx_single, bvhnodes,
+                                                                       other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb,
+                                                                       queue, flags, wseg, status, nullptr, leaf_tri);
+      launch_pdl(k_refit_seg_super, dim3(supers), dim3(256), 0, s, total_tri, queue, wseg, sseg, tseg, top_log);
+      launch_pdl(k_refit_seg_cross_groups<false, false>, dim3(cross_grid), dim3(256), 0, s, total_tri, seg, other_end,
+                 aabb, queue, flags, v, cross_groups, status);
+      launch_pdl(k_refit_seg_cross_threads<false, false>, dim3(cross_grid1), dim3(256), 0, s, total_tri, seg,
+                 other_end, aabb, queue, flags, v, cross_groups, status);
+    }
     launch_pdl(k_refit_win<false>, dim3(climb_grid), dim3(kWinThreads), smem, s, total_tri, seg, num_vtx_single,
                bvhnodes, other_end, tri2vtx, vtx2xyz0, vtx2xyz1, aabb, flags, queue, capacity, height_out, status);
     launch_pdl(k_refit_top<false>, dim3(top_grid), dim3(128), 0, s, total_tri, seg, bvhnodes, aabb, flags, queue,
