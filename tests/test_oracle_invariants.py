@@ -112,3 +112,60 @@ def test_chain_link_boxes_are_suffix_unions(oracle):
     hi = np.where(b[:, 3:] > a[:, 3:], b[:, 3:], a[:, 3:])
     want = np.concatenate([lo, hi], axis=1)
     assert np.array_equal(box[j].view(np.uint32), want.astype(np.float32).view(np.uint32))
+
+
+def _leftmost_fold(leaves):
+    """Fold of boxes [n, 6] with the refit's union (keep the running box's
+    component unless the next one is strictly smaller / larger): per
+    component, the first leaf that attains the extreme, its bits included."""
+    lo, hi = leaves[:, :3], leaves[:, 3:]
+    first_lo = np.argmax(lo == lo.min(axis=0), axis=0)
+    first_hi = np.argmax(hi == hi.max(axis=0), axis=0)
+    return np.concatenate([lo[first_lo, np.arange(3)], hi[first_hi, np.arange(3)]])
+
+
+def test_run_branches_split_at_a_window_edge(oracle):
+    """The identity the refit's run path rests on (1024-leaf windows, as the
+    kernels use): where a run of equal codes crosses a window's right edge,
+    the window's last branch ends at the run's end b*, and every branch whose
+    range [a, b*] starts inside that window has the box union(fold(a ..
+    wEnd), fold(wEnd + 1 .. b*)) in leaf order, bit for bit (-0/+0 ties
+    included), as the oracle's recursion computes it."""
+    tri, vtx = W.clustered_soup(60_000, num_cluster=4, seed=2)
+    r = oracle.build(tri, vtx)
+    bvh, box = r["bvhnodes"].astype(np.int64), r["bvhnode2aabb"]
+    T = tri.shape[0]
+    # leaf range of every node, children before parents (explicit post-order)
+    lo, hi = np.zeros(2 * T - 1, np.int64), np.zeros(2 * T - 1, np.int64)
+    lo[T - 1:] = hi[T - 1:] = np.arange(T)
+    stack, order = [0], []
+    while stack:
+        n = stack.pop()
+        order.append(n)
+        if n < T - 1:
+            stack += [int(bvh[n, 1]), int(bvh[n, 2])]
+    for n in reversed(order):
+        if n < T - 1:
+            c0, c1 = bvh[n, 1], bvh[n, 2]
+            lo[n], hi[n] = min(lo[c0], lo[c1]), max(hi[c0], hi[c1])
+    leaves = box[T - 1:]
+    win, checked, windows_with_runs = 1024, 0, 0
+    for w0 in range(0, T - 1, win):
+        w_end = w0 + win - 1
+        if w_end >= T - 1:
+            break
+        if not (lo[w_end] >= w0 and hi[w_end] > w_end):
+            continue
+        bstar = hi[w_end]
+        g = np.arange(w0, w_end + 1)
+        run = g[(lo[g] >= w0) & (hi[g] == bstar)]
+        if run.size < 64:
+            continue
+        windows_with_runs += 1
+        right = _leftmost_fold(leaves[w_end + 1:bstar + 1])
+        for n in run:
+            left = _leftmost_fold(leaves[lo[n]:w_end + 1])
+            both = _leftmost_fold(np.stack([left, right]))
+            assert np.array_equal(box[n].view(np.uint32), both.astype(np.float32).view(np.uint32)), (w0, n)
+            checked += 1
+    assert windows_with_runs >= 8 and checked >= 512
