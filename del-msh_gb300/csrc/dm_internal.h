@@ -85,10 +85,10 @@ struct Segments {
 constexpr uint32_t kRefitWindowLog = 10;
 constexpr uint32_t kRefitWindow = 1u << kRefitWindowLog;  // leaves per window
 constexpr uint32_t kRefitWinHeap = kRefitWindow / 4;      // stored window heap: nodes of 8.. leaves, index 1..
-constexpr uint32_t kRefitSuper = 64;
+constexpr uint32_t kRefitSuper = 64;                      // windows per superblock
 // a window whose right edge is crossed by at least this many branches with a
 // shared right end (a run of equal codes) folds that end once for all of them
-constexpr uint32_t kRefitRunMin = 64;                      // windows per superblock
+constexpr uint32_t kRefitRunMin = 64;
 constexpr uint32_t kRefitSuperLog = kRefitWindowLog + 6;  // log2(kRefitWindow * kRefitSuper)
 constexpr uint32_t kRefitQueueHdr = 8;      // queue count, climb flag, ticket, crossing-list count, runs present, spare
 // climb-flag bit: the tree is not in Karras leaf order (or could not be
